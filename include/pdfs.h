@@ -1,0 +1,145 @@
+/*
+ * pdfs.h -- C ABI of the GB300 Fast Sweeping Method solver (libpdfs.so).
+ *
+ * Drop-in for the FSM solve of GEM3D/PDFS.  Plain C types only: pointers,
+ * sizes, ints and doubles.  No function calls exit(); every entry point
+ * returns a status code (PDFS_OK = 0, negative on failure).
+ *
+ * Field layout everywhere in this ABI is the reference's: a halo-padded
+ * array of (nx+2)*(ny+2)*(nz+2) doubles, x fastest, then y, then z
+ * (single_gpu_cuda/src/phi3D.c:66-68, mpi_openacc/src/phi3D_fsm.c:86-112).
+ * Interior nodes have 1-based coordinates; halo values are read, never written.
+ */
+#ifndef PDFS_H
+#define PDFS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define PDFS_OK 0
+#define PDFS_ERR_INVALID (-1)       /* bad argument (sizes, spacings, options)      */
+#define PDFS_ERR_OOM (-2)           /* device or pinned host allocation failed      */
+#define PDFS_ERR_CUDA (-3)          /* a CUDA runtime call failed                   */
+#define PDFS_ERR_TIMEOUT (-4)       /* a bounded inter-tile wait gave up            */
+#define PDFS_ERR_NOT_CONVERGED (-5) /* max_sweeps reached before the tolerance      */
+#define PDFS_ERR_IO (-6)            /* file could not be read or written            */
+#define PDFS_ERR_NO_DEVICE (-7)     /* no CUDA device (the library never falls back) */
+
+/* ---- problem description ----------------------------------------------------- */
+typedef struct {
+  int nx, ny, nz;    /* interior nodes per axis (>= 1)        */
+  double dx, dy, dz; /* node spacings (> 0)                   */
+} pdfs_grid;
+
+/* Arithmetic of the sweeps. */
+enum {
+  PDFS_PREC_FP64 = 0,          /* every sweep in FP64                                        */
+  PDFS_PREC_FP32 = 1,          /* FP32 sweeps to an exact FP32 fixed point, widened to FP64   */
+  PDFS_PREC_FP32_POLISH64 = 2, /* FP32 bulk sweeps, then FP64 replace-update polish sweeps    */
+};
+
+/* FP64 local-solver arithmetic. */
+enum {
+  PDFS_ARITH_REFERENCE = 0, /* the reference's expression trees, no fused multiply-add:
+                               bit-identical to phi3D_fsm.c compiled with -ffp-contract=off */
+  PDFS_ARITH_FAST = 1,      /* shifted quadratic with fused multiply-add (about 1e-15 rel.)  */
+};
+
+/* Which nodes are updated. */
+enum {
+  PDFS_FREEZE_NONE = 0, /* every interior node is min-updated, as the reference does        */
+  PDFS_FREEZE_MASK = 1, /* nodes with frozen[i] != 0 keep their input value                 */
+};
+
+/* Active-block scheduling of the sweeps (8^3 node blocks). */
+enum {
+  PDFS_SCHED_NONE = 0,    /* every sweep visits every block                               */
+  PDFS_SCHED_CHANGE = 1,  /* visit blocks that changed, or touch a block that changed,
+                             in the previous two sweeps                                   */
+  PDFS_SCHED_LEARNED = 2, /* visit blocks the MLP predicts will change                    */
+};
+/* Whatever the scheduler, a solve only terminates after a sweep that visits
+ * every block and changes nothing (FP32) or less than tol (FP64). */
+
+typedef struct {
+  int precision;         /* PDFS_PREC_*                                           */
+  int arith;             /* PDFS_ARITH_* (FP64 sweeps)                            */
+  int freeze;            /* PDFS_FREEZE_*                                         */
+  int scheduler;         /* PDFS_SCHED_*                                          */
+  double tol;            /* FP64 convergence: stop at a full sweep whose max
+                            |u_new - u_old| <= tol                                */
+  int max_sweeps;        /* bound on sweeps of each phase (0 = 100000)             */
+  int fixed_sweeps;      /* > 0: run exactly this many sweeps, orderings 1,2,..,8,1,..
+                            with no convergence test (run_fsm semantics)          */
+  int first_ordering;    /* 1..8: ordering of the first sweep (0 = 1)               */
+  int tile;              /* sweep tile variant (0 = autotuned choice)               */
+  int device;            /* CUDA device ordinal                                   */
+  const float *mlp_weights; /* PDFS_SCHED_LEARNED: packed bf16-exact FP32 weights,
+                               NULL = the weights compiled into the library        */
+  long long spin_limit;  /* bound on polls of an inter-tile wait (0 = default)       */
+  int verbose;           /* 0 quiet, 1 per-phase summary on stderr                 */
+  int reserved[8];
+} pdfs_opts;
+
+typedef struct {
+  int status;
+  int sweeps_fp32;            /* FP32 sweeps run                                    */
+  int sweeps_fp64;            /* FP64 sweeps run                                    */
+  int full_sweeps;            /* sweeps that visited every block                    */
+  long long voxel_updates;    /* node updates executed (skipped blocks excluded)   */
+  long long blocks_skipped;   /* 8^3 blocks skipped by the scheduler, all sweeps   */
+  double final_change;        /* max change of the last sweep                       */
+  double ms_total;            /* wall time of the call                              */
+  double ms_h2d, ms_d2h;      /* host<->device copies (host pointers only)          */
+  double ms_fp32, ms_fp64;    /* device time of the two sweep phases                */
+  double ms_sched;            /* device time of scheduler inference                 */
+  int tile;                   /* tile variant used                                  */
+  int reserved[7];
+} pdfs_stats;
+
+/* Fills *o with the defaults: FP64, reference arithmetic, no freezing, no
+ * scheduler, tol = 0 (exact fixed point), device 0. */
+void pdfs_default_opts(pdfs_opts *o);
+
+/* Solves |grad u| = 1 on the grid, in place.  field and frozen may be host
+ * or device pointers (frozen may be NULL; it is read only with
+ * PDFS_FREEZE_MASK).  Replaces run_fsm (single_gpu_cuda/src/phi3D_fsm.cu:64-106)
+ * with a convergent, status-returning call. */
+int pdfs_solve(const pdfs_grid *g, double *field, const uint8_t *frozen, const pdfs_opts *o,
+               pdfs_stats *stats);
+
+/* One ordering sn (1..8) of the plain FSM, in place: the GPU counterpart of
+ * runFSM(pf, sn) (mpi_openacc/src/phi3D_fsm.c:67).  *max_change (nullable)
+ * receives the sweep's max |u_new - u_old|.  o may be NULL (FP64 reference
+ * arithmetic). */
+int pdfs_sweep(const pdfs_grid *g, double *field, const uint8_t *frozen, int sn, const pdfs_opts *o,
+               double *max_change);
+
+/* ---- device-resident context ----------------------------------------------------
+ * A context owns the device buffers of one grid so repeated solves re-use
+ * them.  pdfs_solve() is create + load + run + store + destroy. */
+typedef struct pdfs_ctx pdfs_ctx;
+
+int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o, pdfs_ctx **out);
+/* Copies the input field (and mask) into the context; host or device pointers. */
+int pdfs_ctx_load(pdfs_ctx *c, const double *field, const uint8_t *frozen);
+/* Solves from the loaded input; the input stays resident, so it can be re-run. */
+int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats);
+/* Copies the solution into field (host or device pointer, reference layout). */
+int pdfs_ctx_store(pdfs_ctx *c, double *field);
+void pdfs_ctx_destroy(pdfs_ctx *c);
+
+/* Human-readable text of a status code (static storage). */
+const char *pdfs_status_string(int status);
+/* Library version string. */
+const char *pdfs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDFS_H */

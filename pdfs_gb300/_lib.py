@@ -1,0 +1,90 @@
+"""ctypes binding of libpdfs.so (include/pdfs.h).  No fallback: if the CUDA
+library cannot be loaded, every call raises."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libpdfs.so")
+
+PDFS_OK = 0
+PDFS_ERR_INVALID = -1
+PDFS_ERR_OOM = -2
+PDFS_ERR_CUDA = -3
+PDFS_ERR_TIMEOUT = -4
+PDFS_ERR_NOT_CONVERGED = -5
+PDFS_ERR_IO = -6
+PDFS_ERR_NO_DEVICE = -7
+
+PREC_FP64, PREC_FP32, PREC_FP32_POLISH64 = 0, 1, 2
+ARITH_REFERENCE, ARITH_FAST = 0, 1
+FREEZE_NONE, FREEZE_MASK = 0, 1
+SCHED_NONE, SCHED_CHANGE, SCHED_LEARNED = 0, 1, 2
+
+# Every function declared in include/pdfs.h (the CPU tests check the exports).
+EXPORTS = [
+    "pdfs_default_opts", "pdfs_solve", "pdfs_sweep", "pdfs_ctx_create", "pdfs_ctx_load", "pdfs_ctx_run",
+    "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_status_string", "pdfs_version",
+]
+
+
+class Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double)]
+
+
+class Opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("arith", C.c_int), ("freeze", C.c_int), ("scheduler", C.c_int),
+                ("tol", C.c_double), ("max_sweeps", C.c_int), ("fixed_sweeps", C.c_int),
+                ("first_ordering", C.c_int), ("tile", C.c_int), ("device", C.c_int),
+                ("mlp_weights", C.c_void_p), ("spin_limit", C.c_longlong), ("verbose", C.c_int),
+                ("reserved", C.c_int * 8)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("status", C.c_int), ("sweeps_fp32", C.c_int), ("sweeps_fp64", C.c_int),
+                ("full_sweeps", C.c_int), ("voxel_updates", C.c_longlong), ("blocks_skipped", C.c_longlong),
+                ("final_change", C.c_double), ("ms_total", C.c_double), ("ms_h2d", C.c_double),
+                ("ms_d2h", C.c_double), ("ms_fp32", C.c_double), ("ms_fp64", C.c_double),
+                ("ms_sched", C.c_double), ("tile", C.c_int), ("reserved", C.c_int * 7)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads libpdfs.so (built in-tree by pdfs_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libpdfs.so not found at {path}: run `python -m pdfs_gb300.build` "
+                           "(the solver has no CPU fallback)")
+    L = C.CDLL(path)
+    vp, ip = C.c_void_p, C.c_int
+    L.pdfs_default_opts.argtypes = [C.POINTER(Opts)]
+    L.pdfs_default_opts.restype = None
+    L.pdfs_solve.argtypes = [C.POINTER(Grid), vp, vp, C.POINTER(Opts), C.POINTER(Stats)]
+    L.pdfs_solve.restype = ip
+    L.pdfs_sweep.argtypes = [C.POINTER(Grid), vp, vp, ip, C.POINTER(Opts), C.POINTER(C.c_double)]
+    L.pdfs_sweep.restype = ip
+    L.pdfs_ctx_create.argtypes = [C.POINTER(Grid), C.POINTER(Opts), C.POINTER(vp)]
+    L.pdfs_ctx_create.restype = ip
+    L.pdfs_ctx_load.argtypes = [vp, vp, vp]
+    L.pdfs_ctx_load.restype = ip
+    L.pdfs_ctx_run.argtypes = [vp, C.POINTER(Stats)]
+    L.pdfs_ctx_run.restype = ip
+    L.pdfs_ctx_store.argtypes = [vp, vp]
+    L.pdfs_ctx_store.restype = ip
+    L.pdfs_ctx_destroy.argtypes = [vp]
+    L.pdfs_ctx_destroy.restype = None
+    L.pdfs_status_string.argtypes = [ip]
+    L.pdfs_status_string.restype = C.c_char_p
+    L.pdfs_version.argtypes = []
+    L.pdfs_version.restype = C.c_char_p
+    _lib = L
+    return L

@@ -1,0 +1,134 @@
+"""Python front end of the GB300 FSM solver (thin layer over the C ABI).
+
+Mirrors the reference's solve entry points: ``sweep(field, spacing, sn)`` is
+runFSM(pf, sn) (mpi_openacc/src/phi3D_fsm.c:67), ``run_fsm(field, spacing,
+rounds)`` is run_fsm(pf, iterations) (single_gpu_cuda/src/phi3D_fsm.cu:64),
+``solve`` iterates to convergence.  Fields are numpy float64 arrays of shape
+(nz+2, ny+2, nx+2) in the reference's halo-padded layout; they are updated in
+place.  Errors raise PdfsError carrying the C status code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class PdfsError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = L.load().pdfs_status_string(status).decode()
+        super().__init__(f"{what}: {msg} ({status})" if what else f"{msg} ({status})")
+
+
+def _grid(field: np.ndarray, spacing) -> L.Grid:
+    if field.ndim != 3:
+        raise ValueError("field must be 3-D (nz+2, ny+2, nx+2)")
+    nz, ny, nx = (s - 2 for s in field.shape)
+    return L.Grid(nx, ny, nz, float(spacing[0]), float(spacing[1]), float(spacing[2]))
+
+
+def _check_field(field):
+    if field.dtype != np.float64 or not field.flags.c_contiguous:
+        raise ValueError("field must be a C-contiguous float64 array")
+
+
+def make_opts(precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, freeze=L.FREEZE_NONE, scheduler=L.SCHED_NONE,
+              tol=0.0, max_sweeps=0, fixed_sweeps=0, first_ordering=0, tile=0, device=0, verbose=0,
+              wait_ms=0) -> L.Opts:
+    o = L.Opts()
+    L.load().pdfs_default_opts(C.byref(o))
+    o.precision, o.arith, o.freeze, o.scheduler = precision, arith, freeze, scheduler
+    o.tol, o.max_sweeps, o.fixed_sweeps, o.first_ordering = tol, max_sweeps, fixed_sweeps, first_ordering
+    o.tile, o.device, o.verbose, o.spin_limit = tile, device, verbose, wait_ms
+    return o
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data if isinstance(a, np.ndarray) else int(a))
+
+
+def solve(field: np.ndarray, spacing, frozen: np.ndarray | None = None, **kw) -> dict:
+    """Solves in place; returns the stats as a dict.  Keyword arguments are
+    the pdfs_opts fields (see make_opts)."""
+    _check_field(field)
+    if frozen is not None:
+        if frozen.shape != field.shape or frozen.dtype != np.uint8:
+            raise ValueError("frozen must be a uint8 array shaped like field")
+        frozen = np.ascontiguousarray(frozen)
+    g = _grid(field, spacing)
+    o = make_opts(**kw)
+    st = L.Stats()
+    s = L.load().pdfs_solve(C.byref(g), _ptr(field), _ptr(frozen), C.byref(o), C.byref(st))
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_solve")
+    return st.as_dict()
+
+
+def sweep(field: np.ndarray, spacing, sn: int, frozen=None, arith=L.ARITH_REFERENCE, freeze=L.FREEZE_NONE,
+          tile=0) -> float:
+    """One ordering sn (1..8) in place; returns the sweep's max change."""
+    _check_field(field)
+    g = _grid(field, spacing)
+    o = make_opts(arith=arith, freeze=freeze, tile=tile)
+    ch = C.c_double(0.0)
+    s = L.load().pdfs_sweep(C.byref(g), _ptr(field), _ptr(frozen), int(sn), C.byref(o), C.byref(ch))
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_sweep")
+    return ch.value
+
+
+def run_fsm(field: np.ndarray, spacing, rounds: int = 1, **kw) -> dict:
+    """`rounds` rounds of the 8 orderings with no convergence test, as the
+    reference's run_fsm(pf, iterations)."""
+    return solve(field, spacing, fixed_sweeps=8 * int(rounds), **kw)
+
+
+class Context:
+    """Device-resident solve context (pdfs_ctx_*)."""
+
+    def __init__(self, nx, ny, nz, spacing, **kw):
+        self._lib = L.load()
+        self.grid = L.Grid(nx, ny, nz, *map(float, spacing))
+        self.opts = make_opts(**kw)
+        h = C.c_void_p()
+        s = self._lib.pdfs_ctx_create(C.byref(self.grid), C.byref(self.opts), C.byref(h))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_ctx_create")
+        self.h = h
+
+    def load(self, field, frozen=None):
+        s = self._lib.pdfs_ctx_load(self.h, _ptr(field), _ptr(frozen))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_ctx_load")
+
+    def run(self) -> dict:
+        st = L.Stats()
+        s = self._lib.pdfs_ctx_run(self.h, C.byref(st))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_ctx_run")
+        return st.as_dict()
+
+    def store(self, field):
+        s = self._lib.pdfs_ctx_store(self.h, _ptr(field))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_ctx_store")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.pdfs_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

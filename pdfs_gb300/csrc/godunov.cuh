@@ -1,0 +1,169 @@
+// godunov.cuh -- device local solvers of |grad u| = 1 (Godunov upwind update).
+//
+// Given the three axis minima m = (min(u[x-1],u[x+1]), min(u[y-1],u[y+1]),
+// min(u[z-1],u[z+1])) and the spacings h, the update is the largest root u of
+//     sum_k max(u - m_k, 0)^2 / h_k^2 = 1,
+// found by sorting the minima and trying 1, 2 then 3 active terms
+// (mpi_openacc/src/phi3D_fsm.c:132-182, single_gpu_cuda/src/phi3D_fsm.cu:249-295).
+//
+// Three variants:
+//   god_ref64  -- the reference's own expanded expression trees, every
+//                 operation an explicitly rounded intrinsic so nothing is fused:
+//                 bit-identical to the reference's C compiled without contraction.
+//   god_fast64 -- FP64, shifted form in the differences a = m1-m0, b = m2-m0.
+//   god32      -- FP32, same shifted form (the expanded form cancels
+//                 catastrophically in FP32 once m is a few hundred cells).
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace pdfs {
+
+template <class T>
+__device__ __forceinline__ void cswap(T &a, T &b) {
+  T t = a;
+  a = b;
+  b = t;
+}
+
+// Per-sweep constants of the local solver.
+struct GodConst64 {
+  double h[3];   // spacings
+  double h2[3];  // squared spacings
+  double q[3];   // 1/h^2
+  double qsum;   // q0+q1+q2
+  double iqsum;  // 1/(q0+q1+q2)
+};
+struct GodConst32 {
+  float h[3];
+  float q[3];
+  float iqsum;
+  float iso_h, iso_2h2, iso_h2;  // isotropic shortcuts
+};
+
+// Reference arithmetic.  The bubble sort of solveEikonal (phi3D_fsm.c:148-159)
+// is the compare-exchange sequence (0,1), (1,2), (0,1) with a strict '>', so
+// ties keep axis order; the squared spacings travel with their minima (they
+// are squared after the sort in the reference, which rounds identically).
+__device__ __forceinline__ double god_ref64(double m0, double m1, double m2, const GodConst64 &k) {
+  double d0 = k.h[0], d1 = k.h[1], d2 = k.h[2];
+  double q0 = k.h2[0], q1 = k.h2[1], q2 = k.h2[2];
+  if (m0 > m1) { cswap(m0, m1); cswap(d0, d1); cswap(q0, q1); }
+  if (m1 > m2) { cswap(m1, m2); cswap(d1, d2); cswap(q1, q2); }
+  if (m0 > m1) { cswap(m0, m1); cswap(d0, d1); cswap(q0, q1); }
+
+  double u = __dadd_rn(m0, d0);  // phi3D_fsm.c:165
+  if (u > m1) {
+    const double m2_0 = __dmul_rn(m0, m0), m2_1 = __dmul_rn(m1, m1);
+    // sqrt(-m2_0 + 2*m0*m1 - m2_1 + d2_0 + d2_1), left to right (phi3D_fsm.c:167)
+    double t = __dadd_rn(-m2_0, __dmul_rn(__dmul_rn(2.0, m0), m1));
+    t = __dsub_rn(t, m2_1);
+    t = __dadd_rn(t, q0);
+    t = __dadd_rn(t, q1);
+    const double s = __dsqrt_rn(t);
+    // (m1*d2_0 + m0*d2_1 + d0*d1*s) / (d2_0 + d2_1)  (phi3D_fsm.c:168)
+    double num = __dadd_rn(__dadd_rn(__dmul_rn(m1, q0), __dmul_rn(m0, q1)), __dmul_rn(__dmul_rn(d0, d1), s));
+    u = __ddiv_rn(num, __dadd_rn(q0, q1));
+    if (u > m2) {
+      const double m2_2 = __dmul_rn(m2, m2);
+      // phi3D_fsm.c:171-173, a left-to-right chain of twelve terms
+      double r = __dmul_rn(-m2_0, q1);
+      r = __dsub_rn(r, __dmul_rn(m2_0, q2));
+      r = __dadd_rn(r, __dmul_rn(__dmul_rn(__dmul_rn(2.0, m0), m1), q2));
+      r = __dsub_rn(r, __dmul_rn(m2_1, q0));
+      r = __dsub_rn(r, __dmul_rn(m2_1, q2));
+      r = __dadd_rn(r, __dmul_rn(__dmul_rn(__dmul_rn(2.0, m0), m2), q1));
+      r = __dsub_rn(r, __dmul_rn(m2_2, q0));
+      r = __dsub_rn(r, __dmul_rn(m2_2, q1));
+      r = __dadd_rn(r, __dmul_rn(__dmul_rn(__dmul_rn(2.0, m1), m2), q0));
+      r = __dadd_rn(r, __dmul_rn(q0, q1));
+      r = __dadd_rn(r, __dmul_rn(q0, q2));
+      r = __dadd_rn(r, __dmul_rn(q1, q2));
+      const double a = __dsqrt_rn(r);
+      // phi3D_fsm.c:175-177
+      double n3 = __dadd_rn(__dmul_rn(__dmul_rn(m2, q0), q1), __dmul_rn(__dmul_rn(m1, q0), q2));
+      n3 = __dadd_rn(n3, __dmul_rn(__dmul_rn(m0, q1), q2));
+      n3 = __dadd_rn(n3, __dmul_rn(__dmul_rn(__dmul_rn(d0, d1), d2), a));
+      const double den = __dadd_rn(__dadd_rn(__dmul_rn(q0, q1), __dmul_rn(q0, q2)), __dmul_rn(q1, q2));
+      u = __ddiv_rn(n3, den);
+    }
+  }
+  return u;
+}
+
+// FP64 shifted form.  v = u - m0;  2 terms:
+//   v = (a q1 + sqrt(q0 + q1 - a^2 q0 q1)) / (q0 + q1)
+// 3 terms:  v = (B + sqrt(B^2 - A C)) / A  with A = q0+q1+q2,
+//   B = a q1 + b q2,  C = a^2 q1 + b^2 q2 - 1.
+__device__ __forceinline__ double god_fast64(double m0, double m1, double m2, const GodConst64 &k) {
+  double h0 = k.h[0], h1 = k.h[1], h2 = k.h[2];
+  double q0 = k.q[0], q1 = k.q[1], q2 = k.q[2];
+  if (m0 > m1) { cswap(m0, m1); cswap(h0, h1); cswap(q0, q1); }
+  if (m1 > m2) { cswap(m1, m2); cswap(h1, h2); cswap(q1, q2); }
+  if (m0 > m1) { cswap(m0, m1); cswap(h0, h1); cswap(q0, q1); }
+  double u = m0 + h0;
+  if (u > m1) {
+    const double a = m1 - m0;
+    const double s = q0 + q1;
+    const double disc = fma(-a * a, q0 * q1, s);
+    u = m0 + (a * q1 + sqrt(fmax(disc, 0.0))) / s;
+    if (u > m2) {
+      const double b = m2 - m0;
+      const double B = fma(a, q1, b * q2);
+      const double Cc = fma(a * a, q1, fma(b * b, q2, -1.0));
+      const double D = fma(B, B, -k.qsum * Cc);
+      u = m0 + (B + sqrt(fmax(D, 0.0))) * k.iqsum;
+    }
+  }
+  return u;
+}
+
+// FP32 shifted form; ISO = all three spacings equal.
+template <bool ISO>
+__device__ __forceinline__ float god32(float m0, float m1, float m2, const GodConst32 &k) {
+  if (ISO) {
+    // sort without payload
+    float lo = fminf(m0, m1), hi = fmaxf(m0, m1);
+    float mid = fminf(hi, m2), top = fmaxf(hi, m2);
+    m0 = fminf(lo, mid);
+    m1 = fmaxf(lo, mid);
+    m2 = top;
+    float u = m0 + k.iso_h;
+    if (u > m1) {
+      const float a = m1 - m0;
+      // v = (a + sqrt(2h^2 - a^2)) / 2
+      u = m0 + 0.5f * (a + sqrtf(fmaxf(fmaf(-a, a, k.iso_2h2), 0.0f)));
+      if (u > m2) {
+        const float b = m2 - m0;
+        const float s = a + b;
+        // v = (s + sqrt(s^2 - 3(a^2 + b^2 - h^2))) / 3
+        const float c = fmaf(a, a, fmaf(b, b, -k.iso_h2));
+        u = m0 + (s + sqrtf(fmaxf(fmaf(s, s, -3.0f * c), 0.0f))) * (1.0f / 3.0f);
+      }
+    }
+    return u;
+  } else {
+    float h0 = k.h[0], h1 = k.h[1], h2 = k.h[2];
+    float q0 = k.q[0], q1 = k.q[1], q2 = k.q[2];
+    if (m0 > m1) { cswap(m0, m1); cswap(h0, h1); cswap(q0, q1); }
+    if (m1 > m2) { cswap(m1, m2); cswap(h1, h2); cswap(q1, q2); }
+    if (m0 > m1) { cswap(m0, m1); cswap(h0, h1); cswap(q0, q1); }
+    float u = m0 + h0;
+    if (u > m1) {
+      const float a = m1 - m0;
+      const float s = q0 + q1;
+      const float disc = fmaf(-a * a, q0 * q1, s);
+      u = m0 + __fdividef(fmaf(a, q1, sqrtf(fmaxf(disc, 0.0f))), s);
+      if (u > m2) {
+        const float b = m2 - m0;
+        const float B = fmaf(a, q1, b * q2);
+        const float Cc = fmaf(a * a, q1, fmaf(b * b, q2, -1.0f));
+        const float D = fmaf(B, B, -(q0 + q1 + q2) * Cc);
+        u = m0 + (B + sqrtf(fmaxf(D, 0.0f))) * k.iqsum;
+      }
+    }
+    return u;
+  }
+}
+
+}  // namespace pdfs

@@ -1,0 +1,642 @@
+// solver.cu -- host driver of the GB300 FSM solve and the C ABI of include/pdfs.h.
+//
+// Replaces run_fsm (single_gpu_cuda/src/phi3D_fsm.cu:64-106): the field is
+// copied once into a padded device layout, swept by the persistent column
+// kernels until convergence (the reference runs a fixed single round,
+// single_gpu_cuda/src/phi3D.c:118-119, and has no convergence test), and
+// copied back.  Errors are returned, never exit()ed (phi3D_fsm.h:39-46 exits).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace pdfs {
+
+Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize) {
+  Layout L;
+  L.tx = tx;
+  L.ty = ty;
+  L.esize = esize;
+  L.V = 16 / esize;
+  L.ncx = (g.nx + tx - 1) / tx;
+  L.ncy = (g.ny + ty - 1) / ty;
+  const long long need = (long long)L.ncx * tx + 2 * L.V;
+  const long long align = 128 / esize;
+  L.px = (need + align - 1) / align * align;
+  L.ry = (long long)L.ncy * ty + 2;
+  L.plane = L.px * L.ry;
+  L.elems = (size_t)L.plane * (size_t)(g.nz + 2);
+  return L;
+}
+
+MaskLayout make_mask_layout(const pdfs_grid &g) {
+  MaskLayout M;
+  M.fpw = (g.nx + 63) / 32;
+  M.fry = g.ny + 34;
+  M.fplane = M.fpw * M.fry;
+  M.words = (size_t)M.fplane * (size_t)(g.nz + 2);
+  return M;
+}
+
+// ---- layout conversion kernels (one thread per node of a row; grid (rows, planes)) ----
+template <class T>
+__global__ void k_fill(T *p, size_t n, T v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// reference layout (double) -> internal layout of T
+template <class T>
+__global__ void k_pack(const double *__restrict__ ref, T *__restrict__ dst, int nx, int ny, Layout L) {
+  const int y = blockIdx.x, z = blockIdx.y;
+  const double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
+  T *out = dst + L.index(0, y, z);
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) out[x] = (T)row[x];
+}
+
+// internal layout -> reference layout (double).  FP32 source: frozen nodes
+// (mask bit set) take the exact FP64 input instead of the rounded value.
+template <class T>
+__global__ void k_unpack(const T *__restrict__ src, Layout L, const double *__restrict__ in64, Layout L64,
+                         const uint32_t *__restrict__ fmask, MaskLayout M, double *__restrict__ ref, int nx, int ny) {
+  const int y = blockIdx.x, z = blockIdx.y;
+  double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
+  const T *s = src + L.index(0, y, z);
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
+    double v = (double)s[x];
+    if (fmask && x >= 1 && x <= nx && y >= 1 && y <= ny) {
+      const uint32_t w = fmask[(size_t)z * M.fplane + (size_t)y * M.fpw + (x - 1) / 32];
+      if ((w >> ((x - 1) & 31)) & 1u) v = in64[L64.index(x, y, z)];
+    }
+    row[x] = v;
+  }
+}
+
+// internal layout of S -> internal layout of D, every halo-padded node
+template <class S, class D>
+__global__ void k_convert(const S *__restrict__ src, Layout Ls, D *__restrict__ dst, Layout Ld, int nx) {
+  const int y = blockIdx.x, z = blockIdx.y;
+  const S *s = src + Ls.index(0, y, z);
+  D *d = dst + Ld.index(0, y, z);
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) d[x] = (D)s[x];
+}
+
+// FP32 working field -> FP64 working field (polish start): frozen nodes and
+// the halo keep the exact FP64 input.
+__global__ void k_widen(const float *__restrict__ u32, Layout L32, const double *__restrict__ in64,
+                        double *__restrict__ u64, Layout L64, const uint32_t *__restrict__ fmask, MaskLayout M,
+                        int nx, int ny, int nz) {
+  const int y = blockIdx.x, z = blockIdx.y;
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
+    const long long i64 = L64.index(x, y, z);
+    const bool interior = x >= 1 && x <= nx && y >= 1 && y <= ny && z >= 1 && z <= nz;
+    bool frz = !interior;
+    if (interior && fmask) {
+      const uint32_t w = fmask[(size_t)z * M.fpw * M.fry + (size_t)y * M.fpw + (x - 1) / 32];
+      frz = (w >> ((x - 1) & 31)) & 1u;
+    }
+    u64[i64] = frz ? in64[i64] : (double)u32[L32.index(x, y, z)];
+  }
+}
+
+// uint8 mask in the reference layout -> frozen bitmask (interior nodes only)
+__global__ void k_pack_mask(const uint8_t *__restrict__ m, uint32_t *__restrict__ bits, MaskLayout M, int nx,
+                            int ny) {
+  const int y = blockIdx.x + 1, z = blockIdx.y + 1;  // interior rows only
+  const uint8_t *row = m + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
+  uint32_t *out = bits + (size_t)z * M.fplane + (size_t)y * M.fpw;
+  const int nwords = (nx + 31) / 32;
+  for (int w = threadIdx.x; w < nwords; w += blockDim.x) {
+    uint32_t v = 0;
+    for (int b = 0; b < 32; ++b) {
+      const int x = 1 + w * 32 + b;
+      if (x <= nx && row[x]) v |= 1u << b;
+    }
+    out[w] = v;
+  }
+}
+
+// Wavefront order of columns: ticket -> local column id, by diagonal lcx+lcy.
+static std::vector<int> wavefront_order(int ncx, int ncy) {
+  std::vector<int> o;
+  o.reserve((size_t)ncx * ncy);
+  for (int d = 0; d <= ncx + ncy - 2; ++d)
+    for (int lcx = std::max(0, d - (ncy - 1)); lcx <= std::min(d, ncx - 1); ++lcx) o.push_back((d - lcx) * ncx + lcx);
+  return o;
+}
+
+// Sweep direction of ordering sn (1..8), from makeSweepInfo
+// (mpi_openacc/src/phi3D_fsm.c:206-218): a reflection offset reverses its
+// axis, descending levels reverse all three.
+void ordering_signs(int sn, int *sx, int *sy, int *sz) {
+  const int desc = (sn == 2 || sn == 5 || sn == 7 || sn == 8) ? -1 : 1;
+  *sx = ((sn == 4 || sn == 8) ? -1 : 1) * desc;
+  *sy = ((sn == 2 || sn == 6) ? -1 : 1) * desc;
+  *sz = ((sn == 3 || sn == 7) ? -1 : 1) * desc;
+}
+
+struct DevStatus {
+  int err[4];
+  unsigned long long chg;
+};
+
+}  // namespace pdfs
+
+using namespace pdfs;
+
+struct pdfs_ctx {
+  pdfs_grid g{};
+  pdfs_opts o{};
+  int dev = 0, sms = 0;
+  cudaStream_t st = nullptr;
+  int t32 = 1, t64 = 1;
+  Layout L32, L64;
+  MaskLayout M;
+  double *in64 = nullptr;   // exact input, internal FP64 layout (also the polish cap)
+  double *u64 = nullptr;    // FP64 working field
+  float *u32 = nullptr;     // FP32 working field
+  uint32_t *fmask = nullptr;
+  void *stage = nullptr;    // reference-layout staging buffer for host transfers
+  size_t stage_bytes = 0;
+  int *order32 = nullptr, *order64 = nullptr, *progress = nullptr, *ticket = nullptr;
+  DevStatus *dstat = nullptr;
+  DevStatus *hstat = nullptr;  // pinned
+  bool loaded = false, has_mask = false;
+  int last_prec = -1;      // which working field holds the last result
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+static int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return PDFS_OK;
+  if (e == cudaErrorMemoryAllocation) return PDFS_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return PDFS_ERR_NO_DEVICE;
+  return PDFS_ERR_CUDA;
+}
+#define CK(call)                                 \
+  do {                                           \
+    cudaError_t e_ = (call);                     \
+    if (e_ != cudaSuccess) {                     \
+      if (getenv("PDFS_LOG"))                    \
+        fprintf(stderr, "pdfs: %s:%d %s: %s\n", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+      return cuda_status(e_);                    \
+    }                                            \
+  } while (0)
+
+static bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static bool verbose(const pdfs_opts &o) { return o.verbose || getenv("PDFS_LOG"); }
+
+extern "C" void pdfs_default_opts(pdfs_opts *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = PDFS_PREC_FP64;
+  o->arith = PDFS_ARITH_REFERENCE;
+  o->freeze = PDFS_FREEZE_NONE;
+  o->scheduler = PDFS_SCHED_NONE;
+  o->tol = 0.0;
+}
+
+extern "C" const char *pdfs_status_string(int s) {
+  switch (s) {
+    case PDFS_OK: return "ok";
+    case PDFS_ERR_INVALID: return "invalid argument";
+    case PDFS_ERR_OOM: return "out of memory";
+    case PDFS_ERR_CUDA: return "CUDA error";
+    case PDFS_ERR_TIMEOUT: return "inter-tile wait timed out";
+    case PDFS_ERR_NOT_CONVERGED: return "not converged within max_sweeps";
+    case PDFS_ERR_IO: return "I/O error";
+    case PDFS_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char *pdfs_version(void) { return "pdfs-gb300 0.1 (sm_103a)"; }
+
+static int validate(const pdfs_grid *g, const pdfs_opts *o) {
+  if (!g || !o) return PDFS_ERR_INVALID;
+  if (g->nx < 1 || g->ny < 1 || g->nz < 1) return PDFS_ERR_INVALID;
+  if ((long long)g->nx + 2 > (1 << 20) || (long long)g->ny + 2 > 65535 || (long long)g->nz + 2 > 65535)
+    return PDFS_ERR_INVALID;
+  if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !std::isfinite(g->dx) || !std::isfinite(g->dy) ||
+      !std::isfinite(g->dz))
+    return PDFS_ERR_INVALID;
+  if (o->precision < 0 || o->precision > 2 || o->arith < 0 || o->arith > 1 || o->freeze < 0 || o->freeze > 1 ||
+      o->scheduler < 0 || o->scheduler > 2 || o->tol < 0 || !std::isfinite(o->tol) || o->fixed_sweeps < 0 ||
+      o->max_sweeps < 0 || o->first_ordering < 0 || o->first_ordering > 8)
+    return PDFS_ERR_INVALID;
+  const int t32 = o->tile & 0xff, t64 = (o->tile >> 8) & 0xff;
+  if (t32 > tile_count32() || t64 > tile_count64()) return PDFS_ERR_INVALID;
+  return PDFS_OK;
+}
+
+// Default tile choice (the autotuner in sched.cu may override through opts.tile).
+static void pick_tiles(pdfs_ctx *c) {
+  const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
+  c->t32 = t32 ? t32 : 1;
+  c->t64 = t64 ? t64 : 1;
+}
+
+extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_ctx **out) {
+  if (!out) return PDFS_ERR_INVALID;
+  *out = nullptr;
+  pdfs_opts o;
+  if (o_in)
+    o = *o_in;
+  else
+    pdfs_default_opts(&o);
+  int s = validate(g, &o);
+  if (s) return s;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return PDFS_ERR_NO_DEVICE;
+  }
+  if (o.device < 0 || o.device >= ndev) return PDFS_ERR_INVALID;
+  CK(cudaSetDevice(o.device));
+  pdfs_ctx *c = new pdfs_ctx();
+  c->g = *g;
+  c->o = o;
+  c->dev = o.device;
+  pick_tiles(c);
+  const TileShape s32 = tile32(c->t32), s64 = tile64(c->t64);
+  c->L32 = make_layout(*g, s32.tx, s32.ty, 4);
+  c->L64 = make_layout(*g, s64.tx, s64.ty, 8);
+  c->M = make_mask_layout(*g);
+  int rc = PDFS_OK;
+  auto fail = [&](cudaError_t e) {
+    rc = cuda_status(e);
+    pdfs_ctx_destroy(c);
+    return rc;
+  };
+  cudaError_t e;
+  if ((e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->dev)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  const bool need32 = o.precision != PDFS_PREC_FP64;
+  const bool need64 = o.precision != PDFS_PREC_FP32 || true;  // FP64 input always resident
+  if (need64 && (e = cudaMalloc(&c->in64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
+  if ((o.precision != PDFS_PREC_FP32) && (e = cudaMalloc(&c->u64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
+  if (need32 && (e = cudaMalloc(&c->u32, c->L32.elems * 4)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->fmask, c->M.words * 4)) != cudaSuccess) return fail(e);
+  const int ncol = std::max(c->L32.ncx * c->L32.ncy, c->L64.ncx * c->L64.ncy);
+  if ((e = cudaMalloc(&c->progress, (size_t)ncol * 4)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->ticket, 16)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->dstat, sizeof(DevStatus))) != cudaSuccess) return fail(e);
+  if ((e = cudaHostAlloc(&c->hstat, sizeof(DevStatus), cudaHostAllocDefault)) != cudaSuccess) return fail(e);
+  {
+    std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy), w64 = wavefront_order(c->L64.ncx, c->L64.ncy);
+    if ((e = cudaMalloc(&c->order32, w32.size() * 4)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&c->order64, w64.size() * 4)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpy(c->order32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpy(c->order64, w64.data(), w64.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+  }
+  // padding outside the halo-padded grid is never written by the sweeps; fill it with +inf once
+  if (c->in64) k_fill<double><<<2 * c->sms, 256, 0, c->st>>>(c->in64, c->L64.elems, INFINITY);
+  if (c->u64) k_fill<double><<<2 * c->sms, 256, 0, c->st>>>(c->u64, c->L64.elems, INFINITY);
+  if (c->u32) k_fill<float><<<2 * c->sms, 256, 0, c->st>>>(c->u32, c->L32.elems, INFINITY);
+  if ((e = cudaMemsetAsync(c->fmask, 0, c->M.words * 4, c->st)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->e0)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->e1)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) return fail(e);
+  *out = c;
+  return PDFS_OK;
+}
+
+extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->dev);
+  if (c->st) cudaStreamSynchronize(c->st);
+  cudaFree(c->in64);
+  cudaFree(c->u64);
+  cudaFree(c->u32);
+  cudaFree(c->fmask);
+  cudaFree(c->stage);
+  cudaFree(c->order32);
+  cudaFree(c->order64);
+  cudaFree(c->progress);
+  cudaFree(c->ticket);
+  cudaFree(c->dstat);
+  if (c->hstat) cudaFreeHost(c->hstat);
+  if (c->e0) cudaEventDestroy(c->e0);
+  if (c->e1) cudaEventDestroy(c->e1);
+  if (c->st) cudaStreamDestroy(c->st);
+  cudaGetLastError();
+  delete c;
+}
+
+static size_t ref_nodes(const pdfs_grid &g) { return (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2); }
+
+static int ensure_stage(pdfs_ctx *c) {
+  const size_t b = ref_nodes(c->g) * 8;
+  if (c->stage_bytes >= b) return PDFS_OK;
+  cudaFree(c->stage);
+  c->stage = nullptr;
+  c->stage_bytes = 0;
+  CK(cudaMalloc(&c->stage, b));
+  c->stage_bytes = b;
+  return PDFS_OK;
+}
+
+static double ms_between(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+static int load_impl(pdfs_ctx *c, const double *field, const uint8_t *frozen, double *ms_h2d) {
+  if (!c || !field) return PDFS_ERR_INVALID;
+  CK(cudaSetDevice(c->dev));
+  const pdfs_grid &g = c->g;
+  const size_t n = ref_nodes(g);
+  const double *src = field;
+  const bool dev_field = is_device_ptr(field);
+  const bool use_mask = c->o.freeze == PDFS_FREEZE_MASK && frozen;
+  const bool dev_mask = use_mask && is_device_ptr(frozen);
+  int s;
+  if (!dev_field || (use_mask && !dev_mask)) {
+    if ((s = ensure_stage(c))) return s;
+  }
+  CK(cudaEventRecord(c->e0, c->st));
+  if (!dev_field) {
+    CK(cudaMemcpyAsync(c->stage, field, n * 8, cudaMemcpyHostToDevice, c->st));
+    src = (const double *)c->stage;
+  }
+  dim3 grid(g.ny + 2, g.nz + 2);
+  k_pack<double><<<grid, 128, 0, c->st>>>(src, c->in64, g.nx, g.ny, c->L64);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(c->fmask, 0, c->M.words * 4, c->st));
+  if (use_mask) {
+    const uint8_t *m = frozen;
+    if (!dev_mask) {
+      // the stage is re-used for the mask bytes; the stream orders the copy
+      // after k_pack has read the field out of it
+      CK(cudaMemcpyAsync(c->stage, frozen, n, cudaMemcpyHostToDevice, c->st));
+      m = (const uint8_t *)c->stage;
+    }
+    dim3 mg(g.ny, g.nz);
+    k_pack_mask<<<mg, 64, 0, c->st>>>(m, c->fmask, c->M, g.nx, g.ny);
+    CK(cudaGetLastError());
+  }
+  CK(cudaEventRecord(c->e1, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (ms_h2d) *ms_h2d = ms_between(c->e0, c->e1);
+  c->has_mask = use_mask;
+  c->loaded = true;
+  c->last_prec = -1;
+  return PDFS_OK;
+}
+
+extern "C" int pdfs_ctx_load(pdfs_ctx *c, const double *field, const uint8_t *frozen) {
+  return load_impl(c, field, frozen, nullptr);
+}
+
+// One sweep of ordering sn on the FP32 (which = 0) or FP64 (1 min, 2 replace)
+// working field.  *chg receives the sweep's max change (relative for FP32,
+// absolute for FP64).  active: per-block visit mask or nullptr.
+static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, float *blk_chg, double *chg) {
+  const pdfs_grid &g = c->g;
+  const bool f32 = which == 0;
+  const Layout &L = f32 ? c->L32 : c->L64;
+  SweepArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.u = f32 ? (void *)c->u32 : (void *)c->u64;
+  a.cap = which == 2 ? (const void *)c->in64 : nullptr;
+  a.fmask = c->has_mask ? c->fmask : nullptr;
+  a.px = L.px;
+  a.plane = L.plane;
+  a.fpw = c->M.fpw;
+  a.fplane = c->M.fplane;
+  a.nx = g.nx;
+  a.ny = g.ny;
+  a.nz = g.nz;
+  ordering_signs(sn, &a.sx, &a.sy, &a.sz);
+  a.ncx = L.ncx;
+  a.ncy = L.ncy;
+  a.order = f32 ? c->order32 : c->order64;
+  a.progress = c->progress;
+  a.ticket = c->ticket;
+  a.err = c->dstat->err;
+  a.maxchg = &c->dstat->chg;
+  a.blk_active = active;
+  a.blk_chg = blk_chg;
+  a.nbx = (g.nx + 7) / 8;
+  a.nby = (g.ny + 7) / 8;
+  a.nbz = (g.nz + 7) / 8;
+  a.hmin = (float)std::min(g.dx, std::min(g.dy, g.dz));
+  long long wait_ms = c->o.spin_limit > 0 ? c->o.spin_limit : 4000;
+  if (getenv("PDFS_WAIT_MS")) wait_ms = atoll(getenv("PDFS_WAIT_MS"));
+  a.wait_ns = wait_ms * 1000000LL;
+  a.poison_col = getenv("PDFS_TEST_POISON_COLUMN") ? atoi(getenv("PDFS_TEST_POISON_COLUMN")) : -1;
+  const double h[3] = {g.dx, g.dy, g.dz};
+  for (int i = 0; i < 3; ++i) {
+    a.k64.h[i] = h[i];
+    a.k64.h2[i] = h[i] * h[i];
+    a.k64.q[i] = 1.0 / (h[i] * h[i]);
+    a.k32.h[i] = (float)h[i];
+    a.k32.q[i] = (float)(1.0 / (h[i] * h[i]));
+  }
+  a.k64.qsum = a.k64.q[0] + a.k64.q[1] + a.k64.q[2];
+  a.k64.iqsum = 1.0 / a.k64.qsum;
+  a.k32.iqsum = (float)a.k64.iqsum;
+  a.k32.iso_h = (float)g.dx;
+  a.k32.iso_2h2 = (float)(2.0 * g.dx * g.dx);
+  a.k32.iso_h2 = (float)(g.dx * g.dx);
+  const bool iso = g.dx == g.dy && g.dy == g.dz;
+
+  CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * 4, c->st));
+  CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
+  CK(cudaMemsetAsync(c->dstat, 0, sizeof(DevStatus), c->st));
+  const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : ARITH_FAST;
+  int grid = 0;
+  CK(launch_sweep(which, f32 ? c->t32 : c->t64, arith, iso, a, c->sms, c->st, &grid));
+  CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (c->hstat->err[0]) {
+    if (verbose(c->o))
+      fprintf(stderr, "pdfs: sweep sn=%d timed out waiting on column %d\n", sn, c->hstat->err[2]);
+    return PDFS_ERR_TIMEOUT;
+  }
+  if (chg) {
+    if (f32) {
+      unsigned int b = (unsigned int)c->hstat->chg;
+      float f;
+      std::memcpy(&f, &b, 4);
+      *chg = f;
+    } else {
+      double d;
+      std::memcpy(&d, &c->hstat->chg, 8);
+      *chg = d;
+    }
+  }
+  return PDFS_OK;
+}
+
+static int widen(pdfs_ctx *c) {
+  const pdfs_grid &g = c->g;
+  dim3 grid(g.ny + 2, g.nz + 2);
+  k_widen<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64, c->has_mask ? c->fmask : nullptr, c->M,
+                                   g.nx, g.ny, g.nz);
+  CK(cudaGetLastError());
+  return PDFS_OK;
+}
+
+static int narrow(pdfs_ctx *c) {  // FP64 input -> FP32 working field
+  const pdfs_grid &g = c->g;
+  dim3 grid(g.ny + 2, g.nz + 2);
+  k_convert<double, float><<<grid, 128, 0, c->st>>>(c->in64, c->L64, c->u32, c->L32, g.nx);
+  CK(cudaGetLastError());
+  return PDFS_OK;
+}
+
+extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
+  if (!c || !c->loaded) return PDFS_ERR_INVALID;
+  CK(cudaSetDevice(c->dev));
+  const auto t0 = std::chrono::steady_clock::now();
+  pdfs_stats st;
+  std::memset(&st, 0, sizeof(st));
+  st.tile = c->t32 | (c->t64 << 8);
+  const pdfs_opts &o = c->o;
+  const pdfs_grid &g = c->g;
+  const long long nodes = (long long)g.nx * g.ny * g.nz;
+  const int max_sweeps = o.max_sweeps > 0 ? o.max_sweeps : 100000;
+  const int first = o.first_ordering ? o.first_ordering - 1 : 0;
+  int rc = PDFS_OK;
+  double chg = 0.0;
+
+  auto phase = [&](int which, double tol, int *count, double *ms) -> int {
+    CK(cudaEventRecord(c->e0, c->st));
+    int s = 0;
+    for (;;) {
+      if (o.fixed_sweeps > 0 && s >= o.fixed_sweeps) break;
+      if (o.fixed_sweeps == 0 && s >= max_sweeps) {
+        rc = PDFS_ERR_NOT_CONVERGED;
+        break;
+      }
+      const int sn = (first + s) % 8 + 1;
+      int r = run_sweep(c, which, sn, nullptr, nullptr, &chg);
+      if (r) return r;
+      ++s;
+      st.full_sweeps++;
+      st.voxel_updates += nodes;
+      if (o.fixed_sweeps == 0 && chg <= tol) break;
+    }
+    CK(cudaEventRecord(c->e1, c->st));
+    CK(cudaEventSynchronize(c->e1));
+    *count += s;
+    *ms += ms_between(c->e0, c->e1);
+    st.final_change = chg;
+    return PDFS_OK;
+  };
+
+  int r = PDFS_OK;
+  if (o.precision == PDFS_PREC_FP64) {
+    CK(cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st));
+    r = phase(1, o.tol, &st.sweeps_fp64, &st.ms_fp64);
+    c->last_prec = 1;
+  } else {
+    if ((r = narrow(c))) return r;
+    const double tol32 = 4.0e-6;  // relative; FP32 rounding creep stays ~1e-7
+    r = phase(0, tol32, &st.sweeps_fp32, &st.ms_fp32);
+    c->last_prec = 0;
+    if (!r && o.precision == PDFS_PREC_FP32_POLISH64 && o.fixed_sweeps == 0) {
+      if ((r = widen(c))) return r;
+      r = phase(2, o.tol, &st.sweeps_fp64, &st.ms_fp64);
+      c->last_prec = 1;
+    }
+  }
+  if (!r) r = rc;
+  st.status = r;
+  st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = st;
+  if (verbose(o))
+    fprintf(stderr, "pdfs: run status=%d fp32 sweeps=%d (%.2f ms) fp64 sweeps=%d (%.2f ms) final change=%g\n", r,
+            st.sweeps_fp32, st.ms_fp32, st.sweeps_fp64, st.ms_fp64, st.final_change);
+  return r;
+}
+
+static int store_impl(pdfs_ctx *c, double *field, double *ms_d2h) {
+  if (!c || !field || c->last_prec < 0) return PDFS_ERR_INVALID;
+  CK(cudaSetDevice(c->dev));
+  const pdfs_grid &g = c->g;
+  const bool dev = is_device_ptr(field);
+  double *dst = field;
+  int s;
+  if (!dev) {
+    if ((s = ensure_stage(c))) return s;
+    dst = (double *)c->stage;
+  }
+  CK(cudaEventRecord(c->e0, c->st));
+  dim3 grid(g.ny + 2, g.nz + 2);
+  const uint32_t *fm = c->has_mask ? c->fmask : nullptr;
+  if (c->last_prec == 1)
+    k_unpack<double><<<grid, 128, 0, c->st>>>(c->u64, c->L64, c->in64, c->L64, nullptr, c->M, dst, g.nx, g.ny);
+  else
+    k_unpack<float><<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->L64, fm, c->M, dst, g.nx, g.ny);
+  CK(cudaGetLastError());
+  if (!dev) CK(cudaMemcpyAsync(field, c->stage, ref_nodes(g) * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaEventRecord(c->e1, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (ms_d2h) *ms_d2h = ms_between(c->e0, c->e1);
+  return PDFS_OK;
+}
+
+extern "C" int pdfs_ctx_store(pdfs_ctx *c, double *field) { return store_impl(c, field, nullptr); }
+
+extern "C" int pdfs_solve(const pdfs_grid *g, double *field, const uint8_t *frozen, const pdfs_opts *o,
+                          pdfs_stats *stats) {
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!field) return PDFS_ERR_INVALID;
+  pdfs_ctx *c = nullptr;
+  int s = pdfs_ctx_create(g, o, &c);
+  if (s) {
+    if (stats) stats->status = s;
+    return s;
+  }
+  double h2d = 0, d2h = 0;
+  pdfs_stats st;
+  std::memset(&st, 0, sizeof(st));
+  s = load_impl(c, field, frozen, &h2d);
+  if (!s) {
+    s = pdfs_ctx_run(c, &st);
+    if (!s || s == PDFS_ERR_NOT_CONVERGED) {
+      int s2 = store_impl(c, field, &d2h);
+      if (s2) s = s2;
+    }
+  }
+  pdfs_ctx_destroy(c);
+  st.status = s;
+  st.ms_h2d = h2d;
+  st.ms_d2h = d2h;
+  st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = st;
+  return s;
+}
+
+extern "C" int pdfs_sweep(const pdfs_grid *g, double *field, const uint8_t *frozen, int sn, const pdfs_opts *o_in,
+                          double *max_change) {
+  if (sn < 1 || sn > 8 || !field) return PDFS_ERR_INVALID;
+  pdfs_opts o;
+  if (o_in)
+    o = *o_in;
+  else
+    pdfs_default_opts(&o);
+  o.precision = PDFS_PREC_FP64;
+  o.fixed_sweeps = 1;
+  o.first_ordering = sn;
+  o.scheduler = PDFS_SCHED_NONE;
+  pdfs_stats st;
+  int s = pdfs_solve(g, field, frozen, &o, &st);
+  if (max_change) *max_change = st.final_change;
+  return s;
+}
