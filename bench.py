@@ -1,0 +1,346 @@
+"""Benchmark of the GB300 FSM distance-field solve.
+
+Metric (the reference's headline): time-to-converge and Gvoxel-updates/s of
+the FP32-bulk + FP64-polish solve (with active-block scheduling) against the
+plain FP64 FSM, at <= 1e-6 relative error.
+
+One step = one complete solve of the workload to convergence, from the input
+already resident in HBM (pdfs_ctx_run).  value = plain-equivalent
+Gvox-updates/s: (interior nodes x sweeps the plain FP64 FSM needs on this
+input) / (time of our solve).  e2e = the same through pdfs_solve() with pinned
+host buffers, host<->device copies and layout passes inside the timed region.
+
+Default workload: 768^3, dx = 1, union of 150 seeded spheres (radii
+log-uniform 4..50 cells), interface nodes frozen; inputs (3.6 GB) are larger
+than L2 (129 MB), so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload C4|C2|C3|C1|spheresN] [--mode polish|fp32|fp64|fp64ref]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="C4")
+    p.add_argument("--mode", default="polish", choices=["polish", "fp32", "fp64", "fp64ref"])
+    p.add_argument("--scheduler", default="change", choices=["none", "change", "learned"])
+    p.add_argument("--tol", type=float, default=1e-9, help="FP64 polish tolerance (max change)")
+    p.add_argument("--tile", type=int, default=0)
+    p.add_argument("--fixed-sweeps", type=int, default=0, help="profiling: run exactly this many sweeps")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 FSM comparison solve")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--cpu-sweeps", type=int, default=0, help="CPU sample: sweeps of the full grid")
+    return p.parse_args()
+
+
+def workload(name, seed=0):
+    from pdfs_gb300 import workloads as W
+    if name.startswith("spheres"):
+        n = int(name[len("spheres"):])
+        return W.random_spheres(n, n, n, 1.0, 1.0, 1.0, max(8, int(150 * (n / 768) ** 3)), 4.0, 50.0 * n / 768,
+                                seed=seed + 4, name=f"spheres_{n}^3")
+    return W.config(name, seed=seed)
+
+
+# ---- distributed plumbing (one process per GPU; replicas: the single-grid path does not shard) ----
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+            else:
+                torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(w, sweeps, threads):
+    """The CPU restatement of the reference FSM (OpenMP over each hyperplane),
+    timed on the host cores on `sweeps` orderings of the full grid."""
+    from oracle import oracle as O
+    O.build(ref=False)
+    a = w.field.copy()
+    sp = (w.dx, w.dy, w.dz)
+    t0 = time.perf_counter()
+    for s in range(sweeps):
+        O.sweep(a, sp, s % 8 + 1, frozen=w.frozen, threads=threads)
+    dt = time.perf_counter() - t0
+    return w.interior * sweeps / dt / 1e9, dt
+
+
+def run_reference(args, rank, world, pg):
+    """Reference arm: the reference's CPU FSM path on the host cores (the
+    oracle port; the reference sources are not available on the GPU machine)."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    w = workload(args.workload)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    sp = (w.dx, w.dy, w.dz)
+    a = w.field.copy()
+    O.build(ref=False)
+    for s in range(args.warmup):
+        O.sweep(a, sp, s % 8 + 1, frozen=w.frozen, threads=threads)
+    times = []
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        O.sweep(a, sp, (args.warmup + s) % 8 + 1, frozen=w.frozen, threads=threads)
+        times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    v = w.interior / t / 1e9
+    line = {"metric": "Gvox-updates/s (plain FP64 FSM, one ordering per step)", "value": v,
+            "unit": "Gvox-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": "Gvox-updates/s", "cores": threads, "kind": kind,
+                             "sample": f"one FP64 ordering over the full {w.nx}x{w.ny}x{w.nz} grid per step"},
+            "e2e": {"value": v, "unit": "Gvox-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world, pg)
+        return
+    from pdfs_gb300 import _lib as L
+    from pdfs_gb300 import api
+    from pdfs_gb300 import build as B
+    B.build()
+    device = local
+    w = workload(args.workload)
+    sp = (w.dx, w.dy, w.dz)
+    freeze = L.FREEZE_MASK
+    prec = {"polish": L.PREC_FP32_POLISH64, "fp32": L.PREC_FP32, "fp64": L.PREC_FP64,
+            "fp64ref": L.PREC_FP64}[args.mode]
+    arith = L.ARITH_REFERENCE if args.mode == "fp64ref" else L.ARITH_FAST
+    sched = {"none": L.SCHED_NONE, "change": L.SCHED_CHANGE, "learned": L.SCHED_LEARNED}[args.scheduler]
+    if args.mode in ("fp64", "fp64ref"):
+        sched = L.SCHED_NONE
+    opts = dict(precision=prec, arith=arith, freeze=freeze, scheduler=sched, tol=args.tol, tile=args.tile,
+                fixed_sweeps=args.fixed_sweeps, device=device)
+    ctx = api.Context(w.nx, w.ny, w.nz, sp, **opts)
+    ctx.load(w.field, w.frozen)
+    for _ in range(args.warmup):
+        ctx.run()
+    clocks = Clocks(device)
+    barrier(pg)
+    clocks.start()
+    t0 = time.perf_counter()
+    stats = []
+    for _ in range(args.steps):
+        stats.append(ctx.run())  # each run synchronises the device before returning
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    barrier(pg)
+    wall = max_over_ranks(pg, wall)
+    t_step = wall / args.steps
+    out = np.empty_like(w.field)
+    ctx.store(out)
+    ctx.close()
+    st = stats[-1]
+
+    # plain FP64 FSM on the same input: sweep count (for the plain-equivalent
+    # rate), its time, and the error of our answer against it
+    plain = None
+    if not args.no_plain and args.fixed_sweeps == 0:
+        ref = w.field.copy()
+        ps = api.solve(ref, sp, frozen=w.frozen, freeze=freeze, precision=L.PREC_FP64, arith=L.ARITH_FAST,
+                       tol=1e-12, device=device)
+        i = (slice(1, -1),) * 3
+        err = float(np.max(np.abs(out[i] - ref[i]) / np.maximum(np.abs(ref[i]), min(sp))))
+        plain = {"sweeps": ps["sweeps_fp64"], "time_s": (ps["ms_fp64"] + 0.0) / 1e3,
+                 "kernel_ms": ps["ms_kern_fp64"], "max_rel_err_vs_plain": err}
+    plain_sweeps = plain["sweeps"] if plain else (st["sweeps_fp32"] + st["sweeps_fp64"])
+    value = w.interior * plain_sweeps / t_step / 1e9
+
+    # e2e through pdfs_solve with pinned host buffers
+    e2e = None
+    if not args.no_e2e and args.fixed_sweeps == 0:
+        try:
+            import torch
+            hf = torch.empty(w.field.shape, dtype=torch.float64).pin_memory()
+            hm = torch.empty(w.frozen.shape, dtype=torch.uint8).pin_memory()
+            hf.numpy()[:] = w.field
+            hm.numpy()[:] = w.frozen
+            f_np, m_np = hf.numpy(), hm.numpy()
+        except Exception:
+            f_np, m_np = w.field.copy(), w.frozen
+        ts = []
+        for k in range(2):
+            f_np[:] = w.field
+            t1 = time.perf_counter()
+            api.solve(f_np, sp, frozen=m_np, **opts)
+            ts.append(time.perf_counter() - t1)
+        te = min(ts)
+        e2e = {"value": w.interior * plain_sweeps / te / 1e9, "unit": "Gvox-updates/s",
+               "h2d_bytes_per_step": int(w.field.nbytes + w.frozen.nbytes),
+               "d2h_bytes_per_step": int(w.field.nbytes), "time_to_converge_s": te}
+
+    # roofline of the dominant kernel
+    pk = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    k32, k64 = st["ms_kern_fp32"], st["ms_kern_fp64"]
+    s32, s64 = st["sweeps_fp32"], st["sweeps_fp64"]
+    dominant = "fp64" if k64 >= k32 else "fp32"
+    mask_b = 1.0 / 8.0
+    if dominant == "fp32":
+        per_launch = w.interior * (8 + mask_b)
+        dur = k32 / max(s32, 1)
+    else:
+        per_launch = w.interior * (16 + 8 + mask_b) if prec == L.PREC_FP32_POLISH64 else w.interior * (16 + mask_b)
+        dur = k64 / max(s64, 1)
+    achieved = per_launch / (dur / 1e3) / 1e9 if dur > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "kernel": f"col_sweep_kernel<{'float' if dominant == 'fp32' else 'double'}>",
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800 GB/s"}
+    fp32_roof = None
+    if s32:
+        a32 = w.interior * (8 + mask_b) / (k32 / s32 / 1e3) / 1e9
+        fp32_roof = {"achieved": a32, "frac": a32 / hbm, "ms_per_sweep": k32 / s32}
+
+    cpu = None
+    if rank == 0 and world >= 1 and not args.no_cpu and args.fixed_sweeps == 0:
+        threads = os.cpu_count() or 1
+        sweeps = args.cpu_sweeps or 2
+        v, dt = cpu_baseline(w, sweeps, threads)
+        cpu = {"value": v, "unit": "Gvox-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{sweeps} FP64 orderings of the full grid ({dt:.1f} s), OpenMP over hyperplanes"}
+
+    if rank == 0:
+        line = {
+            "metric": "time-to-converge & Gvox-updates/s (plain-equivalent): FP32 bulk + FP64 polish with "
+                      "active-block scheduling vs plain FP64 FSM at <=1e-6 rel err",
+            "value": value, "unit": "Gvox-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if prec == L.PREC_FP32_POLISH64 else
+            ("f32" if prec == L.PREC_FP32 else "f64"), "data": "synthetic (seeded spheres)",
+            "config": {"workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "spacing": list(sp),
+                       "mode": args.mode, "scheduler": args.scheduler, "polish_tol": args.tol,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (no flush needed)"},
+            "time_to_converge_s": t_step,
+            "sweeps": {"fp32": s32, "fp64": s64, "full": st["full_sweeps"],
+                       "voxel_updates": st["voxel_updates"], "blocks_skipped": st["blocks_skipped"]},
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": (plain["time_s"] / t_step) if plain else None,
+            "roofline": roof, "roofline_fp32_sweep": fp32_roof,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(sum(s["launches"] for s in stats)),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

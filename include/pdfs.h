@@ -98,8 +98,11 @@ typedef struct {
   double ms_h2d, ms_d2h;      /* host<->device copies (host pointers only)          */
   double ms_fp32, ms_fp64;    /* device time of the two sweep phases                */
   double ms_sched;            /* device time of scheduler inference                 */
-  int tile;                   /* tile variant used                                  */
-  int reserved[7];
+  double ms_kern_fp32;        /* summed durations of the FP32 sweep kernels alone    */
+  double ms_kern_fp64;        /* summed durations of the FP64 sweep kernels alone    */
+  int tile;                   /* tile variant used (FP32 id | FP64 id << 8)         */
+  int launches;               /* kernels this call launched                          */
+  int reserved[6];
 } pdfs_stats;
 
 /* Fills *o with the defaults: FP64, reference arithmetic, no freezing, no

@@ -47,7 +47,9 @@ class Stats(C.Structure):
                 ("full_sweeps", C.c_int), ("voxel_updates", C.c_longlong), ("blocks_skipped", C.c_longlong),
                 ("final_change", C.c_double), ("ms_total", C.c_double), ("ms_h2d", C.c_double),
                 ("ms_d2h", C.c_double), ("ms_fp32", C.c_double), ("ms_fp64", C.c_double),
-                ("ms_sched", C.c_double), ("tile", C.c_int), ("reserved", C.c_int * 7)]
+                ("ms_sched", C.c_double), ("ms_kern_fp32", C.c_double),
+                ("ms_kern_fp64", C.c_double), ("tile", C.c_int), ("launches", C.c_int),
+                ("reserved", C.c_int * 6)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

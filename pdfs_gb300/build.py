@@ -59,11 +59,14 @@ def build(verbose: bool = False, force: bool = False) -> str:
     jobs, objs = [], []
     nv_flags = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC,
                        "--expt-relaxed-constexpr"]
+    # the sweep kernels' FP32 arithmetic uses approximate sqrt/divide (the
+    # FP64 polish removes the difference); FP64 arithmetic is unaffected
+    per_tu = {"sweep.cu": ["-prec-sqrt=false", "-prec-div=false"]}
     for src in cu:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _newer(obj, [src] + hdrs):
-            jobs.append(([nvcc] + nv_flags + ["-c", src, "-o", obj], src))
+            jobs.append(([nvcc] + nv_flags + per_tu.get(os.path.basename(src), []) + ["-c", src, "-o", obj], src))
     c_flags = ["-O2", "-fPIC", "-std=gnu99", "-ffp-contract=off", "-I" + INC, "-I" + CSRC]
     for src in lib_c:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")

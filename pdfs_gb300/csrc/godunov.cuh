@@ -11,8 +11,9 @@
 //                 operation an explicitly rounded intrinsic so nothing is fused:
 //                 bit-identical to the reference's C compiled without contraction.
 //   god_fast64 -- FP64, shifted form in the differences a = m1-m0, b = m2-m0.
-//   god32      -- FP32, same shifted form (the expanded form cancels
-//                 catastrophically in FP32 once m is a few hundred cells).
+//   god32s     -- FP32, same shifted form evaluated branch-free (the expanded
+//                 form cancels catastrophically in FP32 once m is a few
+//                 hundred cells).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -118,51 +119,43 @@ __device__ __forceinline__ double god_fast64(double m0, double m1, double m2, co
   return u;
 }
 
-// FP32 shifted form; ISO = all three spacings equal.
+// FP32 shifted form evaluated branch-free: all three candidates are computed
+// and the Godunov selection (1 term unless it exceeds the second minimum, 2
+// terms unless they exceed the third) picks one.  Each candidate that can be
+// selected is finite: u2 is only chosen when m1 < m0 + h (so a is finite), u3
+// only when u2 > m2 (so b is finite); infinite minima only reach candidates
+// that are not selected.
 template <bool ISO>
-__device__ __forceinline__ float god32(float m0, float m1, float m2, const GodConst32 &k) {
+__device__ __forceinline__ float god32s(float m0, float m1, float m2, const GodConst32 &k) {
   if (ISO) {
-    // sort without payload
-    float lo = fminf(m0, m1), hi = fmaxf(m0, m1);
-    float mid = fminf(hi, m2), top = fmaxf(hi, m2);
+    const float lo = fminf(m0, m1), hi = fmaxf(m0, m1);
+    const float mid = fminf(hi, m2);
+    m2 = fmaxf(hi, m2);
     m0 = fminf(lo, mid);
     m1 = fmaxf(lo, mid);
-    m2 = top;
-    float u = m0 + k.iso_h;
-    if (u > m1) {
-      const float a = m1 - m0;
-      // v = (a + sqrt(2h^2 - a^2)) / 2
-      u = m0 + 0.5f * (a + sqrtf(fmaxf(fmaf(-a, a, k.iso_2h2), 0.0f)));
-      if (u > m2) {
-        const float b = m2 - m0;
-        const float s = a + b;
-        // v = (s + sqrt(s^2 - 3(a^2 + b^2 - h^2))) / 3
-        const float c = fmaf(a, a, fmaf(b, b, -k.iso_h2));
-        u = m0 + (s + sqrtf(fmaxf(fmaf(s, s, -3.0f * c), 0.0f))) * (1.0f / 3.0f);
-      }
-    }
-    return u;
+    const float u1 = m0 + k.iso_h;
+    const float a = m1 - m0;
+    const float u2 = fmaf(0.5f, a + sqrtf(fmaxf(fmaf(-a, a, k.iso_2h2), 0.0f)), m0);
+    const float b = m2 - m0;
+    const float s = a + b;
+    const float cc = fmaf(a, a, fmaf(b, b, -k.iso_h2));
+    const float u3 = fmaf(s + sqrtf(fmaxf(fmaf(s, s, -3.0f * cc), 0.0f)), 1.0f / 3.0f, m0);
+    return (u1 <= m1) ? u1 : ((u2 <= m2) ? u2 : u3);
   } else {
     float h0 = k.h[0], h1 = k.h[1], h2 = k.h[2];
     float q0 = k.q[0], q1 = k.q[1], q2 = k.q[2];
     if (m0 > m1) { cswap(m0, m1); cswap(h0, h1); cswap(q0, q1); }
     if (m1 > m2) { cswap(m1, m2); cswap(h1, h2); cswap(q1, q2); }
     if (m0 > m1) { cswap(m0, m1); cswap(h0, h1); cswap(q0, q1); }
-    float u = m0 + h0;
-    if (u > m1) {
-      const float a = m1 - m0;
-      const float s = q0 + q1;
-      const float disc = fmaf(-a * a, q0 * q1, s);
-      u = m0 + __fdividef(fmaf(a, q1, sqrtf(fmaxf(disc, 0.0f))), s);
-      if (u > m2) {
-        const float b = m2 - m0;
-        const float B = fmaf(a, q1, b * q2);
-        const float Cc = fmaf(a * a, q1, fmaf(b * b, q2, -1.0f));
-        const float D = fmaf(B, B, -(q0 + q1 + q2) * Cc);
-        u = m0 + (B + sqrtf(fmaxf(D, 0.0f))) * k.iqsum;
-      }
-    }
-    return u;
+    const float u1 = m0 + h0;
+    const float a = m1 - m0;
+    const float sq = q0 + q1;
+    const float u2 = m0 + __fdividef(fmaf(a, q1, sqrtf(fmaxf(fmaf(-a * a, q0 * q1, sq), 0.0f))), sq);
+    const float b = m2 - m0;
+    const float B = fmaf(a, q1, b * q2);
+    const float Cc = fmaf(a * a, q1, fmaf(b * b, q2, -1.0f));
+    const float u3 = fmaf(B + sqrtf(fmaxf(fmaf(B, B, -(q0 + q1 + q2) * Cc), 0.0f)), k.iqsum, m0);
+    return (u1 <= m1) ? u1 : ((u2 <= m2) ? u2 : u3);
   }
 }
 

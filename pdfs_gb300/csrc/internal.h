@@ -22,10 +22,16 @@ struct Layout {
 
 Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize);
 
-// Frozen bitmask layout: bit (x-1) of word row (z, y); independent of the tile.
+// Frozen bitmask layout, independent of the tile: node (x, y, z) is bit
+// (x-1)%32 of word z*fplane + ((x-1)/32)*fy + (y-1).  The rows of one 32-wide
+// column are contiguous, so a column's mask words for one plane are a single
+// TMA box; fy is a multiple of 4 (16-byte strides).
 struct MaskLayout {
-  long long fpw = 0, fry = 0, fplane = 0;
+  long long fy = 0, fw = 0, fplane = 0;
   size_t words = 0;
+  __host__ __device__ long long word(int x, int y, int z) const {
+    return (long long)z * fplane + (long long)((x - 1) >> 5) * fy + (y - 1);
+  }
 };
 MaskLayout make_mask_layout(const pdfs_grid &g);
 
@@ -40,8 +46,13 @@ TileShape tile32(int id);
 TileShape tile64(int id);
 
 // Launches one sweep; grid is chosen from the occupancy of the variant.
-// which: 0 = FP32 min (iso / aniso from `iso`), 1 = FP64 min, 2 = FP64 replace.
-cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, int sms,
-                         cudaStream_t st, int *grid_used);
+// which: 0 = FP32 min (iso / aniso from `iso`), 1 = FP64 min, 2 = FP64 replace
+// (cap = upper bound field in the same layout).
+cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
+                         const void *cap, int sms, cudaStream_t st, int *grid_used);
+
+// Steps per mailbox chunk (matches WsGeo::C).
+constexpr int kMailboxChunk = 4;
+inline int mailbox_chunks(int nz) { return (nz + 32 + kMailboxChunk - 1) / kMailboxChunk; }
 
 }  // namespace pdfs

@@ -36,9 +36,9 @@ Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize) {
 
 MaskLayout make_mask_layout(const pdfs_grid &g) {
   MaskLayout M;
-  M.fpw = (g.nx + 63) / 32;
-  M.fry = g.ny + 34;
-  M.fplane = M.fpw * M.fry;
+  M.fy = ((long long)g.ny + 32 + 3) / 4 * 4;
+  M.fw = (g.nx + 31) / 32 + 1;
+  M.fplane = M.fy * M.fw;
   M.words = (size_t)M.fplane * (size_t)(g.nz + 2);
   return M;
 }
@@ -69,7 +69,7 @@ __global__ void k_unpack(const T *__restrict__ src, Layout L, const double *__re
   for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
     double v = (double)s[x];
     if (fmask && x >= 1 && x <= nx && y >= 1 && y <= ny) {
-      const uint32_t w = fmask[(size_t)z * M.fplane + (size_t)y * M.fpw + (x - 1) / 32];
+      const uint32_t w = fmask[M.word(x, y, z)];
       if ((w >> ((x - 1) & 31)) & 1u) v = in64[L64.index(x, y, z)];
     }
     row[x] = v;
@@ -96,7 +96,7 @@ __global__ void k_widen(const float *__restrict__ u32, Layout L32, const double 
     const bool interior = x >= 1 && x <= nx && y >= 1 && y <= ny && z >= 1 && z <= nz;
     bool frz = !interior;
     if (interior && fmask) {
-      const uint32_t w = fmask[(size_t)z * M.fpw * M.fry + (size_t)y * M.fpw + (x - 1) / 32];
+      const uint32_t w = fmask[M.word(x, y, z)];
       frz = (w >> ((x - 1) & 31)) & 1u;
     }
     u64[i64] = frz ? in64[i64] : (double)u32[L32.index(x, y, z)];
@@ -108,7 +108,6 @@ __global__ void k_pack_mask(const uint8_t *__restrict__ m, uint32_t *__restrict_
                             int ny) {
   const int y = blockIdx.x + 1, z = blockIdx.y + 1;  // interior rows only
   const uint8_t *row = m + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
-  uint32_t *out = bits + (size_t)z * M.fplane + (size_t)y * M.fpw;
   const int nwords = (nx + 31) / 32;
   for (int w = threadIdx.x; w < nwords; w += blockDim.x) {
     uint32_t v = 0;
@@ -116,16 +115,24 @@ __global__ void k_pack_mask(const uint8_t *__restrict__ m, uint32_t *__restrict_
       const int x = 1 + w * 32 + b;
       if (x <= nx && row[x]) v |= 1u << b;
     }
-    out[w] = v;
+    bits[M.word(1 + w * 32, y, z)] = v;
   }
 }
 
-// Wavefront order of columns: ticket -> local column id, by diagonal lcx+lcy.
-static std::vector<int> wavefront_order(int ncx, int ncy) {
-  std::vector<int> o;
-  o.reserve((size_t)ncx * ncy);
-  for (int d = 0; d <= ncx + ncy - 2; ++d)
-    for (int lcx = std::max(0, d - (ncy - 1)); lcx <= std::min(d, ncx - 1); ++lcx) o.push_back((d - lcx) * ncx + lcx);
+// Ticket order of columns: ticket -> local column id (lcy*ncx + lcx), sorted
+// by the column's expected start step, lcx*(TX+12) + lcy*(TY+12): a column
+// trails its x-upwind neighbour by about TX steps and its y-upwind one by
+// about TY, plus a few steps of hand-off latency.  Any order with positive
+// weights lists both upwind neighbours first, which is all the deadlock
+// argument needs.
+static std::vector<int> wavefront_order(int ncx, int ncy, int tx, int ty) {
+  std::vector<int> o((size_t)ncx * ncy);
+  for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
+  const long long wx = tx + 12, wy = ty + 12;
+  std::stable_sort(o.begin(), o.end(), [&](int a, int b) {
+    const long long ka = (a % ncx) * wx + (a / ncx) * wy, kb = (b % ncx) * wx + (b / ncx) * wy;
+    return ka < kb;
+  });
   return o;
 }
 
@@ -163,11 +170,16 @@ struct pdfs_ctx {
   void *stage = nullptr;    // reference-layout staging buffer for host transfers
   size_t stage_bytes = 0;
   int *order32 = nullptr, *order64 = nullptr, *progress = nullptr, *ticket = nullptr;
+  void *mailbox = nullptr;  // x- and y-face mailboxes of every column
+  size_t mailbox_bytes = 0;
+  size_t progress_ints = 0;
   DevStatus *dstat = nullptr;
   DevStatus *hstat = nullptr;  // pinned
   bool loaded = false, has_mask = false;
   int last_prec = -1;      // which working field holds the last result
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr;
+  double kern_ms = 0.0;  // accumulated sweep-kernel time since the last reset
+  int launches = 0;      // kernels launched since the last reset
 };
 
 static int cuda_status(cudaError_t e) {
@@ -238,6 +250,7 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
     return PDFS_ERR_INVALID;
   const int t32 = o->tile & 0xff, t64 = (o->tile >> 8) & 0xff;
   if (t32 > tile_count32() || t64 > tile_count64()) return PDFS_ERR_INVALID;
+  if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 > 2) return PDFS_ERR_INVALID;  // polish kernel: TY = 4 only
   return PDFS_OK;
 }
 
@@ -289,13 +302,27 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((o.precision != PDFS_PREC_FP32) && (e = cudaMalloc(&c->u64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
   if (need32 && (e = cudaMalloc(&c->u32, c->L32.elems * 4)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->fmask, c->M.words * 4)) != cudaSuccess) return fail(e);
-  const int ncol = std::max(c->L32.ncx * c->L32.ncy, c->L64.ncx * c->L64.ncy);
-  if ((e = cudaMalloc(&c->progress, (size_t)ncol * 4)) != cudaSuccess) return fail(e);
+  {
+    // per-row progress words and face mailboxes, sized for the larger of the two layouts
+    const int nb = mailbox_chunks(g->nz) * kMailboxChunk;
+    size_t prog = 0, mb = 0;
+    for (int k = 0; k < 2; ++k) {
+      const Layout &L = k ? c->L64 : c->L32;
+      const size_t ncol = (size_t)L.ncx * L.ncy;
+      prog = std::max(prog, ncol * (size_t)L.ty);
+      mb = std::max(mb, ncol * (size_t)nb * (size_t)(L.tx + L.ty) * (size_t)L.esize);
+    }
+    c->progress_ints = prog;
+    if ((e = cudaMalloc(&c->progress, prog * 4)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&c->mailbox, mb)) != cudaSuccess) return fail(e);
+    c->mailbox_bytes = mb;
+  }
   if ((e = cudaMalloc(&c->ticket, 16)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->dstat, sizeof(DevStatus))) != cudaSuccess) return fail(e);
   if ((e = cudaHostAlloc(&c->hstat, sizeof(DevStatus), cudaHostAllocDefault)) != cudaSuccess) return fail(e);
   {
-    std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy), w64 = wavefront_order(c->L64.ncx, c->L64.ncy);
+    std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
+                     w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
     if ((e = cudaMalloc(&c->order32, w32.size() * 4)) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&c->order64, w64.size() * 4)) != cudaSuccess) return fail(e);
     if ((e = cudaMemcpy(c->order32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
@@ -308,6 +335,8 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((e = cudaMemsetAsync(c->fmask, 0, c->M.words * 4, c->st)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->e0)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->e1)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->k0)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->k1)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) return fail(e);
   *out = c;
   return PDFS_OK;
@@ -325,11 +354,14 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   cudaFree(c->order32);
   cudaFree(c->order64);
   cudaFree(c->progress);
+  cudaFree(c->mailbox);
   cudaFree(c->ticket);
   cudaFree(c->dstat);
   if (c->hstat) cudaFreeHost(c->hstat);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
+  if (c->k0) cudaEventDestroy(c->k0);
+  if (c->k1) cudaEventDestroy(c->k1);
   if (c->st) cudaStreamDestroy(c->st);
   cudaGetLastError();
   delete c;
@@ -411,12 +443,11 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, floa
   SweepArgs a;
   std::memset(&a, 0, sizeof(a));
   a.u = f32 ? (void *)c->u32 : (void *)c->u64;
-  a.cap = which == 2 ? (const void *)c->in64 : nullptr;
   a.fmask = c->has_mask ? c->fmask : nullptr;
   a.px = L.px;
   a.plane = L.plane;
-  a.fpw = c->M.fpw;
-  a.fplane = c->M.fplane;
+  a.mask_fy = c->M.fy;
+  a.mask_fw = c->M.fw;
   a.nx = g.nx;
   a.ny = g.ny;
   a.nz = g.nz;
@@ -424,19 +455,21 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, floa
   a.ncx = L.ncx;
   a.ncy = L.ncy;
   a.order = f32 ? c->order32 : c->order64;
-  a.progress = c->progress;
+  a.prog = c->progress;
+  a.nbands = mailbox_chunks(g.nz);
+  a.xstride = (long long)a.nbands * kMailboxChunk * L.ty;
+  a.ystride = (long long)a.nbands * kMailboxChunk * L.tx;
+  a.xbox = c->mailbox;
+  a.ybox = (char *)c->mailbox + (size_t)L.ncx * L.ncy * a.xstride * L.esize;
   a.ticket = c->ticket;
   a.err = c->dstat->err;
   a.maxchg = &c->dstat->chg;
-  a.blk_active = active;
-  a.blk_chg = blk_chg;
-  a.nbx = (g.nx + 7) / 8;
-  a.nby = (g.ny + 7) / 8;
-  a.nbz = (g.nz + 7) / 8;
+  (void)active;
+  (void)blk_chg;
   a.hmin = (float)std::min(g.dx, std::min(g.dy, g.dz));
   long long wait_ms = c->o.spin_limit > 0 ? c->o.spin_limit : 4000;
   if (getenv("PDFS_WAIT_MS")) wait_ms = atoll(getenv("PDFS_WAIT_MS"));
-  a.wait_ns = wait_ms * 1000000LL;
+  a.wait_cycles = wait_ms * 1000000LL * 21 / 10;  // at most 2.07 GHz: never shorter than wait_ms
   a.poison_col = getenv("PDFS_TEST_POISON_COLUMN") ? atoi(getenv("PDFS_TEST_POISON_COLUMN")) : -1;
   const double h[3] = {g.dx, g.dy, g.dz};
   for (int i = 0; i < 3; ++i) {
@@ -454,18 +487,23 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, floa
   a.k32.iso_h2 = (float)(g.dx * g.dx);
   const bool iso = g.dx == g.dy && g.dy == g.dz;
 
-  CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * 4, c->st));
+  CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
   CK(cudaMemsetAsync(c->dstat, 0, sizeof(DevStatus), c->st));
   const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : ARITH_FAST;
   int grid = 0;
-  CK(launch_sweep(which, f32 ? c->t32 : c->t64, arith, iso, a, c->sms, c->st, &grid));
+  CK(cudaEventRecord(c->k0, c->st));
+  CK(launch_sweep(which, f32 ? c->t32 : c->t64, arith, iso, a, L, which == 2 ? (const void *)c->in64 : nullptr,
+                  c->sms, c->st, &grid));
+  CK(cudaEventRecord(c->k1, c->st));
   CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  c->kern_ms += ms_between(c->k0, c->k1);
+  c->launches++;
   if (c->hstat->err[0]) {
     if (verbose(c->o))
-      fprintf(stderr, "pdfs: sweep sn=%d timed out waiting on column %d\n", sn, c->hstat->err[2]);
-    return PDFS_ERR_TIMEOUT;
+      fprintf(stderr, "pdfs: sweep sn=%d device error %d (column %d)\n", sn, c->hstat->err[0], c->hstat->err[2]);
+    return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
   }
   if (chg) {
     if (f32) {
@@ -487,6 +525,7 @@ static int widen(pdfs_ctx *c) {
   dim3 grid(g.ny + 2, g.nz + 2);
   k_widen<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64, c->has_mask ? c->fmask : nullptr, c->M,
                                    g.nx, g.ny, g.nz);
+  c->launches++;
   CK(cudaGetLastError());
   return PDFS_OK;
 }
@@ -495,6 +534,7 @@ static int narrow(pdfs_ctx *c) {  // FP64 input -> FP32 working field
   const pdfs_grid &g = c->g;
   dim3 grid(g.ny + 2, g.nz + 2);
   k_convert<double, float><<<grid, 128, 0, c->st>>>(c->in64, c->L64, c->u32, c->L32, g.nx);
+  c->launches++;
   CK(cudaGetLastError());
   return PDFS_OK;
 }
@@ -506,6 +546,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   pdfs_stats st;
   std::memset(&st, 0, sizeof(st));
   st.tile = c->t32 | (c->t64 << 8);
+  c->launches = 0;
   const pdfs_opts &o = c->o;
   const pdfs_grid &g = c->g;
   const long long nodes = (long long)g.nx * g.ny * g.nz;
@@ -514,7 +555,8 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   int rc = PDFS_OK;
   double chg = 0.0;
 
-  auto phase = [&](int which, double tol, int *count, double *ms) -> int {
+  auto phase = [&](int which, double tol, int *count, double *ms, double *kms) -> int {
+    c->kern_ms = 0.0;
     CK(cudaEventRecord(c->e0, c->st));
     int s = 0;
     for (;;) {
@@ -535,6 +577,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     CK(cudaEventSynchronize(c->e1));
     *count += s;
     *ms += ms_between(c->e0, c->e1);
+    *kms += c->kern_ms;
     st.final_change = chg;
     return PDFS_OK;
   };
@@ -542,21 +585,22 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   int r = PDFS_OK;
   if (o.precision == PDFS_PREC_FP64) {
     CK(cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st));
-    r = phase(1, o.tol, &st.sweeps_fp64, &st.ms_fp64);
+    r = phase(1, o.tol, &st.sweeps_fp64, &st.ms_fp64, &st.ms_kern_fp64);
     c->last_prec = 1;
   } else {
     if ((r = narrow(c))) return r;
     const double tol32 = 4.0e-6;  // relative; FP32 rounding creep stays ~1e-7
-    r = phase(0, tol32, &st.sweeps_fp32, &st.ms_fp32);
+    r = phase(0, tol32, &st.sweeps_fp32, &st.ms_fp32, &st.ms_kern_fp32);
     c->last_prec = 0;
     if (!r && o.precision == PDFS_PREC_FP32_POLISH64 && o.fixed_sweeps == 0) {
       if ((r = widen(c))) return r;
-      r = phase(2, o.tol, &st.sweeps_fp64, &st.ms_fp64);
+      r = phase(2, o.tol, &st.sweeps_fp64, &st.ms_fp64, &st.ms_kern_fp64);
       c->last_prec = 1;
     }
   }
   if (!r) r = rc;
   st.status = r;
+  st.launches = c->launches;
   st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats) *stats = st;
   if (verbose(o))

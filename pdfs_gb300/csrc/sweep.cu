@@ -1,73 +1,131 @@
-// sweep.cu -- instantiations and launcher of the column-pipelined sweep kernels.
+// sweep.cu -- instantiations and launcher of the warp-specialised sweep kernels.
+#include <cudaTypedefs.h>
+
+
 #include "internal.h"
 
 namespace pdfs {
 
-// FP32 tiles: 32 lanes span x so each warp reads one smem row (bank-conflict
-// free without a swizzle); TY sets the skew (TX+TY-2) and the column count.
-static const TileShape kTiles32[] = {{32, 8, 4}, {32, 4, 4}, {32, 16, 2}, {32, 8, 2}};
-// FP64 tiles: a 16-lane half warp reads 128 contiguous bytes per row.
-static const TileShape kTiles64[] = {{16, 8, 2}, {32, 8, 2}, {16, 16, 2}, {32, 4, 2}};
+// Tile variants: columns are 32 nodes wide (one warp lane per x); TY rows,
+// R rows per compute warp.  {tx, ty, rows per warp}
+static const TileShape kT32[] = {{32, 8, 2}, {32, 8, 4}, {32, 16, 4}, {32, 8, 1}, {32, 4, 2}};
+static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}};
 
-int tile_count32() { return (int)(sizeof(kTiles32) / sizeof(kTiles32[0])); }
-int tile_count64() { return (int)(sizeof(kTiles64) / sizeof(kTiles64[0])); }
-TileShape tile32(int id) { return kTiles32[(id >= 1 && id <= tile_count32()) ? id - 1 : 0]; }
-TileShape tile64(int id) { return kTiles64[(id >= 1 && id <= tile_count64()) ? id - 1 : 0]; }
+int tile_count32() { return (int)(sizeof(kT32) / sizeof(kT32[0])); }
+int tile_count64() { return (int)(sizeof(kT64) / sizeof(kT64[0])); }
+TileShape tile32(int id) { return kT32[(id >= 1 && id <= tile_count32()) ? id - 1 : 0]; }
+TileShape tile64(int id) { return kT64[(id >= 1 && id <= tile_count64()) ? id - 1 : 0]; }
 
-template <class T, int TX, int TY, int C, int MODE, int ARITH, bool ISO>
-static cudaError_t launch_one(const SweepArgs &a, int sms, cudaStream_t st, int *grid_used) {
-  auto kern = col_sweep_kernel<T, TX, TY, C, MODE, ARITH, ISO>;
-  const size_t smem = ColGeo<T, TX, TY, C>::smem_bytes(MODE == MODE_REPLACE);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 3-D tiled map over an internal-layout field: dims {px, ry, nz+2}, box {bx, by, 1}.
+cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  cuuint64_t dims[3] = {(cuuint64_t)L.px, (cuuint64_t)L.ry, (cuuint64_t)nplanes};
+  cuuint64_t strides[2] = {(cuuint64_t)L.px * esize, (cuuint64_t)L.plane * esize};
+  cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = fn(m, esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims,
+                  strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// Frozen-mask map: 32-bit words, dims {fy, fw, nz+2}, box {TY, 1, 1}.
+static cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  cuuint64_t dims[3] = {(cuuint64_t)a.mask_fy, (cuuint64_t)a.mask_fw, (cuuint64_t)(a.nz + 2)};
+  cuuint64_t strides[2] = {(cuuint64_t)a.mask_fy * 4, (cuuint64_t)(a.mask_fy * a.mask_fw) * 4};
+  cuuint32_t box[3] = {(cuuint32_t)ty, 1, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint32_t *>(a.fmask), dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+template <class T, int TY, int R, int MODE, int ARITH, bool ISO>
+static cudaError_t launch_one(const SweepArgs &a, const Layout &L, const void *cap, int sms, cudaStream_t st,
+                              int *grid_used) {
+  using G = WsGeo<T, TY, R, MODE>;
+  auto kern = ws_sweep_kernel<T, TY, R, MODE, ARITH, ISO>;
+  CUtensorMap tm_u, tm_cap, tm_mask;
+  cudaError_t e = encode_field_map(&tm_u, a.u, sizeof(T), L, a.nz + 2, G::W, G::R);
+  if (e != cudaSuccess) return e;
+  if (G::CAP) {
+    e = encode_field_map(&tm_cap, const_cast<void *>(cap), sizeof(T), L, a.nz + 2, G::TX, TY);
+    if (e != cudaSuccess) return e;
+  } else {
+    tm_cap = tm_u;
+  }
+  if (a.fmask) {
+    e = encode_mask_map(&tm_mask, a, TY);
+    if (e != cudaSuccess) return e;
+  } else {
+    tm_mask = tm_u;
+  }
+  const size_t smem = G::BYTES;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * TY, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, G::NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   const int ncol = a.ncx * a.ncy;
   int grid = per_sm * sms;
   if (grid > ncol) grid = ncol;
-  kern<<<grid, TX * TY, smem, st>>>(a);
+  kern<<<grid, G::NT, smem, st>>>(tm_u, tm_cap, tm_mask, a);
   if (grid_used) *grid_used = grid;
   return cudaGetLastError();
 }
 
-#define PDFS_T32(ID, TX, TY, C)                                                               \
-  case ID:                                                                                    \
-    return iso ? launch_one<float, TX, TY, C, MODE_MIN, ARITH_FAST, true>(a, sms, st, g)      \
-               : launch_one<float, TX, TY, C, MODE_MIN, ARITH_FAST, false>(a, sms, st, g);
-#define PDFS_T64(ID, TX, TY, C, MODE)                                                          \
-  case ID:                                                                                     \
-    return arith == ARITH_REF ? launch_one<double, TX, TY, C, MODE, ARITH_REF, false>(a, sms, st, g) \
-                              : launch_one<double, TX, TY, C, MODE, ARITH_FAST, false>(a, sms, st, g);
+#define PDFS_T32(ID, TY, R)                                                                      \
+  case ID:                                                                                       \
+    return iso ? launch_one<float, TY, R, MODE_MIN, ARITH_FAST, true>(a, L, cap, sms, st, g)     \
+               : launch_one<float, TY, R, MODE_MIN, ARITH_FAST, false>(a, L, cap, sms, st, g);
+#define PDFS_T64(ID, TY, R, MODE)                                                                         \
+  case ID:                                                                                                \
+    return arith == ARITH_REF ? launch_one<double, TY, R, MODE, ARITH_REF, false>(a, L, cap, sms, st, g) \
+                              : launch_one<double, TY, R, MODE, ARITH_FAST, false>(a, L, cap, sms, st, g);
 
-cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, int sms,
-                         cudaStream_t st, int *g) {
+cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
+                         const void *cap, int sms, cudaStream_t st, int *g) {
   if (which == 0) {
     switch (tile) {
-      PDFS_T32(1, 32, 8, 4)
-      PDFS_T32(2, 32, 4, 4)
-      PDFS_T32(3, 32, 16, 2)
-      PDFS_T32(4, 32, 8, 2)
+      PDFS_T32(1, 8, 2)
+      PDFS_T32(2, 8, 4)
+      PDFS_T32(3, 16, 4)
+      PDFS_T32(4, 8, 1)
+      PDFS_T32(5, 4, 2)
       default:
         return cudaErrorInvalidValue;
     }
   } else if (which == 1) {
     switch (tile) {
-      PDFS_T64(1, 16, 8, 2, MODE_MIN)
-      PDFS_T64(2, 32, 8, 2, MODE_MIN)
-      PDFS_T64(3, 16, 16, 2, MODE_MIN)
-      PDFS_T64(4, 32, 4, 2, MODE_MIN)
+      PDFS_T64(1, 4, 1, MODE_MIN)
+      PDFS_T64(2, 4, 2, MODE_MIN)
+      PDFS_T64(3, 8, 2, MODE_MIN)
       default:
         return cudaErrorInvalidValue;
     }
   } else {
     switch (tile) {
-      PDFS_T64(1, 16, 8, 2, MODE_REPLACE)
-      PDFS_T64(2, 32, 8, 2, MODE_REPLACE)
-      PDFS_T64(3, 16, 16, 2, MODE_REPLACE)
-      PDFS_T64(4, 32, 4, 2, MODE_REPLACE)
-      default:
+      PDFS_T64(1, 4, 1, MODE_REPLACE)
+      PDFS_T64(2, 4, 2, MODE_REPLACE)
+      default:  // the polish kernel (cap ring) fits shared memory only with TY = 4
         return cudaErrorInvalidValue;
     }
   }

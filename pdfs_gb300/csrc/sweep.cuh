@@ -1,4 +1,4 @@
-// sweep.cuh -- persistent column-pipelined sweep of one FSM ordering.
+// sweep.cuh -- warp-specialised, TMA-fed, column-pipelined sweep of one FSM ordering.
 //
 // The reference sweeps one hyperplane x+y+z = level per kernel launch
 // (single_gpu_cuda/src/phi3D_fsm.cu:161-185, mpi_openacc/src/phi3D_fsm.c:92-117):
@@ -6,28 +6,43 @@
 // Any topological order of an ordering's dependency DAG gives the same
 // result (each node reads the new values of its three upwind neighbours and
 // the old values of its three downwind ones), so this kernel uses a blocked
-// order instead:
+// order instead.
 //
-//   * the x-y plane is cut into TX*TY columns that run the whole z extent;
-//     a CTA owns one column at a time and marches it along z in the sweep's
-//     z direction;
-//   * inside a column, thread (lx, ly) (coordinates in the sweep's direction)
-//     updates plane lz = step - lx - ly at each step, so all TX*TY threads work
-//     on every step (a skewed wavefront, one __syncthreads per step);
-//   * planes stream through a shared-memory ring of D slots by cp.async
-//     (16-byte L2 loads), C planes per chunk, two chunks ahead;
-//   * columns depend on their upwind x and y neighbours only.  Each column
-//     publishes how many planes it has finished (release store); a column
-//     loads a chunk only once both upwind columns have published it (acquire
-//     load, bounded by wall time).  CTAs take columns from an atomic ticket in
-//     wavefront order, so every column a CTA waits on is held by a CTA that is
-//     already running: no deadlock, whatever the grid size.
+// Decomposition.  The x-y plane is cut into columns of 32 x TY nodes that run
+// the whole z extent.  A persistent CTA owns one column at a time (tickets in
+// wavefront order) and marches it along the sweep's z direction:
+//   * compute warp `ly` (row ly of the column in sweep order) has lane `lx`
+//     update plane lz = t - lx - ly at its step t: a skewed wavefront in which
+//     lane lx-1 produced the upwind x value one step earlier (same warp) and
+//     warp ly-1 produced the upwind y value one step earlier;
+//   * warps chain through per-warp step counters in shared memory (release /
+//     acquire), so there is no CTA-wide barrier per step;
+//   * a loader warp streams planes (field, frozen-mask words and, for the
+//     polish, the per-node cap) into a ring of D shared-memory slots with TMA
+//     (cp.async.bulk.tensor, mbarrier full/empty pairs), as far ahead as the
+//     ring allows;
+//   * a communication warp fetches the upwind faces of the neighbouring
+//     columns (all chunks that are ready, in one round trip) and publishes
+//     this column's per-row progress, so the compute warps never wait on a
+//     global fence or a global round trip;
+//   * faces cross columns through diagonal-indexed mailboxes in global memory:
+//     item (row, z) of a column's downwind x face is stored at [z + row][row]
+//     and item (x, z) of its downwind y face at [z + x][x].  A downstream
+//     column at step t needs exactly mailbox row d = t, so each step's halo is
+//     one contiguous run that is written and read with coalesced accesses, and
+//     the downstream column trails its upstream by about TX (or TY) steps;
+//   * every wait is bounded (in SM cycles): on expiry the kernel records
+//     DEV_ERR_TIMEOUT, raises an abort flag, drains its own TMA loads and
+//     returns, so the host gets PDFS_ERR_TIMEOUT and the context stays usable.
 //
 // Memory layout (internal, per element type T, V = 16/sizeof(T)):
 //   element (x, y, z) of the halo-padded grid (0 <= x <= nx+1, ...) lives at
-//   z*plane + y*px + x + (V-1), so interior x = 1 + cx*TX starts on a 16-byte
-//   boundary; px >= ncx*TX + 2V, rows ry = ncy*TY + 2, planes nz + 2.
+//   z*plane + y*px + x + (V-1), so interior x = 1 + cx*32 starts on a 16-byte
+//   boundary (a legal TMA x coordinate); px >= ncx*32 + 2V, rows ry =
+//   ncy*TY + 2, planes nz + 2.
 #pragma once
+#include <cuda.h>
+
 #include <cstdint>
 
 #include "godunov.cuh"
@@ -36,103 +51,129 @@ namespace pdfs {
 
 enum { MODE_MIN = 0, MODE_REPLACE = 1 };
 enum { ARITH_REF = 0, ARITH_FAST = 1 };
-enum { DEV_ERR_TIMEOUT = 1 };
+enum { DEV_ERR_TIMEOUT = 1, DEV_ERR_SMEM_ALIGN = 2 };
 
 struct SweepArgs {
   void *u;                // working field (internal layout)
-  const void *cap;        // MODE_REPLACE: upper bound per node (internal layout, same T)
-  const uint32_t *fmask;  // frozen bit per node, or nullptr
+  const uint32_t *fmask;  // frozen bit per node (MaskLayout), or nullptr
   long long px;           // row pitch (elements)
   long long plane;        // plane stride (elements)
-  long long fpw;          // frozen mask words per row
-  long long fplane;       // frozen mask words per plane
+  long long mask_fy;      // frozen mask: words per 32-wide column of a plane
+  long long mask_fw;      // frozen mask: word columns per plane
   int nx, ny, nz;
   int sx, sy, sz;         // +1 / -1 sweep direction per axis
   int ncx, ncy;           // columns
+  int nbands;             // mailbox chunks per column
   const int *order;       // ticket -> local column id (lcy*ncx + lcx), wavefront order
-  int *progress;          // per global column id: planes finished in this sweep
+  int *prog;              // [column][row]: steps published by each row of each column
+  void *xbox;             // x-face mailboxes, [column][d][row]
+  void *ybox;             // y-face mailboxes, [column][d][x]
+  long long xstride, ystride;  // mailbox elements per column
   int *ticket;            // column ticket counter
   int *err;               // [0] error code, [1] abort flag, [2] column that timed out
   void *maxchg;           // FP32: uint bits of max relative change; FP64: u64 bits of max abs change
-  const uint8_t *blk_active;  // per 8^3 block: visit it (nullptr = all)
-  float *blk_chg;         // per 8^3 block: max change in this sweep (nullptr = not tracked)
-  int nbx, nby, nbz;      // block grid
   float hmin;             // smallest spacing (relative-change floor)
-  long long wait_ns;      // bound on a single inter-column wait
+  long long wait_cycles;  // bound on any single wait, in SM cycles
   int poison_col;         // test hook: this column never publishes (-1 = off)
   GodConst64 k64;
   GodConst32 k32;
 };
 
-template <class T, int TX, int TY, int C>
-struct ColGeo {
+// Shared-memory plan of one kernel variant: columns of 32 x TY nodes, R rows
+// per compute warp (TY/R compute warps).
+template <class T, int TY, int R_, int MODE>
+struct WsGeo {
+  static constexpr int TX = 32;
+  static constexpr int RW = R_;        // rows per compute warp
+  static constexpr int NW = TY / R_;   // compute warps
   static constexpr int V = 16 / (int)sizeof(T);
-  static constexpr int W = TX + 2 * V;  // smem row: x0-V .. x0+TX+V-1
-  static constexpr int R = TY + 2;      // rows y0-1 .. y0+TY
+  static constexpr int W = TX + 2 * V;  // slot row: x0-V .. x0+TX+V-1
+  static constexpr int R = TY + 2;      // slot rows: y0-1 .. y0+TY
   static constexpr int SK = TX + TY - 2;
-  static constexpr int D = SK + 3 * C;  // ring depth (planes)
+  static constexpr int LOOK = sizeof(T) == 8 ? 4 : 8;  // planes the producer may run ahead
+  static constexpr int D = SK + 3 + LOOK;               // ring depth (planes)
   static constexpr int ALIGN = 128 / (int)sizeof(T);
   static constexpr int SLOT = ((R * W + ALIGN - 1) / ALIGN) * ALIGN;
-  static constexpr int NT = TX * TY;
-  static constexpr int CAPSLOT = TX * TY;
-  static size_t smem_bytes(bool with_cap) {
-    size_t b = (size_t)D * SLOT * sizeof(T) + (size_t)D * TY * sizeof(uint32_t);
-    b = (b + 127) & ~size_t(127);
-    if (with_cap) b += (size_t)D * CAPSLOT * sizeof(T);
-    return b;
-  }
+  static constexpr int C = 4;   // steps per mailbox chunk
+  static constexpr int HB = sizeof(T) == 8 ? 4 : 8;  // mailbox chunk ring depth
+  static constexpr int NT = (NW + 2) * 32;  // NW compute warps, a TMA loader warp, a communication warp
+  static constexpr bool CAP = MODE == MODE_REPLACE;
+  static constexpr size_t OFF_RING = 0;
+  static constexpr size_t OFF_CAP = OFF_RING + (size_t)D * SLOT * sizeof(T);
+  static constexpr size_t OFF_FR = OFF_CAP + (CAP ? (size_t)D * TX * TY * sizeof(T) : 0);
+  static constexpr int MSL = 32;  // mask words per slot: 128 bytes, a legal TMA destination
+  static constexpr size_t OFF_XB = OFF_FR + (size_t)D * MSL * 4;
+  static constexpr size_t OFF_YB = OFF_XB + (size_t)HB * C * TY * sizeof(T);
+  static constexpr size_t OFF_BAR = (OFF_YB + (size_t)HB * C * TX * sizeof(T) + 15) & ~size_t(15);
+  static constexpr size_t OFF_DONE = OFF_BAR + (size_t)(2 * D + 2 * HB) * 8;
+  static constexpr size_t BYTES = OFF_DONE + (size_t)NW * 4 + 16;
+  static_assert(TY % R_ == 0, "rows per warp must divide TY");
+  static constexpr unsigned TX_BYTES = (unsigned)(R * W * sizeof(T) + (CAP ? TX * TY * sizeof(T) : 0));
+  static constexpr unsigned MASK_BYTES = TY * 4;
+  // every TMA destination (field slot, cap slot, mask slot) starts on 128 bytes
+  static_assert((SLOT * sizeof(T)) % 128 == 0 && OFF_CAP % 128 == 0 && OFF_FR % 128 == 0, "TMA alignment");
+  static_assert((TX * TY * sizeof(T)) % 128 == 0 && TY * 4 >= 16 && TY <= MSL, "TMA box");
 };
 
-// ---- small PTX helpers -------------------------------------------------------------
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+// ---- PTX helpers ---------------------------------------------------------------------
+__device__ __forceinline__ unsigned saddr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(saddr(b)), "r"(n) : "memory");
 }
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+__device__ __forceinline__ void mbar_inval(uint64_t *b) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(saddr(b)) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(saddr(b)) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-__device__ __forceinline__ int ld_acquire(const int *p) {
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t *b, unsigned parity) {
+  unsigned r;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *b, unsigned parity) {
+  unsigned r;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"(saddr(b)), "r"(parity)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];\n" ::"r"(saddr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(saddr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ int ld_acquire_gpu(const int *p) {
   int v;
   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(int *p, int v) {
-  asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed_gpu(int *p, int v) {
+  asm volatile("st.relaxed.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ unsigned long long globaltimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
-  return t;
+__device__ __forceinline__ int ld_acquire_cta_s(const int *p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared.s32 %0, [%1];\n" : "=r"(v) : "r"(saddr(p)) : "memory");
+  return v;
 }
-
-// Bounded wait until progress[col] >= need.  On timeout: record the error and
-// raise the abort flag so every CTA of the launch drains and returns.
-static __device__ __noinline__ bool wait_progress(const SweepArgs &a, int col, int need) {
-  if (col < 0 || need <= 0) return true;
-  const int *p = a.progress + col;
-  if (ld_acquire(p) >= need) return true;
-  const unsigned long long t0 = globaltimer();
-  unsigned ns = 32;
-  for (;;) {
-    if (ld_acquire(p) >= need) return true;
-    if (*(volatile int *)(a.err + 1)) return false;
-    if (globaltimer() - t0 > (unsigned long long)a.wait_ns) {
-      atomicCAS(a.err, 0, DEV_ERR_TIMEOUT);
-      atomicExch(a.err + 2, col);
-      atomicExch(a.err + 1, 1);
-      return false;
-    }
-    __nanosleep(ns);
-    if (ns < 256) ns <<= 1;
-  }
+__device__ __forceinline__ void st_release_cta_s(int *p, int v) {
+  asm volatile("st.release.cta.shared.s32 [%0], %1;\n" ::"r"(saddr(p)), "r"(v) : "memory");
 }
+// Wait bounds are counted in SM cycles (clock64() is a register read).
+__device__ __forceinline__ long long cycles() { return clock64(); }
 
 template <class T>
 __device__ __forceinline__ T tmin(T a, T b) {  // the reference's min macro: a < b ? a : b
@@ -144,12 +185,12 @@ __device__ __forceinline__ T local_update(T m0, T m1, T m2, const SweepArgs &a);
 template <>
 __device__ __forceinline__ float local_update<float, MODE_MIN, ARITH_FAST, true>(float m0, float m1, float m2,
                                                                                   const SweepArgs &a) {
-  return god32<true>(m0, m1, m2, a.k32);
+  return god32s<true>(m0, m1, m2, a.k32);
 }
 template <>
 __device__ __forceinline__ float local_update<float, MODE_MIN, ARITH_FAST, false>(float m0, float m1, float m2,
                                                                                    const SweepArgs &a) {
-  return god32<false>(m0, m1, m2, a.k32);
+  return god32s<false>(m0, m1, m2, a.k32);
 }
 #define PDFS_LU64(MODE_, ARITH_, FN)                                                                  \
   template <>                                                                                         \
@@ -164,45 +205,98 @@ PDFS_LU64(MODE_REPLACE, ARITH_REF, god_ref64)
 PDFS_LU64(MODE_REPLACE, ARITH_FAST, god_fast64)
 #undef PDFS_LU64
 
-template <class T, int TX, int TY, int C, int MODE, int ARITH, bool ISO>
-__global__ void __launch_bounds__(TX *TY) col_sweep_kernel(const SweepArgs a) {
-  using G = ColGeo<T, TX, TY, C>;
-  constexpr int V = G::V, W = G::W, R = G::R, SK = G::SK, D = G::D, SLOT = G::SLOT, NT = G::NT;
-  constexpr int NV = W / V;  // 16-byte vectors per smem row
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  T *ring = reinterpret_cast<T *>(smem_raw);
-  uint32_t *fring = reinterpret_cast<uint32_t *>(ring + (size_t)D * SLOT);
-  T *cring = reinterpret_cast<T *>(smem_raw + ((((size_t)D * SLOT * sizeof(T) + (size_t)D * TY * 4) + 127) & ~size_t(127)));
+// Records a timeout and raises the abort flags (global and CTA).
+__device__ __forceinline__ void raise_timeout(const SweepArgs &a, int col, volatile int *s_abort) {
+  atomicCAS(a.err, 0, DEV_ERR_TIMEOUT);
+  atomicExch(a.err + 2, col);
+  atomicExch(a.err + 1, 1);
+  *s_abort = 1;
+}
+
+// Bounded wait on an mbarrier phase; false on abort or timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity, const SweepArgs &a, int col,
+                                          volatile int *s_abort) {
+  if (mbar_try(b, parity)) return true;
+  const long long t0 = cycles();
+  for (;;) {
+    if (mbar_try(b, parity)) return true;
+    if (*s_abort) return false;
+    if (cycles() - t0 > a.wait_cycles) {
+      raise_timeout(a, col, s_abort);
+      return false;
+    }
+  }
+}
+
+template <class T, int TY, int R, int MODE, int ARITH, bool ISO>
+__global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
+                                                                     const __grid_constant__ CUtensorMap tm_cap,
+                                                                     const __grid_constant__ CUtensorMap tm_mask,
+                                                                     const SweepArgs a) {
+  using G = WsGeo<T, TY, R, MODE>;
+  constexpr int TX = G::TX, V = G::V, W = G::W, D = G::D, SLOT = G::SLOT, C = G::C, HB = G::HB, NW = G::NW;
+  static_assert((C & (C - 1)) == 0 && (HB & (HB - 1)) == 0, "power-of-two chunk sizes");
+  extern __shared__ __align__(1024) unsigned char sm[];
+  T *ring = reinterpret_cast<T *>(sm + G::OFF_RING);
+  T *capr = reinterpret_cast<T *>(sm + G::OFF_CAP);
+  uint32_t *fring = reinterpret_cast<uint32_t *>(sm + G::OFF_FR);
+  T *xband = reinterpret_cast<T *>(sm + G::OFF_XB);
+  T *yband = reinterpret_cast<T *>(sm + G::OFF_YB);
+  uint64_t *full = reinterpret_cast<uint64_t *>(sm + G::OFF_BAR);
+  uint64_t *empty = full + D;
+  uint64_t *bfull = empty + D;
+  uint64_t *bempty = bfull + HB;
+  int *done = reinterpret_cast<int *>(sm + G::OFF_DONE);  // per compute warp: steps completed
   __shared__ int s_ticket;
-  __shared__ int s_stop;      // written by thread 0 before the ticket barrier
-  __shared__ int s_stopk[2];  // per chunk parity: a slot is rewritten only two chunks later
-  __shared__ T s_red[NT / 32];
+  __shared__ volatile int s_abort;
+  __shared__ T s_red[NW];
+
+  // TMA needs 128-byte aligned shared-memory destinations: refuse to start otherwise
+  if ((saddr(sm) & 127u) != 0) {
+    if (threadIdx.x == 0) {
+      atomicCAS(a.err, 0, DEV_ERR_SMEM_ALIGN);
+      atomicExch(a.err + 1, 1);
+    }
+    return;
+  }
 
   T *__restrict__ u = reinterpret_cast<T *>(a.u);
-  const T *__restrict__ capg = reinterpret_cast<const T *>(a.cap);
-  const int tid = threadIdx.x;
-  const int gxo = tid % TX, gyo = tid / TX;  // position in global orientation
-  const int lx = a.sx > 0 ? gxo : TX - 1 - gxo;
-  const int ly = a.sy > 0 ? gyo : TY - 1 - gyo;
-  const int skew = lx + ly;
+  T *__restrict__ xbox = reinterpret_cast<T *>(a.xbox);
+  T *__restrict__ ybox = reinterpret_cast<T *>(a.ybox);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ncol = a.ncx * a.ncy;
-  const int nz = a.nz;
-  const int nplanes = nz + 2;
-  const int nsteps = nz + SK;
-  const int nphase = (nsteps + C - 1) / C;
-  const int o = (gyo + 1) * W + gxo + V;  // my node inside a ring slot
-  // global-orientation z neighbours: local p-1 is global z-1 when sz > 0
-  const int zlo = a.sz > 0 ? -1 : 1;
+  const int nz = a.nz, NP = nz + 2, NB = a.nbands;
+  const int tsteps = max(nz + TX + TY + 1, NB * C);  // steps every compute warp runs per column
+  const bool masked = a.fmask != nullptr;
   T tmax = T(0);
 
-  for (;;) {
+  if (tid == 0) s_abort = 0;
+  for (int ncols_done = 0;; ++ncols_done) {
     if (tid == 0) {
       s_ticket = atomicAdd(a.ticket, 1);
-      s_stop = *(volatile int *)(a.err + 1);
+      if (*(volatile int *)(a.err + 1)) s_abort = 1;
+      for (int i = 0; i < D; ++i) {
+        if (ncols_done) {
+          mbar_inval(full + i);
+          mbar_inval(empty + i);
+        }
+        mbar_init(full + i, 1);
+        mbar_init(empty + i, NW);
+      }
+      for (int i = 0; i < HB; ++i) {
+        if (ncols_done) {
+          mbar_inval(bfull + i);
+          mbar_inval(bempty + i);
+        }
+        mbar_init(bfull + i, 1);
+        mbar_init(bempty + i, NW);
+      }
+      mbar_fence_init();
     }
+    if (tid < NW) done[tid] = 0;
     __syncthreads();
     const int tk = s_ticket;
-    if (tk >= ncol || s_stop) break;
+    if (tk >= ncol || s_abort) break;
     const int lc = a.order[tk];
     const int lcx = lc % a.ncx, lcy = lc / a.ncx;
     const int cx = a.sx > 0 ? lcx : a.ncx - 1 - lcx;
@@ -210,133 +304,289 @@ __global__ void __launch_bounds__(TX *TY) col_sweep_kernel(const SweepArgs a) {
     const int col = cy * a.ncx + cx;
     const int upx = lcx > 0 ? col - a.sx : -1;
     const int upy = lcy > 0 ? col - a.sy * a.ncx : -1;
+    const bool has_dnx = lcx < a.ncx - 1, has_dny = lcy < a.ncy - 1;
     const int x0 = 1 + cx * TX, y0 = 1 + cy * TY;
-    const bool valid = (x0 + gxo <= a.nx) && (y0 + gyo <= a.ny);
     const long long rowbase = (long long)cx * TX;  // internal x index of x0 - V
 
-    // Issues the loads of chunk k (planes p = k*C .. k*C+C-1, p = lz + 1) once
-    // the upwind columns have finished them.  Collective; false = abort.
-    auto load_chunk = [&](int k) -> bool {
-      const int p0 = k * C;
-      if (p0 < nplanes) {
-        if (tid == 0) {
-          const int need = min(nz, p0 + C - 1);
-          const bool ok = wait_progress(a, upx, need) && wait_progress(a, upy, need);
-          s_stopk[k & 1] = ok ? 0 : 1;
-        }
-        __syncthreads();
-        if (s_stopk[k & 1]) return false;
-        for (int i = tid; i < C * R * NV; i += NT) {
-          const int v = i % NV;
-          const int rr = (i / NV) % R;
-          const int p = p0 + i / (NV * R);
-          if (p < nplanes) {
-            const int gz = a.sz > 0 ? p : nz + 1 - p;
-            const T *src = u + (long long)gz * a.plane + (long long)(y0 - 1 + rr) * a.px + rowbase + v * V;
-            cp_async16(ring + (p % D) * SLOT + rr * W + v * V, src);
-          }
-        }
-        if (a.fmask) {
-          for (int i = tid; i < C * TY; i += NT) {
-            const int p = p0 + i / TY, r = i % TY;
-            if (p < nplanes) {
-              const int gz = a.sz > 0 ? p : nz + 1 - p;
-              cp_async4(fring + (p % D) * TY + r,
-                        a.fmask + (long long)gz * a.fplane + (long long)(y0 + r) * a.fpw + (x0 - 1) / 32);
+    if (warp == NW) {
+      // ---------------------------- TMA loader warp (lane 0) ----------------------------
+      if (lane == 0) {
+        int pl = 0;
+        long long t_last = cycles();
+        while (pl < NP) {
+          const int s = pl % D, use = pl / D;
+          if (use == 0 || mbar_test(empty + s, (use - 1) & 1)) {
+            const int gz = a.sz > 0 ? pl : nz + 1 - pl;
+            mbar_arrive_tx(full + s, G::TX_BYTES + (masked ? G::MASK_BYTES : 0u));
+            tma_load_3d(ring + (size_t)s * SLOT, &tm_u, (int)rowbase, y0 - 1, gz, full + s);
+            if (G::CAP) tma_load_3d(capr + (size_t)s * TX * TY, &tm_cap, (int)rowbase + V, y0, gz, full + s);
+            if (masked) tma_load_3d(fring + s * G::MSL, &tm_mask, y0 - 1, cx, gz, full + s);
+            ++pl;
+            t_last = cycles();
+          } else {
+            if (s_abort) break;
+            if (cycles() - t_last > a.wait_cycles) {
+              raise_timeout(a, col, &s_abort);
+              break;
             }
+            __nanosleep(64);
           }
         }
-        if (MODE == MODE_REPLACE) {
-          constexpr int CV = TX / V;
-          for (int i = tid; i < C * TY * CV; i += NT) {
-            const int v = i % CV;
-            const int r = (i / CV) % TY;
-            const int p = p0 + i / (CV * TY);
-            if (p < nplanes) {
-              const int gz = a.sz > 0 ? p : nz + 1 - p;
-              const T *src = capg + (long long)gz * a.plane + (long long)(y0 + r) * a.px + rowbase + V + v * V;
-              cp_async16(cring + (p % D) * G::CAPSLOT + r * TX + v * V, src);
+        if (s_abort) {
+          // drain the TMA loads still in flight before the CTA leaves
+          for (int q = max(0, pl - D); q < pl; ++q) {
+            const long long t0 = cycles();
+            while (!mbar_try(full + q % D, (q / D) & 1) && cycles() - t0 < 4000000000ll) {
             }
           }
         }
       }
-      cp_async_commit();
-      return true;
-    };
+    } else if (warp == NW + 1) {
+      // ------------------------------ communication warp ------------------------------
+      // Fills the mailbox-chunk ring from the upwind columns' mailboxes (every
+      // ready chunk with a free slot, in one round trip) and publishes this
+      // column's per-row progress.
+      int kb = 0, pub = 0;
+      long long t_last = cycles();
+      for (;;) {
+        bool moved = false;
+        if (kb < NB) {
+          // chunk k is complete once the row's progress >= k*C + C + TX - 1
+          // (x face) / + TY - 1 (y face), or once the column is done
+          int rdy = NB;
+          if (upx >= 0 && lane < TY) {
+            const int v = ld_acquire_gpu(a.prog + (long long)upx * TY + lane);
+            rdy = v >= tsteps ? NB : max(0, (v - TX + 1) / C);
+          }
+          if (upy >= 0 && lane == TY) {
+            const int v = ld_acquire_gpu(a.prog + (long long)upy * TY + (TY - 1));
+            rdy = v >= tsteps ? NB : max(0, (v - TY + 1) / C);
+          }
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) rdy = min(rdy, __shfl_xor_sync(0xffffffffu, rdy, off));
+          int n = 0;  // chunks to fill now: ready and with a free slot
+          while (kb + n < min(rdy, NB) && n < HB) {
+            const int k = kb + n, useb = k / HB;
+            if (useb > 0 && !mbar_test(bempty + k % HB, (useb - 1) & 1)) break;
+            ++n;
+          }
+          if (n > 0) {
+            if (upx >= 0)
+              for (int i = lane; i < n * C * TY; i += 32) {
+                const int k = kb + i / (C * TY);
+                xband[(k % HB) * C * TY + i % (C * TY)] =
+                    __ldcg(xbox + (long long)upx * a.xstride + (long long)kb * C * TY + i);
+              }
+            if (upy >= 0)
+              for (int i = lane; i < n * C * TX; i += 32) {
+                const int k = kb + i / (C * TX);
+                yband[(k % HB) * C * TX + i % (C * TX)] =
+                    __ldcg(ybox + (long long)upy * a.ystride + (long long)kb * C * TX + i);
+              }
+            __syncwarp();
+            if (lane < n) mbar_arrive(bfull + (kb + lane) % HB);
+            kb += n;
+            moved = true;
+          }
+        }
+        {  // publish this column's progress, row by row (row ly belongs to compute warp ly / R)
+          bool need = false;
+          int dv = 0;
+          if (lane < TY) {
+            dv = ld_acquire_cta_s(done + lane / R);
+            need = dv > pub;
+          }
+          if (__any_sync(0xffffffffu, need)) {
+            __threadfence();
+            if (need) {
+              if (col != a.poison_col) st_relaxed_gpu(a.prog + (long long)col * TY + lane, dv);
+              pub = dv;
+            }
+            moved = true;
+          }
+        }
+        const bool published = __all_sync(0xffffffffu, lane >= TY || pub == tsteps);
+        if (kb >= NB && published) break;
+        if (moved) {
+          t_last = cycles();
+        } else {
+          if (s_abort || *(volatile int *)(a.err + 1)) {
+            s_abort = 1;
+            break;
+          }
+          if (cycles() - t_last > a.wait_cycles) {
+            if (lane == 0) raise_timeout(a, col, &s_abort);
+            s_abort = 1;
+            break;
+          }
+          __nanosleep(128);
+        }
+      }
+    } else {
+      // ------------------------------- compute warps -------------------------------
+      // warp w owns rows ly = w*R + r (sweep order); lane = global x offset.
+      // At step t, lane lx of row ly updates plane lz = t - lx - ly.
+      const int w = warp;
+      const int ly0 = w * R;
+      const int lx = a.sx > 0 ? lane : TX - 1 - lane;
+      int o[R], gy[R];
+      bool valid[R];
+      long long grow[R];  // global row offset of my node (without the plane term)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int ly = ly0 + r;
+        gy[r] = a.sy > 0 ? ly : TY - 1 - ly;
+        valid[r] = (y0 + gy[r] <= a.ny) && (x0 + lane <= a.nx);
+        o[r] = (gy[r] + 1) * W + lane + V;
+        grow[r] = (long long)(y0 + gy[r]) * a.px + rowbase + V + lane;
+      }
+      const bool band_x = (lx == 0) && (upx >= 0);
+      const bool band_y = (w == 0) && (upy >= 0);
+      const bool wr_x = (lx == TX - 1) && has_dnx;
+      const bool wr_y = (w == NW - 1) && has_dny;
+      const int xm = a.sx > 0 ? -1 : 1;           // smem offset of the upwind x neighbour
+      const int ym = a.sy > 0 ? -W : W;           // smem offset of the upwind y neighbour
+      const int zlo_slot = a.sz > 0 ? -1 : 1;     // ring step to the global z-1 plane
+      T *xout = xbox + (long long)col * a.xstride;
+      T *yout = ybox + (long long)col * a.ystride;
+      // ring slot of plane p = lz + 1 of row 0 at step t (per lane), and of
+      // the write-back plane of row 0 (lane TX-1's plane, uniform)
+      int s0 = (1 - lx - ly0) % D;
+      if (s0 < 0) s0 += D;
+      int swb = (1 - (TX - 1) - ly0) % D;
+      if (swb < 0) swb += D;
+      int qw = 0, qslot = 0, qpar = 0;  // next plane to wait for, its slot and phase parity
+      for (int t = 0; t < tsteps; ++t) {
+        if (w > 0 && ld_acquire_cta_s(done + w - 1) < t) {
+          const long long t0 = cycles();
+          while (ld_acquire_cta_s(done + w - 1) < t) {
+            if (s_abort) break;
+            if (cycles() - t0 > a.wait_cycles) {
+              if (lane == 0) raise_timeout(a, col, &s_abort);
+              break;
+            }
+          }
+          if (__any_sync(0xffffffffu, s_abort != 0)) break;
+        }
+        const int qneed = min(t - ly0 + 2, NP - 1);
+        bool ok = true;
+        while (ok && qw <= qneed) {
+          ok = mbar_wait(full + qslot, qpar, a, col, &s_abort);
+          ++qw;
+          if (++qslot == D) {
+            qslot = 0;
+            qpar ^= 1;
+          }
+        }
+        const int kb = t / C;
+        const int tc = t & (C - 1);
+        if (ok && tc == 0 && kb < NB) ok = mbar_wait(bfull + (kb & (HB - 1)), (kb / HB) & 1, a, col, &s_abort);
+        if (!__all_sync(0xffffffffu, ok)) break;
 
-    bool ok = load_chunk(0) && load_chunk(1);
-    for (int k = 0; ok && k < nphase; ++k) {
-      if (!load_chunk(k + 2)) {
-        ok = false;
-        break;
-      }
-      cp_async_wait<1>();
-      __syncthreads();
+        // Rows of one step are independent (different planes), so the step is
+        // split into a load phase, a compute phase and a store phase: the R
+        // update chains then overlap instead of waiting on each other's stores.
+        bool act[R];
+        T cv[R], m0[R], m1[R], m2[R], capv[R];
+        int sr[R];
 #pragma unroll
-      for (int s = 0; s < C; ++s) {
-        const int lz = k * C + s - skew;
-        if (valid && lz >= 0 && lz < nz) {
-          const int p = lz + 1;
-          T *sl = ring + (p % D) * SLOT;
-          const T c = sl[o];
-          bool frz = false;
-          if (a.fmask) frz = (fring[(p % D) * TY + gyo] >> ((x0 - 1 + gxo) & 31)) & 1u;
-          if (!frz) {
-            const T *zl = ring + ((p + zlo) % D) * SLOT;  // global z-1
-            const T *zh = ring + ((p - zlo) % D) * SLOT;  // global z+1
-            const T m0 = tmin(sl[o - 1], sl[o + 1]);
-            const T m1 = tmin(sl[o - W], sl[o + W]);
-            const T m2 = tmin(zl[o], zh[o]);
-            const T g = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, a);
-            T nv;
-            if (MODE == MODE_REPLACE)
-              nv = tmin(cring[(p % D) * G::CAPSLOT + gyo * TX + gxo], g);
-            else
-              nv = tmin(c, g);
-            if (nv != c) {
-              sl[o] = nv;
-              T d;
-              if (sizeof(T) == 4)
-                d = (T)(fabsf((float)c - (float)nv) / fmaxf((float)nv, a.hmin));
-              else
-                d = (T)fabs((double)c - (double)nv);
-              tmax = fmax(tmax, d);
-            }
+        for (int r = 0; r < R; ++r) {
+          const int lz = t - lx - ly0 - r;
+          int sx_ = s0 - r;
+          if (sx_ < 0) sx_ += D;
+          sr[r] = sx_;
+          act[r] = valid[r] && (unsigned)lz < (unsigned)nz;
+          if (act[r] && masked) act[r] = !((fring[sx_ * G::MSL + gy[r]] >> lane) & 1u);
+          cv[r] = T(0);
+          m0[r] = m1[r] = m2[r] = capv[r] = T(0);
+          if (valid[r] && (unsigned)lz < (unsigned)nz) {
+            const T *sl = ring + sx_ * SLOT + o[r];
+            cv[r] = sl[0];
+            T up_x = sl[xm], dn_x = sl[-xm], up_y = sl[ym], dn_y = sl[-ym];
+            if (band_x) up_x = xband[(kb & (HB - 1)) * C * TY + tc * TY + ly0 + r];
+            if (r == 0 && band_y) up_y = yband[(kb & (HB - 1)) * C * TX + tc * TX + lx];
+            int sz_lo = sx_ + zlo_slot, sz_hi = sx_ - zlo_slot;
+            sz_lo = sz_lo < 0 ? sz_lo + D : (sz_lo >= D ? sz_lo - D : sz_lo);
+            sz_hi = sz_hi < 0 ? sz_hi + D : (sz_hi >= D ? sz_hi - D : sz_hi);
+            const T zl = ring[sz_lo * SLOT + o[r]], zh = ring[sz_hi * SLOT + o[r]];
+            // the reference's minima keep global orientation: min(u[x-1], u[x+1])
+            const T xl = a.sx > 0 ? up_x : dn_x, xr = a.sx > 0 ? dn_x : up_x;
+            const T yd = a.sy > 0 ? up_y : dn_y, yu = a.sy > 0 ? dn_y : up_y;
+            m0[r] = tmin(xl, xr);
+            m1[r] = tmin(yd, yu);
+            m2[r] = tmin(zl, zh);
+            if (MODE == MODE_REPLACE) capv[r] = capr[sx_ * TX * TY + gy[r] * TX + lane];
           }
         }
-        __syncthreads();
-      }
-      // planes lz in [kC-SK, kC+C-SK) are now complete: write my nodes back
+        T nv[R];
 #pragma unroll
-      for (int j = 0; j < C; ++j) {
-        const int lz = k * C - SK + j;
-        if (valid && lz >= 0 && lz < nz) {
-          const int p = lz + 1;
-          const int gz = a.sz > 0 ? p : nz + 1 - p;
-          u[(long long)gz * a.plane + (long long)(y0 + gyo) * a.px + rowbase + V + gxo] =
-              ring[(p % D) * SLOT + o];
+        for (int r = 0; r < R; ++r) {
+          nv[r] = cv[r];
+          if (act[r]) {
+            const T g = local_update<T, MODE, ARITH, ISO>(m0[r], m1[r], m2[r], a);
+            nv[r] = MODE == MODE_REPLACE ? tmin(capv[r], g) : tmin(cv[r], g);
+          }
         }
-      }
-      __syncthreads();
-      if (tid == 0) {
-        __threadfence();
-        if (col != a.poison_col) st_release(a.progress + col, max(0, min(nz, k * C + C - SK)));
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int lz = t - lx - ly0 - r;
+          if (act[r] && nv[r] != cv[r]) {
+            ring[sr[r] * SLOT + o[r]] = nv[r];
+            if (sizeof(T) == 4)
+              tmax = fmax(tmax, (T)__fdividef(fabsf((float)cv[r] - (float)nv[r]), fmaxf((float)nv[r], a.hmin)));
+            else
+              tmax = fmax(tmax, (T)fabs((double)cv[r] - (double)nv[r]));
+          }
+          if (valid[r] && (unsigned)lz < (unsigned)nz) {
+            if (wr_x) xout[(long long)(t - (TX - 1)) * TY + ly0 + r] = nv[r];
+            if (wr_y && r == R - 1) yout[(long long)(lz + lx) * TX + lx] = nv[r];
+          }
+        }
+        __syncwarp();
+        // rows completed by lane lx = TX-1 at this step: write them back
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int lzw = t - (TX - 1) - ly0 - r;
+          if (valid[r] && (unsigned)lzw < (unsigned)nz) {
+            int s = swb - r;
+            if (s < 0) s += D;
+            const int gz = a.sz > 0 ? lzw + 1 : nz - lzw;
+            u[(long long)gz * a.plane + grow[r]] = ring[s * SLOT + o[r]];
+          }
+        }
+        // ring plane t-(TX-1)-ly0-(R-1) is no longer touched by this warp; a
+        // mailbox chunk is released after its last step
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) {
+          const int q = t - (TX - 1) - ly0 - (R - 1);
+          if (q >= 0 && q < NP) {
+            int s = swb - R;
+            if (s < 0) s += D;
+            mbar_arrive(empty + s);
+          }
+          if (tc == C - 1 && kb < NB) mbar_arrive(bempty + (kb & (HB - 1)));
+          st_release_cta_s(done + w, t + 1);
+        }
+        if (++s0 == D) s0 = 0;
+        if (++swb == D) swb = 0;
       }
     }
-    cp_async_wait_all();
     __syncthreads();
-    if (!ok) break;
+    if (s_abort) break;
   }
 
-  // CTA max-change reduction -> one atomic per CTA
-  T v = tmax;
+  // max-change reduction over the compute warps -> one atomic per CTA
+  if (warp < NW) {
+    T v = tmax;
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-  if ((tid & 31) == 0) s_red[tid >> 5] = v;
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (lane == 0) s_red[warp] = v;
+  }
   __syncthreads();
   if (tid == 0) {
     T m = s_red[0];
-    for (int w = 1; w < NT / 32; ++w) m = fmax(m, s_red[w]);
+    for (int w = 1; w < NW; ++w) m = fmax(m, s_red[w]);
     if (m > T(0)) {
       if (sizeof(T) == 4)
         atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint((float)m));
