@@ -42,7 +42,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="C4")
     p.add_argument("--mode", default="polish", choices=["polish", "fp32", "fp64", "fp64ref"])
-    p.add_argument("--scheduler", default="change", choices=["none", "change", "learned"])
+    p.add_argument("--scheduler", default="none", choices=["none", "change", "learned"])
     p.add_argument("--tol", type=float, default=1e-9, help="FP64 polish tolerance (max change)")
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--fixed-sweeps", type=int, default=0, help="profiling: run exactly this many sweeps")

@@ -26,6 +26,7 @@ SCHED_NONE, SCHED_CHANGE, SCHED_LEARNED = 0, 1, 2
 EXPORTS = [
     "pdfs_default_opts", "pdfs_solve", "pdfs_sweep", "pdfs_ctx_create", "pdfs_ctx_load", "pdfs_ctx_run",
     "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_status_string", "pdfs_version",
+    "run_fsm", "pdfs_vti_read", "pdfs_vti_write", "pdfs_phi_free", "pdfs_calc_dist_field",
 ]
 
 
@@ -53,6 +54,13 @@ class Stats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class Phi(C.Structure):
+    """Layout of the reference's Phi (single_gpu_cuda/src/phi3D.h:45-55)."""
+    _fields_ = [("x", C.c_int), ("y", C.c_int), ("z", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
+                ("dz", C.c_double), ("location", C.POINTER(C.c_int)), ("distance", C.POINTER(C.c_double)),
+                ("F", C.c_double)]
 
 
 _lib = None
@@ -88,5 +96,15 @@ def load(path: str = LIB_PATH):
     L.pdfs_status_string.restype = C.c_char_p
     L.pdfs_version.argtypes = []
     L.pdfs_version.restype = C.c_char_p
+    L.run_fsm.argtypes = [C.POINTER(Phi), ip]
+    L.run_fsm.restype = None
+    L.pdfs_vti_read.argtypes = [C.c_char_p, C.POINTER(Phi)]
+    L.pdfs_vti_read.restype = ip
+    L.pdfs_vti_write.argtypes = [C.c_char_p, C.POINTER(Phi)]
+    L.pdfs_vti_write.restype = ip
+    L.pdfs_phi_free.argtypes = [C.POINTER(Phi)]
+    L.pdfs_phi_free.restype = None
+    L.pdfs_calc_dist_field.argtypes = [C.POINTER(Phi), ip, C.POINTER(Opts), C.POINTER(Stats)]
+    L.pdfs_calc_dist_field.restype = ip
     _lib = L
     return L

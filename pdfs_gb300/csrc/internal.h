@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <algorithm>
 #include <cstdint>
 
 #include "../../include/pdfs.h"
@@ -50,6 +51,11 @@ TileShape tile64(int id);
 // (cap = upper bound field in the same layout).
 cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
                          const void *cap, int sms, cudaStream_t st, int *grid_used);
+
+// Change-based active set: blocks (or their face neighbours) that changed by
+// more than thr in either of the last two sweeps.  *count += active blocks.
+cudaError_t sched_change(const unsigned int *chg1, const unsigned int *chg2, float thr, uint8_t *active, int nbx,
+                         int nby, int nbz, int *count, int sms, cudaStream_t st);
 
 // Steps per mailbox chunk (matches WsGeo::C).
 constexpr int kMailboxChunk = 4;

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstddef>
 #include <cstring>
 #include <vector>
 
@@ -149,6 +150,8 @@ void ordering_signs(int sn, int *sx, int *sy, int *sz) {
 struct DevStatus {
   int err[4];
   unsigned long long chg;
+  int active_blocks;  // blocks the scheduler activated for this sweep
+  int pad;
 };
 
 }  // namespace pdfs
@@ -175,6 +178,11 @@ struct pdfs_ctx {
   size_t progress_ints = 0;
   DevStatus *dstat = nullptr;
   DevStatus *hstat = nullptr;  // pinned
+  // 8^3 block bookkeeping for the scheduler
+  int nbx = 0, nby = 0, nbz = 0;
+  long long nblocks = 0;
+  unsigned int *bchg = nullptr;  // [3][nblocks] float bits of per-block max change, rotating
+  uint8_t *bact = nullptr;       // [nblocks] active mask of the next sweep
   bool loaded = false, has_mask = false;
   int last_prec = -1;      // which working field holds the last result
   cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr;
@@ -320,6 +328,12 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((e = cudaMalloc(&c->ticket, 16)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->dstat, sizeof(DevStatus))) != cudaSuccess) return fail(e);
   if ((e = cudaHostAlloc(&c->hstat, sizeof(DevStatus), cudaHostAllocDefault)) != cudaSuccess) return fail(e);
+  c->nbx = (g->nx + 7) / 8;
+  c->nby = (g->ny + 7) / 8;
+  c->nbz = (g->nz + 7) / 8;
+  c->nblocks = (long long)c->nbx * c->nby * c->nbz;
+  if ((e = cudaMalloc(&c->bchg, (size_t)c->nblocks * 3 * 4)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->bact, (size_t)c->nblocks)) != cudaSuccess) return fail(e);
   {
     std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
                      w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
@@ -357,6 +371,8 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   cudaFree(c->mailbox);
   cudaFree(c->ticket);
   cudaFree(c->dstat);
+  cudaFree(c->bchg);
+  cudaFree(c->bact);
   if (c->hstat) cudaFreeHost(c->hstat);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
@@ -436,7 +452,7 @@ extern "C" int pdfs_ctx_load(pdfs_ctx *c, const double *field, const uint8_t *fr
 // One sweep of ordering sn on the FP32 (which = 0) or FP64 (1 min, 2 replace)
 // working field.  *chg receives the sweep's max change (relative for FP32,
 // absolute for FP64).  active: per-block visit mask or nullptr.
-static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, float *blk_chg, double *chg) {
+static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
   const Layout &L = f32 ? c->L32 : c->L64;
@@ -464,8 +480,11 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, floa
   a.ticket = c->ticket;
   a.err = c->dstat->err;
   a.maxchg = &c->dstat->chg;
-  (void)active;
-  (void)blk_chg;
+  a.blk_active = active;
+  a.blk_chg = blk_chg;
+  a.nbx = c->nbx;
+  a.nby = c->nby;
+  a.nbz = c->nbz;
   a.hmin = (float)std::min(g.dx, std::min(g.dy, g.dz));
   long long wait_ms = c->o.spin_limit > 0 ? c->o.spin_limit : 4000;
   if (getenv("PDFS_WAIT_MS")) wait_ms = atoll(getenv("PDFS_WAIT_MS"));
@@ -488,8 +507,9 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, floa
   const bool iso = g.dx == g.dy && g.dy == g.dz;
 
   CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
+  CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
+  if (blk_chg) CK(cudaMemsetAsync(blk_chg, 0, (size_t)c->nblocks * 4, c->st));
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
-  CK(cudaMemsetAsync(c->dstat, 0, sizeof(DevStatus), c->st));
   const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : ARITH_FAST;
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
@@ -555,9 +575,19 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   int rc = PDFS_OK;
   double chg = 0.0;
 
+  // One phase of sweeps (which: 0 FP32 min-update, 1 FP64 min-update, 2 FP64
+  // replace-update).  tol bounds the phase's change metric.  With a
+  // scheduler, the first round and every judging sweep visit all blocks;
+  // the phase ends only at a full sweep whose change is <= tol.
   auto phase = [&](int which, double tol, int *count, double *ms, double *kms) -> int {
     c->kern_ms = 0.0;
     CK(cudaEventRecord(c->e0, c->st));
+    const bool sched = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0;
+    const float thr = (float)tol;
+    unsigned int *bch[3] = {c->bchg, c->bchg + c->nblocks, c->bchg + 2 * c->nblocks};
+    int cur = 0;
+    if (sched) CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * 3 * 4, c->st));
+    bool need_full = true;
     int s = 0;
     for (;;) {
       if (o.fixed_sweeps > 0 && s >= o.fixed_sweeps) break;
@@ -566,12 +596,30 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         break;
       }
       const int sn = (first + s) % 8 + 1;
-      int r = run_sweep(c, which, sn, nullptr, nullptr, &chg);
+      const bool full = !sched || s < 8 || need_full;
+      const uint8_t *act = nullptr;
+      long long nact = c->nblocks;
+      if (!full) {
+        CK(cudaMemsetAsync(&c->dstat->active_blocks, 0, 4, c->st));
+        CK(sched_change(bch[(cur + 2) % 3], bch[(cur + 1) % 3], thr, c->bact, c->nbx, c->nby, c->nbz,
+                        &c->dstat->active_blocks, c->sms, c->st));
+        c->launches++;
+        act = c->bact;
+      }
+      int r = run_sweep(c, which, sn, act, sched ? bch[cur] : nullptr, &chg);
       if (r) return r;
+      if (!full) nact = c->hstat->active_blocks;
       ++s;
-      st.full_sweeps++;
-      st.voxel_updates += nodes;
-      if (o.fixed_sweeps == 0 && chg <= tol) break;
+      if (full) {
+        st.full_sweeps++;
+        st.voxel_updates += nodes;
+      } else {
+        st.voxel_updates += (long long)((double)nodes * (double)nact / (double)c->nblocks);
+        st.blocks_skipped += c->nblocks - nact;
+      }
+      if (o.fixed_sweeps == 0 && full && chg <= tol) break;
+      need_full = !full && chg <= tol;  // a quiet skipped sweep calls for a judging full sweep
+      cur = (cur + 1) % 3;              // bch[cur] becomes the previous sweep's changes
     }
     CK(cudaEventRecord(c->e1, c->st));
     CK(cudaEventSynchronize(c->e1));

@@ -73,6 +73,9 @@ struct SweepArgs {
   int *err;               // [0] error code, [1] abort flag, [2] column that timed out
   void *maxchg;           // FP32: uint bits of max relative change; FP64: u64 bits of max abs change
   float hmin;             // smallest spacing (relative-change floor)
+  const uint8_t *blk_active;  // per 8^3 block (x fastest): update its nodes?  nullptr = all
+  unsigned int *blk_chg;  // per 8^3 block: float bits of this sweep's max change (nullptr = off)
+  int nbx, nby, nbz;      // 8^3 block grid
   long long wait_cycles;  // bound on any single wait, in SM cycles
   int poison_col;         // test hook: this column never publishes (-1 = off)
   GodConst64 k64;
@@ -440,6 +443,20 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         o[r] = (gy[r] + 1) * W + lane + V;
         grow[r] = (long long)(y0 + gy[r]) * a.px + rowbase + V + lane;
       }
+      // 8^3 block bookkeeping: x and y block indices are fixed per lane/row,
+      // the z block changes every 8 planes
+      const bool track = a.blk_active != nullptr || a.blk_chg != nullptr;
+      const int bxl = (x0 - 1 + lane) >> 3;
+      int byr[R], bzr[R];
+      bool actb[R];
+      T accb[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        byr[r] = (y0 - 1 + gy[r]) >> 3;
+        bzr[r] = -1;
+        actb[r] = true;
+        accb[r] = T(0);
+      }
       const bool band_x = (lx == 0) && (upx >= 0);
       const bool band_y = (w == 0) && (upy >= 0);
       const bool wr_x = (lx == TX - 1) && has_dnx;
@@ -496,6 +513,20 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           if (sx_ < 0) sx_ += D;
           sr[r] = sx_;
           act[r] = valid[r] && (unsigned)lz < (unsigned)nz;
+          if (track && act[r]) {
+            const int gz = a.sz > 0 ? lz + 1 : nz - lz;
+            const int bz = (gz - 1) >> 3;
+            if (bz != bzr[r]) {  // entering a new z block: flush the old one, fetch the new flag
+              const long long base = ((long long)bz * a.nby + byr[r]) * a.nbx + bxl;
+              if (a.blk_chg && bzr[r] >= 0 && accb[r] > T(0))
+                atomicMax(a.blk_chg + ((long long)bzr[r] * a.nby + byr[r]) * a.nbx + bxl,
+                          __float_as_uint((float)accb[r]));
+              accb[r] = T(0);
+              bzr[r] = bz;
+              actb[r] = a.blk_active ? __ldg(a.blk_active + base) != 0 : true;
+            }
+            act[r] = actb[r];
+          }
           if (act[r] && masked) act[r] = !((fring[sx_ * G::MSL + gy[r]] >> lane) & 1u);
           cv[r] = T(0);
           m0[r] = m1[r] = m2[r] = capv[r] = T(0);
@@ -532,10 +563,13 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           const int lz = t - lx - ly0 - r;
           if (act[r] && nv[r] != cv[r]) {
             ring[sr[r] * SLOT + o[r]] = nv[r];
+            T d;
             if (sizeof(T) == 4)
-              tmax = fmax(tmax, (T)__fdividef(fabsf((float)cv[r] - (float)nv[r]), fmaxf((float)nv[r], a.hmin)));
+              d = (T)__fdividef(fabsf((float)cv[r] - (float)nv[r]), fmaxf((float)nv[r], a.hmin));
             else
-              tmax = fmax(tmax, (T)fabs((double)cv[r] - (double)nv[r]));
+              d = (T)fabs((double)cv[r] - (double)nv[r]);
+            tmax = fmax(tmax, d);
+            accb[r] = fmax(accb[r], d);
           }
           if (valid[r] && (unsigned)lz < (unsigned)nz) {
             if (wr_x) xout[(long long)(t - (TX - 1)) * TY + ly0 + r] = nv[r];
@@ -570,6 +604,12 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         }
         if (++s0 == D) s0 = 0;
         if (++swb == D) swb = 0;
+      }
+      if (a.blk_chg) {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (bzr[r] >= 0 && accb[r] > T(0))
+            atomicMax(a.blk_chg + ((long long)bzr[r] * a.nby + byr[r]) * a.nbx + bxl, __float_as_uint((float)accb[r]));
       }
     }
     __syncthreads();

@@ -13,10 +13,15 @@ Outputs (all small):
   solves.npz       -- converged solves of small sphere / multi-sphere grids
   c1_sphere64.json -- the 64^3 unit-sphere configuration solved to 1e-12 and to
                       an exact fixed point: sweep counts and SHA-256 of the field
+  vti/*.vti        -- input files in the reference reader's layout and the
+                      reference program's own output for them (its CLI,
+                      single_gpu_cuda/src/main.c, built for the CPU by
+                      `make -C oracle ref` with the reference's CPU sweep)
 """
 from __future__ import annotations
 
 import hashlib
+import subprocess
 import json
 import math
 import os
@@ -28,6 +33,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from oracle import oracle as O  # noqa: E402
+from pdfs_gb300 import vti as VT  # noqa: E402
 from pdfs_gb300 import workloads as W  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
@@ -148,6 +154,20 @@ def main():
     meta["one_round"] = {"sha256": sha(a)}
     with open(os.path.join(OUT, "c1_sphere64.json"), "w") as fh:
         json.dump(meta, fh, indent=1)
+
+    vdir = os.path.join(OUT, "vti")
+    os.makedirs(vdir, exist_ok=True)
+    cases = {
+        "sphere": (18, 16, 14, (1.0, 1.0, 1.0), (8.5, 7.0, 6.5), 4.2),
+        "aniso": (15, 13, 20, (0.5, 0.7, 0.4), (3.6, 4.1, 3.9), 2.3),
+    }
+    for name, (nx, ny, nz, sp, c, r) in cases.items():
+        loc, dist = VT.sphere_input(nx, ny, nz, sp, c, r)
+        inp = os.path.join(vdir, f"{name}_in.vti")
+        VT.write_input(inp, loc, dist, sp)
+        prefix = os.path.join(vdir, f"{name}_ref")
+        subprocess.run([os.path.join(ROOT, "oracle", "_ref", "PDFS_ref"), inp, prefix], check=True,
+                       stdout=subprocess.DEVNULL)
     print("golden fixtures written to", OUT)
 
 

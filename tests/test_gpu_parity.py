@@ -241,3 +241,31 @@ def test_not_converged_status():
     with pytest.raises(api.PdfsError) as ei:
         api.solve(a, (1.0, 1.0, 1.0), tol=0.0, max_sweeps=2)
     assert ei.value.status == L.PDFS_ERR_NOT_CONVERGED
+
+
+@pytest.mark.parametrize("freeze", [L.FREEZE_MASK, L.FREEZE_NONE])
+def test_change_scheduler_reaches_plain_fixed_point(freeze):
+    """Skipping blocks never moves the answer: the solve ends on a full sweep
+    that changes nothing, i.e. at the plain FSM's fixed point (to rounding)."""
+    w = W.random_spheres(160, 128, 96, 1.0, 1.0, 1.0, 18, 3.0, 16.0, seed=41)
+    sp = (w.dx, w.dy, w.dz)
+    fr = w.frozen if freeze == L.FREEZE_MASK else None
+    a, b = w.field.copy(), w.field.copy()
+    O.solve(b, sp, tol=0.0, frozen=fr, threads=8)
+    st = api.solve(a, sp, frozen=fr, freeze=freeze, scheduler=L.SCHED_CHANGE, arith=L.ARITH_FAST, tol=0.0)
+    assert st["blocks_skipped"] > 0
+    assert st["full_sweeps"] < st["sweeps_fp64"]
+    # tolerance: different visiting orders reach the FP64 fixed point to rounding
+    assert rel_err(a, b, 1.0) <= 1e-13
+
+
+def test_change_scheduler_fp32_polish():
+    w = W.random_spheres(160, 144, 128, 1.0, 1.0, 1.0, 24, 3.0, 16.0, seed=42)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
+                   scheduler=L.SCHED_CHANGE, arith=L.ARITH_FAST, tol=1e-12)
+    assert st["blocks_skipped"] > 0
+    # tolerance: polish to a 1e-12 max change; error vs the plain FP64 fixed point 1e-10 relative
+    assert rel_err(a, b, 1.0) <= 1e-10
