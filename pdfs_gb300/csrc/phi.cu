@@ -127,4 +127,5 @@ extern "C" void run_fsm(pdfs_phi *pf, int iterations) {
   }
   const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   printf("Parallel FSM time: %f s.\n", sec);  // the reference's report line (phi3D_fsm.cu:104)
+  fflush(stdout);
 }
