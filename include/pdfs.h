@@ -137,6 +137,20 @@ int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats);
 int pdfs_ctx_store(pdfs_ctx *c, double *field);
 void pdfs_ctx_destroy(pdfs_ctx *c);
 
+/* Solves n independent grids together (the batched configuration): each
+ * sweep is one persistent launch over the columns of every grid still
+ * sweeping, each round of 8 orderings replays from a CUDA graph, and a grid
+ * leaves the launch once one of its sweeps changes by <= the phase tolerance.
+ * fields[i] / frozen[i] as in pdfs_solve (frozen may be NULL, or hold NULL
+ * entries).  stats: NULL or n entries.  opts.fixed_sweeps must be 0 and the
+ * scheduler is not used.  Returns the first failing grid's status. */
+int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fields, const uint8_t *const *frozen,
+                     const pdfs_opts *o, pdfs_stats *stats);
+
+/* Times the sweep tile variants on grid g (two sweeps each, synthetic field)
+ * and returns the fastest pair as an opts.tile value (FP32 id | FP64 id << 8). */
+int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o, int *tile);
+
 /* Human-readable text of a status code (static storage). */
 const char *pdfs_status_string(int status);
 /* Library version string. */

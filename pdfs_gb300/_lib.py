@@ -27,6 +27,7 @@ EXPORTS = [
     "pdfs_default_opts", "pdfs_solve", "pdfs_sweep", "pdfs_ctx_create", "pdfs_ctx_load", "pdfs_ctx_run",
     "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_status_string", "pdfs_version",
     "run_fsm", "pdfs_vti_read", "pdfs_vti_write", "pdfs_phi_free", "pdfs_calc_dist_field",
+    "pdfs_solve_batch", "pdfs_autotune",
 ]
 
 
@@ -106,5 +107,10 @@ def load(path: str = LIB_PATH):
     L.pdfs_phi_free.restype = None
     L.pdfs_calc_dist_field.argtypes = [C.POINTER(Phi), ip, C.POINTER(Opts), C.POINTER(Stats)]
     L.pdfs_calc_dist_field.restype = ip
+    L.pdfs_solve_batch.argtypes = [ip, C.POINTER(Grid), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                   C.POINTER(Opts), C.POINTER(Stats)]
+    L.pdfs_solve_batch.restype = ip
+    L.pdfs_autotune.argtypes = [C.POINTER(Grid), C.POINTER(Opts), C.POINTER(ip)]
+    L.pdfs_autotune.restype = ip
     _lib = L
     return L

@@ -86,6 +86,38 @@ def run_fsm(field: np.ndarray, spacing, rounds: int = 1, **kw) -> dict:
     return solve(field, spacing, fixed_sweeps=8 * int(rounds), **kw)
 
 
+def solve_batch(fields, spacings, frozen=None, **kw):
+    """Solves many grids in one batched solve (pdfs_solve_batch), in place.
+    Returns the per-grid stats dicts."""
+    n = len(fields)
+    grids = (L.Grid * n)()
+    fptr = (C.c_void_p * n)()
+    mptr = (C.c_void_p * n)()
+    for i, f in enumerate(fields):
+        _check_field(f)
+        g = _grid(f, spacings[i])
+        grids[i] = g
+        fptr[i] = f.ctypes.data
+        mptr[i] = frozen[i].ctypes.data if frozen is not None and frozen[i] is not None else None
+    o = make_opts(**kw)
+    st = (L.Stats * n)()
+    s = L.load().pdfs_solve_batch(n, grids, fptr, mptr if frozen is not None else None, C.byref(o), st)
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_solve_batch")
+    return [x.as_dict() for x in st]
+
+
+def autotune(nx, ny, nz, spacing, **kw) -> int:
+    """Fastest tile pair for this grid shape (an opts.tile value)."""
+    g = L.Grid(nx, ny, nz, *map(float, spacing))
+    o = make_opts(**kw)
+    t = C.c_int(0)
+    s = L.load().pdfs_autotune(C.byref(g), C.byref(o), C.byref(t))
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_autotune")
+    return t.value
+
+
 class Context:
     """Device-resident solve context (pdfs_ctx_*)."""
 

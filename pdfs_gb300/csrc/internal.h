@@ -4,6 +4,7 @@
 
 #include <cstddef>
 #include <algorithm>
+#include <vector>
 #include <cstdint>
 
 #include "../../include/pdfs.h"
@@ -57,8 +58,66 @@ cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepAr
 cudaError_t sched_change(const unsigned int *chg1, const unsigned int *chg2, float thr, uint8_t *active, int nbx,
                          int nby, int nbz, int *count, int sms, cudaStream_t st);
 
+// Status words a sweep writes on the device (read back after each sweep).
+struct DevStatus {
+  int err[4];
+  unsigned long long chg;
+  int active_blocks;  // blocks the scheduler activated for this sweep
+  int pad;
+};
+
+
 // Steps per mailbox chunk (matches WsGeo::C).
 constexpr int kMailboxChunk = 4;
 inline int mailbox_chunks(int nz) { return (nz + 32 + kMailboxChunk - 1) / kMailboxChunk; }
 
+}  // namespace pdfs
+
+// The context behind the opaque pdfs_ctx handle of the C ABI.
+struct pdfs_ctx {
+  pdfs_grid g{};
+  pdfs_opts o{};
+  int dev = 0, sms = 0;
+  cudaStream_t st = nullptr;
+  int t32 = 1, t64 = 1;
+  pdfs::Layout L32, L64;
+  pdfs::MaskLayout M;
+  double *in64 = nullptr;   // exact input, internal FP64 layout (also the polish cap)
+  double *u64 = nullptr;    // FP64 working field
+  float *u32 = nullptr;     // FP32 working field
+  uint32_t *fmask = nullptr;
+  void *stage = nullptr;    // reference-layout staging buffer for host transfers
+  size_t stage_bytes = 0;
+  int *order32 = nullptr, *order64 = nullptr, *progress = nullptr, *ticket = nullptr;
+  void *mailbox = nullptr;  // x- and y-face mailboxes of every column
+  size_t mailbox_bytes = 0;
+  size_t progress_ints = 0;
+  pdfs::DevStatus *dstat = nullptr;
+  pdfs::DevStatus *hstat = nullptr;  // pinned
+  // 8^3 block bookkeeping for the scheduler
+  int nbx = 0, nby = 0, nbz = 0;
+  long long nblocks = 0;
+  unsigned int *bchg = nullptr;  // [3][nblocks] float bits of per-block max change, rotating
+  uint8_t *bact = nullptr;       // [nblocks] active mask of the next sweep
+  bool loaded = false, has_mask = false;
+  int last_prec = -1;      // which working field holds the last result
+  cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr;
+  double kern_ms = 0.0;  // accumulated sweep-kernel time since the last reset
+  int launches = 0;      // kernels launched since the last reset
+};
+
+namespace pdfs {
+void fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg,
+                     SweepArgs *out);
+void ordering_signs(int sn, int *sx, int *sy, int *sz);
+std::vector<int> wavefront_order(int ncx, int ncy, int tx, int ty);
+// FP64 input -> FP32 working field / FP32 result -> FP64 polish start
+int ctx_narrow(pdfs_ctx *c);
+int ctx_widen(pdfs_ctx *c);
+// Tensor maps of one grid for a sweep kernel variant: field, cap, mask.
+cudaError_t encode_sweep_maps(int which, int tile, const SweepArgs &a, const Layout &L, const void *cap,
+                              CUtensorMap maps[3]);
+// One batched sweep over the grids that a0.batch describes (ntick tickets).
+cudaError_t launch_sweep_batch(int which, int tile, int arith, bool iso, const SweepArgs &a0, int ntick, int sms,
+                               cudaStream_t st, int *grid_used);
 }  // namespace pdfs

@@ -126,7 +126,7 @@ __global__ void k_pack_mask(const uint8_t *__restrict__ m, uint32_t *__restrict_
 // about TY, plus a few steps of hand-off latency.  Any order with positive
 // weights lists both upwind neighbours first, which is all the deadlock
 // argument needs.
-static std::vector<int> wavefront_order(int ncx, int ncy, int tx, int ty) {
+std::vector<int> wavefront_order(int ncx, int ncy, int tx, int ty) {
   std::vector<int> o((size_t)ncx * ncy);
   for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
   const long long wx = tx + 12, wy = ty + 12;
@@ -147,48 +147,9 @@ void ordering_signs(int sn, int *sx, int *sy, int *sz) {
   *sz = ((sn == 3 || sn == 7) ? -1 : 1) * desc;
 }
 
-struct DevStatus {
-  int err[4];
-  unsigned long long chg;
-  int active_blocks;  // blocks the scheduler activated for this sweep
-  int pad;
-};
-
 }  // namespace pdfs
 
 using namespace pdfs;
-
-struct pdfs_ctx {
-  pdfs_grid g{};
-  pdfs_opts o{};
-  int dev = 0, sms = 0;
-  cudaStream_t st = nullptr;
-  int t32 = 1, t64 = 1;
-  Layout L32, L64;
-  MaskLayout M;
-  double *in64 = nullptr;   // exact input, internal FP64 layout (also the polish cap)
-  double *u64 = nullptr;    // FP64 working field
-  float *u32 = nullptr;     // FP32 working field
-  uint32_t *fmask = nullptr;
-  void *stage = nullptr;    // reference-layout staging buffer for host transfers
-  size_t stage_bytes = 0;
-  int *order32 = nullptr, *order64 = nullptr, *progress = nullptr, *ticket = nullptr;
-  void *mailbox = nullptr;  // x- and y-face mailboxes of every column
-  size_t mailbox_bytes = 0;
-  size_t progress_ints = 0;
-  DevStatus *dstat = nullptr;
-  DevStatus *hstat = nullptr;  // pinned
-  // 8^3 block bookkeeping for the scheduler
-  int nbx = 0, nby = 0, nbz = 0;
-  long long nblocks = 0;
-  unsigned int *bchg = nullptr;  // [3][nblocks] float bits of per-block max change, rotating
-  uint8_t *bact = nullptr;       // [nblocks] active mask of the next sweep
-  bool loaded = false, has_mask = false;
-  int last_prec = -1;      // which working field holds the last result
-  cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr;
-  double kern_ms = 0.0;  // accumulated sweep-kernel time since the last reset
-  int launches = 0;      // kernels launched since the last reset
-};
 
 static int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return PDFS_OK;
@@ -452,11 +413,13 @@ extern "C" int pdfs_ctx_load(pdfs_ctx *c, const double *field, const uint8_t *fr
 // One sweep of ordering sn on the FP32 (which = 0) or FP64 (1 min, 2 replace)
 // working field.  *chg receives the sweep's max change (relative for FP32,
 // absolute for FP64).  active: per-block visit mask or nullptr.
-static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
+// The sweep arguments of context c: which 0 = FP32, 1 = FP64 min, 2 = FP64 replace.
+void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg,
+                           SweepArgs *out) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
   const Layout &L = f32 ? c->L32 : c->L64;
-  SweepArgs a;
+  SweepArgs &a = *out;
   std::memset(&a, 0, sizeof(a));
   a.u = f32 ? (void *)c->u32 : (void *)c->u64;
   a.fmask = c->has_mask ? c->fmask : nullptr;
@@ -504,6 +467,14 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   a.k32.iso_h = (float)g.dx;
   a.k32.iso_2h2 = (float)(2.0 * g.dx * g.dx);
   a.k32.iso_h2 = (float)(g.dx * g.dx);
+}
+
+static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
+  const pdfs_grid &g = c->g;
+  const bool f32 = which == 0;
+  const Layout &L = f32 ? c->L32 : c->L64;
+  SweepArgs a;
+  fill_sweep_args(c, which, sn, active, blk_chg, &a);
   const bool iso = g.dx == g.dy && g.dy == g.dz;
 
   CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
@@ -540,7 +511,7 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   return PDFS_OK;
 }
 
-static int widen(pdfs_ctx *c) {
+int pdfs::ctx_widen(pdfs_ctx *c) {
   const pdfs_grid &g = c->g;
   dim3 grid(g.ny + 2, g.nz + 2);
   k_widen<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64, c->has_mask ? c->fmask : nullptr, c->M,
@@ -550,7 +521,7 @@ static int widen(pdfs_ctx *c) {
   return PDFS_OK;
 }
 
-static int narrow(pdfs_ctx *c) {  // FP64 input -> FP32 working field
+int pdfs::ctx_narrow(pdfs_ctx *c) {  // FP64 input -> FP32 working field
   const pdfs_grid &g = c->g;
   dim3 grid(g.ny + 2, g.nz + 2);
   k_convert<double, float><<<grid, 128, 0, c->st>>>(c->in64, c->L64, c->u32, c->L32, g.nx);
@@ -636,12 +607,12 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     r = phase(1, o.tol, &st.sweeps_fp64, &st.ms_fp64, &st.ms_kern_fp64);
     c->last_prec = 1;
   } else {
-    if ((r = narrow(c))) return r;
+    if ((r = ctx_narrow(c))) return r;
     const double tol32 = 4.0e-6;  // relative; FP32 rounding creep stays ~1e-7
     r = phase(0, tol32, &st.sweeps_fp32, &st.ms_fp32, &st.ms_kern_fp32);
     c->last_prec = 0;
     if (!r && o.precision == PDFS_PREC_FP32_POLISH64 && o.fixed_sweeps == 0) {
-      if ((r = widen(c))) return r;
+      if ((r = ctx_widen(c))) return r;
       r = phase(2, o.tol, &st.sweeps_fp64, &st.ms_fp64, &st.ms_kern_fp64);
       c->last_prec = 1;
     }

@@ -1,6 +1,8 @@
 // sweep.cu -- instantiations and launcher of the warp-specialised sweep kernels.
 #include <cudaTypedefs.h>
 
+#include <cstring>
+
 
 #include "internal.h"
 
@@ -57,25 +59,41 @@ static cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty) {
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-template <class T, int TY, int R, int MODE, int ARITH, bool ISO>
-static cudaError_t launch_one(const SweepArgs &a, const Layout &L, const void *cap, int sms, cudaStream_t st,
-                              int *grid_used) {
+// The three tensor maps a variant reads: field slots, cap slots, mask words.
+template <class T, int TY, int R, int MODE>
+static cudaError_t encode_maps(const SweepArgs &a, const Layout &L, const void *cap, CUtensorMap m[3]) {
   using G = WsGeo<T, TY, R, MODE>;
-  auto kern = ws_sweep_kernel<T, TY, R, MODE, ARITH, ISO>;
-  CUtensorMap tm_u, tm_cap, tm_mask;
-  cudaError_t e = encode_field_map(&tm_u, a.u, sizeof(T), L, a.nz + 2, G::W, G::R);
+  cudaError_t e = encode_field_map(&m[0], a.u, sizeof(T), L, a.nz + 2, G::W, G::R);
   if (e != cudaSuccess) return e;
   if (G::CAP) {
-    e = encode_field_map(&tm_cap, const_cast<void *>(cap), sizeof(T), L, a.nz + 2, G::TX, TY);
+    e = encode_field_map(&m[1], const_cast<void *>(cap), sizeof(T), L, a.nz + 2, G::TX, TY);
     if (e != cudaSuccess) return e;
   } else {
-    tm_cap = tm_u;
+    m[1] = m[0];
   }
   if (a.fmask) {
-    e = encode_mask_map(&tm_mask, a, TY);
+    e = encode_mask_map(&m[2], a, TY);
     if (e != cudaSuccess) return e;
   } else {
-    tm_mask = tm_u;
+    m[2] = m[0];
+  }
+  return cudaSuccess;
+}
+
+// Single grid (a.batch == nullptr): maps from a and L.  Batched: the maps
+// live with each grid's description in device memory, ntick tickets.
+template <class T, int TY, int R, int MODE, int ARITH, bool ISO>
+static cudaError_t launch_one(const SweepArgs &a, const Layout *L, const void *cap, int ntick, int sms,
+                              cudaStream_t st, int *grid_used) {
+  using G = WsGeo<T, TY, R, MODE>;
+  auto kern = ws_sweep_kernel<T, TY, R, MODE, ARITH, ISO>;
+  CUtensorMap m[3];
+  cudaError_t e = cudaSuccess;
+  if (a.batch == nullptr) {
+    e = encode_maps<T, TY, R, MODE>(a, *L, cap, m);
+    if (e != cudaSuccess) return e;
+  } else {
+    std::memset(m, 0, sizeof(m));
   }
   const size_t smem = G::BYTES;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -84,25 +102,25 @@ static cudaError_t launch_one(const SweepArgs &a, const Layout &L, const void *c
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, G::NT, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  const int ncol = a.ncx * a.ncy;
   int grid = per_sm * sms;
-  if (grid > ncol) grid = ncol;
-  kern<<<grid, G::NT, smem, st>>>(tm_u, tm_cap, tm_mask, a);
+  if (grid > ntick) grid = ntick;
+  if (grid < 1) grid = 1;
+  kern<<<grid, G::NT, smem, st>>>(m[0], m[1], m[2], a);
   if (grid_used) *grid_used = grid;
   return cudaGetLastError();
 }
 
-#define PDFS_T32(ID, TY, R)                                                                      \
-  case ID:                                                                                       \
-    return iso ? launch_one<float, TY, R, MODE_MIN, ARITH_FAST, true>(a, L, cap, sms, st, g)     \
-               : launch_one<float, TY, R, MODE_MIN, ARITH_FAST, false>(a, L, cap, sms, st, g);
-#define PDFS_T64(ID, TY, R, MODE)                                                                         \
-  case ID:                                                                                                \
-    return arith == ARITH_REF ? launch_one<double, TY, R, MODE, ARITH_REF, false>(a, L, cap, sms, st, g) \
-                              : launch_one<double, TY, R, MODE, ARITH_FAST, false>(a, L, cap, sms, st, g);
+#define PDFS_T32(ID, TY, R)                                                                           \
+  case ID:                                                                                            \
+    return iso ? launch_one<float, TY, R, MODE_MIN, ARITH_FAST, true>(a, L, cap, ntick, sms, st, g)   \
+               : launch_one<float, TY, R, MODE_MIN, ARITH_FAST, false>(a, L, cap, ntick, sms, st, g);
+#define PDFS_T64(ID, TY, R, MODE)                                                                            \
+  case ID:                                                                                                   \
+    return arith == ARITH_REF ? launch_one<double, TY, R, MODE, ARITH_REF, false>(a, L, cap, ntick, sms, st, g) \
+                              : launch_one<double, TY, R, MODE, ARITH_FAST, false>(a, L, cap, ntick, sms, st, g);
 
-cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
-                         const void *cap, int sms, cudaStream_t st, int *g) {
+static cudaError_t dispatch(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout *L,
+                            const void *cap, int ntick, int sms, cudaStream_t st, int *g) {
   if (which == 0) {
     switch (tile) {
       PDFS_T32(1, 8, 2)
@@ -132,5 +150,55 @@ cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepAr
 }
 #undef PDFS_T32
 #undef PDFS_T64
+
+cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
+                         const void *cap, int sms, cudaStream_t st, int *g) {
+  return dispatch(which, tile, arith, iso, a, &L, cap, a.ncx * a.ncy, sms, st, g);
+}
+
+cudaError_t launch_sweep_batch(int which, int tile, int arith, bool iso, const SweepArgs &a0, int ntick, int sms,
+                               cudaStream_t st, int *g) {
+  if (!a0.batch || ntick < 1) return cudaErrorInvalidValue;
+  return dispatch(which, tile, arith, iso, a0, nullptr, nullptr, ntick, sms, st, g);
+}
+
+#define PDFS_M32(ID, TY, R) \
+  case ID:                  \
+    return encode_maps<float, TY, R, MODE_MIN>(a, L, cap, m);
+#define PDFS_M64(ID, TY, R, MODE) \
+  case ID:                        \
+    return encode_maps<double, TY, R, MODE>(a, L, cap, m);
+
+cudaError_t encode_sweep_maps(int which, int tile, const SweepArgs &a, const Layout &L, const void *cap,
+                              CUtensorMap m[3]) {
+  if (which == 0) {
+    switch (tile) {
+      PDFS_M32(1, 8, 2)
+      PDFS_M32(2, 8, 4)
+      PDFS_M32(3, 16, 4)
+      PDFS_M32(4, 8, 1)
+      PDFS_M32(5, 4, 2)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else if (which == 1) {
+    switch (tile) {
+      PDFS_M64(1, 4, 1, MODE_MIN)
+      PDFS_M64(2, 4, 2, MODE_MIN)
+      PDFS_M64(3, 8, 2, MODE_MIN)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (tile) {
+      PDFS_M64(1, 4, 1, MODE_REPLACE)
+      PDFS_M64(2, 4, 2, MODE_REPLACE)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  }
+}
+#undef PDFS_M32
+#undef PDFS_M64
 
 }  // namespace pdfs

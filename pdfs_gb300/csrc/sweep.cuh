@@ -80,6 +80,16 @@ struct SweepArgs {
   int poison_col;         // test hook: this column never publishes (-1 = off)
   GodConst64 k64;
   GodConst32 k32;
+  const struct BatchDesc *batch;  // many grids in one launch (nullptr = this grid only)
+};
+
+// A batched sweep: tickets enumerate (grid, local column) pairs, each grid's
+// columns in wavefront order; args[g] / maps[3g..3g+2] describe grid g.
+struct BatchDesc {
+  int nticket;
+  const int2 *tickets;      // (grid, local column id)
+  const SweepArgs *args;    // per grid (sx/sy/sz are taken from the launch)
+  const CUtensorMap *maps;  // per grid: field, cap, mask
 };
 
 // Shared-memory plan of one kernel variant: columns of 32 x TY nodes, R rows
@@ -235,7 +245,7 @@ template <class T, int TY, int R, int MODE, int ARITH, bool ISO>
 __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                                      const __grid_constant__ CUtensorMap tm_cap,
                                                                      const __grid_constant__ CUtensorMap tm_mask,
-                                                                     const SweepArgs a) {
+                                                                     const __grid_constant__ SweepArgs a0) {
   using G = WsGeo<T, TY, R, MODE>;
   constexpr int TX = G::TX, V = G::V, W = G::W, D = G::D, SLOT = G::SLOT, C = G::C, HB = G::HB, NW = G::NW;
   static_assert((C & (C - 1)) == 0 && (HB & (HB - 1)) == 0, "power-of-two chunk sizes");
@@ -250,34 +260,42 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
   uint64_t *bfull = empty + D;
   uint64_t *bempty = bfull + HB;
   int *done = reinterpret_cast<int *>(sm + G::OFF_DONE);  // per compute warp: steps completed
-  __shared__ int s_ticket;
+  __shared__ int s_ticket, s_grid, s_lc;
   __shared__ volatile int s_abort;
-  __shared__ T s_red[NW];
+  __shared__ SweepArgs s_a;  // the current column's grid
+  __shared__ const CUtensorMap *s_maps;
 
   // TMA needs 128-byte aligned shared-memory destinations: refuse to start otherwise
   if ((saddr(sm) & 127u) != 0) {
     if (threadIdx.x == 0) {
-      atomicCAS(a.err, 0, DEV_ERR_SMEM_ALIGN);
-      atomicExch(a.err + 1, 1);
+      atomicCAS(a0.err, 0, DEV_ERR_SMEM_ALIGN);
+      atomicExch(a0.err + 1, 1);
     }
     return;
   }
 
-  T *__restrict__ u = reinterpret_cast<T *>(a.u);
-  T *__restrict__ xbox = reinterpret_cast<T *>(a.xbox);
-  T *__restrict__ ybox = reinterpret_cast<T *>(a.ybox);
+  const SweepArgs &a = s_a;
+  const BatchDesc *batch = a0.batch;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int ncol = a.ncx * a.ncy;
-  const int nz = a.nz, NP = nz + 2, NB = a.nbands;
-  const int tsteps = max(nz + TX + TY + 1, NB * C);  // steps every compute warp runs per column
-  const bool masked = a.fmask != nullptr;
-  T tmax = T(0);
+  const int ntick = batch ? batch->nticket : a0.ncx * a0.ncy;
+  int cur_grid = -1;
 
   if (tid == 0) s_abort = 0;
   for (int ncols_done = 0;; ++ncols_done) {
     if (tid == 0) {
-      s_ticket = atomicAdd(a.ticket, 1);
-      if (*(volatile int *)(a.err + 1)) s_abort = 1;
+      const int tk = atomicAdd(a0.ticket, 1);
+      s_ticket = tk;
+      if (tk < ntick) {
+        if (batch) {
+          const int2 e = batch->tickets[tk];
+          s_grid = e.x;
+          s_lc = e.y;
+        } else {
+          s_grid = 0;
+          s_lc = a0.order[tk];
+        }
+      }
+      if (*(volatile int *)(a0.err + 1)) s_abort = 1;
       for (int i = 0; i < D; ++i) {
         if (ncols_done) {
           mbar_inval(full + i);
@@ -298,9 +316,36 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
     }
     if (tid < NW) done[tid] = 0;
     __syncthreads();
-    const int tk = s_ticket;
-    if (tk >= ncol || s_abort) break;
-    const int lc = a.order[tk];
+    if (s_ticket >= ntick || s_abort) break;
+    if (s_grid != cur_grid) {  // stage the column's grid description in shared memory
+      cur_grid = s_grid;
+      const SweepArgs *src = batch ? batch->args + cur_grid : &a0;
+      const int *ws = reinterpret_cast<const int *>(src);
+      int *wd = reinterpret_cast<int *>(&s_a);
+      for (int i = tid; i < (int)(sizeof(SweepArgs) / 4); i += blockDim.x) wd[i] = ws[i];
+      __syncthreads();
+      if (tid == 0) {
+        s_a.sx = a0.sx;
+        s_a.sy = a0.sy;
+        s_a.sz = a0.sz;
+        s_a.err = a0.err;
+        s_a.ticket = a0.ticket;
+        if (batch) s_a.maxchg = reinterpret_cast<unsigned long long *>(a0.maxchg) + cur_grid;
+        s_maps = batch ? batch->maps + 3 * cur_grid : nullptr;
+      }
+      __syncthreads();
+    }
+    const CUtensorMap *mp_u = batch ? s_maps : &tm_u;
+    const CUtensorMap *mp_cap = batch ? s_maps + 1 : &tm_cap;
+    const CUtensorMap *mp_mask = batch ? s_maps + 2 : &tm_mask;
+    T *__restrict__ u = reinterpret_cast<T *>(a.u);
+    T *__restrict__ xbox = reinterpret_cast<T *>(a.xbox);
+    T *__restrict__ ybox = reinterpret_cast<T *>(a.ybox);
+    const int nz = a.nz, NP = nz + 2, NB = a.nbands;
+    const int tsteps = max(nz + TX + TY + 1, NB * C);  // steps every compute warp runs per column
+    const bool masked = a.fmask != nullptr;
+    T tmax = T(0);
+    const int lc = s_lc;
     const int lcx = lc % a.ncx, lcy = lc / a.ncx;
     const int cx = a.sx > 0 ? lcx : a.ncx - 1 - lcx;
     const int cy = a.sy > 0 ? lcy : a.ncy - 1 - lcy;
@@ -321,9 +366,9 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           if (use == 0 || mbar_test(empty + s, (use - 1) & 1)) {
             const int gz = a.sz > 0 ? pl : nz + 1 - pl;
             mbar_arrive_tx(full + s, G::TX_BYTES + (masked ? G::MASK_BYTES : 0u));
-            tma_load_3d(ring + (size_t)s * SLOT, &tm_u, (int)rowbase, y0 - 1, gz, full + s);
-            if (G::CAP) tma_load_3d(capr + (size_t)s * TX * TY, &tm_cap, (int)rowbase + V, y0, gz, full + s);
-            if (masked) tma_load_3d(fring + s * G::MSL, &tm_mask, y0 - 1, cx, gz, full + s);
+            tma_load_3d(ring + (size_t)s * SLOT, mp_u, (int)rowbase, y0 - 1, gz, full + s);
+            if (G::CAP) tma_load_3d(capr + (size_t)s * TX * TY, mp_cap, (int)rowbase + V, y0, gz, full + s);
+            if (masked) tma_load_3d(fring + s * G::MSL, mp_mask, y0 - 1, cx, gz, full + s);
             ++pl;
             t_last = cycles();
           } else {
@@ -612,28 +657,21 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             atomicMax(a.blk_chg + ((long long)bzr[r] * a.nby + byr[r]) * a.nbx + bxl, __float_as_uint((float)accb[r]));
       }
     }
+    // the column's max change -> its grid's counter (one atomic per compute warp)
+    if (warp < NW) {
+      T v = tmax;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+      if (lane == 0 && v > T(0)) {
+        if (sizeof(T) == 4)
+          atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint((float)v));
+        else
+          atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg),
+                    (unsigned long long)__double_as_longlong((double)v));
+      }
+    }
     __syncthreads();
     if (s_abort) break;
-  }
-
-  // max-change reduction over the compute warps -> one atomic per CTA
-  if (warp < NW) {
-    T v = tmax;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-    if (lane == 0) s_red[warp] = v;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    T m = s_red[0];
-    for (int w = 1; w < NW; ++w) m = fmax(m, s_red[w]);
-    if (m > T(0)) {
-      if (sizeof(T) == 4)
-        atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint((float)m));
-      else
-        atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg),
-                  (unsigned long long)__double_as_longlong((double)m));
-    }
   }
 }
 
