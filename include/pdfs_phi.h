@@ -5,7 +5,7 @@
  *
  * pdfs_phi has the memory layout of the reference's Phi
  * (single_gpu_cuda/src/phi3D.h:45-55), so the reference's own phi3D.c /
- * main.c can link against run_fsm() below unchanged (see INTEGRATION.md).
+ * main.c can link against run_fsm() below unchanged.
  */
 #ifndef PDFS_PHI_H
 #define PDFS_PHI_H
