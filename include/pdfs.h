@@ -29,6 +29,7 @@ extern "C" {
 #define PDFS_ERR_NOT_CONVERGED (-5) /* max_sweeps reached before the tolerance      */
 #define PDFS_ERR_IO (-6)            /* file could not be read or written            */
 #define PDFS_ERR_NO_DEVICE (-7)     /* no CUDA device (the library never falls back) */
+#define PDFS_ERR_TOO_LARGE (-8)     /* grid exceeds the fixed scratch of pdfs_sweep_static */
 
 /* ---- problem description ----------------------------------------------------- */
 typedef struct {
@@ -150,6 +151,45 @@ int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fields, const
 /* Times the sweep tile variants on grid g (two sweeps each, synthetic field)
  * and returns the fastest pair as an opts.tile value (FP32 id | FP64 id << 8). */
 int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o, int *tile);
+
+/* ---- allocation-free sweep ----------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run: code that executes inside a pre-sized memory pool
+ * or arena handed to it by a host application, real-time or embedded loops
+ * that must not call the allocator after start-up (cudaMalloc can block and
+ * synchronise the device), and plugins whose host process forbids device
+ * allocation after its own set-up.  pdfs_sweep_static() runs one ordering
+ * of the plain FSM (FP64, the reference's arithmetic, every node
+ * min-updated: the same result as pdfs_sweep) without calling cudaMalloc,
+ * cudaFree or any allocating routine.  Its scratch -- column progress words,
+ * the column ticket, the status words and the face mailboxes -- lives in one
+ * fixed device array of PDFS_STATIC_SCRATCH_BYTES that every GPU which loads
+ * the library keeps until the process exits.  The caller passes the field.
+ *
+ * Field: a device array in the sweep's internal layout.  Node (x, y, z) of
+ * the halo-padded grid (0 <= x <= nx+1, ...) is element
+ * z*ry*px + y*px + x + 1; pdfs_static_layout() gives px, ry and the element
+ * count; entries outside the halo-padded grid are not read for any result
+ * (fill them with +inf).
+ *
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  Every call shares the one array and leaves its contents behind:
+ * each call clears the words that must start at zero, but calls whose work
+ * overlaps on the GPU (concurrent streams, other host threads) race on it and
+ * must be serialised by the caller. */
+#define PDFS_STATIC_SCRATCH_BYTES (32ull << 20)
+
+/* Internal layout of the field for pdfs_sweep_static: row pitch px, rows per
+ * plane ry, total elements, and the scratch bytes the grid needs.  Returns
+ * PDFS_ERR_TOO_LARGE if the scratch exceeds PDFS_STATIC_SCRATCH_BYTES. */
+int pdfs_static_layout(const pdfs_grid *g, long long *px, long long *ry, long long *elems,
+                       long long *scratch_bytes);
+
+/* One ordering sn (1..8), in place on field_dev, on `stream` (a
+ * cudaStream_t, NULL = the default stream); waits for the stream, then
+ * stores the sweep's max change in *max_change (nullable). */
+int pdfs_sweep_static(const pdfs_grid *g, double *field_dev, int sn, double *max_change, void *stream);
 
 /* Human-readable text of a status code (static storage). */
 const char *pdfs_status_string(int status);

@@ -16,6 +16,8 @@ PDFS_ERR_TIMEOUT = -4
 PDFS_ERR_NOT_CONVERGED = -5
 PDFS_ERR_IO = -6
 PDFS_ERR_NO_DEVICE = -7
+PDFS_ERR_TOO_LARGE = -8
+STATIC_SCRATCH_BYTES = 32 << 20
 
 PREC_FP64, PREC_FP32, PREC_FP32_POLISH64 = 0, 1, 2
 ARITH_REFERENCE, ARITH_FAST = 0, 1
@@ -27,7 +29,7 @@ EXPORTS = [
     "pdfs_default_opts", "pdfs_solve", "pdfs_sweep", "pdfs_ctx_create", "pdfs_ctx_load", "pdfs_ctx_run",
     "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_status_string", "pdfs_version",
     "run_fsm", "pdfs_vti_read", "pdfs_vti_write", "pdfs_phi_free", "pdfs_calc_dist_field",
-    "pdfs_solve_batch", "pdfs_autotune",
+    "pdfs_solve_batch", "pdfs_autotune", "pdfs_static_layout", "pdfs_sweep_static",
 ]
 
 
@@ -112,5 +114,9 @@ def load(path: str = LIB_PATH):
     L.pdfs_solve_batch.restype = ip
     L.pdfs_autotune.argtypes = [C.POINTER(Grid), C.POINTER(Opts), C.POINTER(ip)]
     L.pdfs_autotune.restype = ip
+    L.pdfs_static_layout.argtypes = [C.POINTER(Grid)] + [C.POINTER(C.c_longlong)] * 4
+    L.pdfs_static_layout.restype = ip
+    L.pdfs_sweep_static.argtypes = [C.POINTER(Grid), vp, ip, C.POINTER(C.c_double), vp]
+    L.pdfs_sweep_static.restype = ip
     _lib = L
     return L

@@ -199,6 +199,7 @@ extern "C" const char *pdfs_status_string(int s) {
     case PDFS_ERR_NOT_CONVERGED: return "not converged within max_sweeps";
     case PDFS_ERR_IO: return "I/O error";
     case PDFS_ERR_NO_DEVICE: return "no CUDA device";
+    case PDFS_ERR_TOO_LARGE: return "grid too large for the fixed scratch of pdfs_sweep_static";
     default: return "unknown status";
   }
 }
