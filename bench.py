@@ -43,7 +43,10 @@ def parse():
     p.add_argument("--workload", default="C4")
     p.add_argument("--mode", default="polish", choices=["polish", "fp32", "fp64", "fp64ref"])
     p.add_argument("--scheduler", default="none", choices=["none", "change", "learned"])
-    p.add_argument("--tol", type=float, default=1e-9, help="FP64 polish tolerance (max change)")
+    p.add_argument("--tol", type=float, default=1e-5, help="FP64 polish tolerance (max change)")
+    p.add_argument("--polish-arith", default="mixed", choices=["mixed", "fast"],
+                   help="polish arithmetic: FP64 field with FP32 increments, or all FP64")
+    p.add_argument("--no-sched-table", action="store_true", help="skip timing the three schedulers")
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--fixed-sweeps", type=int, default=0, help="profiling: run exactly this many sweeps")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 FSM comparison solve")
@@ -160,6 +163,20 @@ def peaks():
         return {}
 
 
+def traffic_per_launch(kind, prec, nodes):
+    """DRAM bytes of one launch of the dominant sweep kernel: the per-update
+    traffic an ncu capture measured (profiles/traffic.json, dram__bytes_read
+    + dram__bytes_write over the capture's voxel updates) times this
+    launch's updates; None without a capture for that kernel."""
+    try:
+        t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+    except (OSError, ValueError):
+        return None
+    key = "fp32" if kind == "fp32" else ("fp64_replace" if prec == 2 else "fp64_min")
+    e = t.get(key)
+    return None if not e else float(e["dram_bytes_per_update"]) * nodes
+
+
 def cpu_baseline(w, sweeps, threads):
     """The CPU restatement of the reference FSM (OpenMP over each hyperplane),
     timed on the host cores on `sweeps` orderings of the full grid."""
@@ -223,6 +240,8 @@ def main():
     prec = {"polish": L.PREC_FP32_POLISH64, "fp32": L.PREC_FP32, "fp64": L.PREC_FP64,
             "fp64ref": L.PREC_FP64}[args.mode]
     arith = L.ARITH_REFERENCE if args.mode == "fp64ref" else L.ARITH_FAST
+    if args.mode == "polish" and args.polish_arith == "mixed":
+        arith = L.ARITH_MIXED
     sched = {"none": L.SCHED_NONE, "change": L.SCHED_CHANGE, "learned": L.SCHED_LEARNED}[args.scheduler]
     if args.mode in ("fp64", "fp64ref"):
         sched = L.SCHED_NONE
@@ -300,13 +319,36 @@ def main():
         per_launch = w.interior * (16 + 8 + mask_b) if prec == L.PREC_FP32_POLISH64 else w.interior * (16 + mask_b)
         dur = k64 / max(s64, 1)
     achieved = per_launch / (dur / 1e3) / 1e9 if dur > 0 else 0.0
+    kname = "ws_sweep_kernel<float, 8, 2, MIN, FAST>" if dominant == "fp32" else \
+        "ws_sweep_kernel<double, 4, 1, %s, %s>" % ("REPLACE" if prec == L.PREC_FP32_POLISH64 else "MIN",
+                                                  {L.ARITH_MIXED: "MIXED", L.ARITH_FAST: "FAST"}.get(arith, "REF"))
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "kernel": f"col_sweep_kernel<{'float' if dominant == 'fp32' else 'double'}>",
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800 GB/s"}
+            "traffic": traffic_per_launch(dominant, prec, w.interior), "kernel": kname,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s",
+            "bytes_per_update": per_launch / w.interior}
     fp32_roof = None
     if s32:
         a32 = w.interior * (8 + mask_b) / (k32 / s32 / 1e3) / 1e9
         fp32_roof = {"achieved": a32, "frac": a32 / hbm, "ms_per_sweep": k32 / s32}
+
+    # the same solve under each scheduler (one timed run each, after one warm run)
+    sched_table = None
+    if not args.no_sched_table and args.fixed_sweeps == 0 and args.mode in ("polish", "fp32"):
+        sched_table = {}
+        for name, sv in (("none", L.SCHED_NONE), ("change", L.SCHED_CHANGE), ("learned", L.SCHED_LEARNED)):
+            o2 = dict(opts, scheduler=sv)
+            try:
+                with api.Context(w.nx, w.ny, w.nz, sp, **o2) as c2:
+                    c2.load(w.field, w.frozen)
+                    c2.run()
+                    t1 = time.perf_counter()
+                    s2 = c2.run()
+                    sched_table[name] = {"time_s": time.perf_counter() - t1,
+                                         "sweeps": s2["sweeps_fp32"] + s2["sweeps_fp64"],
+                                         "full_sweeps": s2["full_sweeps"],
+                                         "voxel_updates_per_node": s2["voxel_updates"] / w.interior}
+            except api.PdfsError as e:
+                sched_table[name] = {"unavailable": str(e)}
 
     cpu = None
     if rank == 0 and world >= 1 and not args.no_cpu and args.fixed_sweeps == 0:
@@ -326,6 +368,7 @@ def main():
             ("f32" if prec == L.PREC_FP32 else "f64"), "data": "synthetic (seeded spheres)",
             "config": {"workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "spacing": list(sp),
                        "mode": args.mode, "scheduler": args.scheduler, "polish_tol": args.tol,
+                       "polish_arith": args.polish_arith if args.mode == "polish" else None,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush needed)"},
             "time_to_converge_s": t_step,
@@ -333,7 +376,7 @@ def main():
                        "voxel_updates": st["voxel_updates"], "blocks_skipped": st["blocks_skipped"]},
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (plain["time_s"] / t_step) if plain else None,
-            "roofline": roof, "roofline_fp32_sweep": fp32_roof,
+            "roofline": roof, "roofline_fp32_sweep": fp32_roof, "schedulers": sched_table,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(sum(s["launches"] for s in stats)),
             "clocks": clk,
         }

@@ -49,6 +49,12 @@ enum {
   PDFS_ARITH_REFERENCE = 0, /* the reference's expression trees, no fused multiply-add:
                                bit-identical to phi3D_fsm.c compiled with -ffp-contract=off */
   PDFS_ARITH_FAST = 1,      /* shifted quadratic with fused multiply-add (about 1e-15 rel.)  */
+  PDFS_ARITH_MIXED = 2,     /* FP64 field, minima, update and convergence test; the local
+                               solve's increment above the smallest minimum (at most about
+                               h) in FP32: within about 1e-7 relative of the FP64 fixed
+                               point, a few FP64 operations per update (tile 1 only).  The
+                               increments' rounding keeps sweeps changing by ~1e-7 h: use
+                               a tol of 1e-6 h or more                                    */
 };
 
 /* Which nodes are updated. */
@@ -60,9 +66,11 @@ enum {
 /* Active-block scheduling of the sweeps (8^3 node blocks). */
 enum {
   PDFS_SCHED_NONE = 0,    /* every sweep visits every block                               */
-  PDFS_SCHED_CHANGE = 1,  /* visit blocks that changed, or touch a block that changed,
-                             in the previous two sweeps                                   */
-  PDFS_SCHED_LEARNED = 2, /* visit blocks the MLP predicts will change                    */
+  PDFS_SCHED_CHANGE = 1,  /* visit blocks that changed in one of the last 8 sweeps (one
+                             cycle of orderings) or whose face neighbour changed in the
+                             last sweep                                                   */
+  PDFS_SCHED_LEARNED = 2, /* of the blocks PDFS_SCHED_CHANGE would visit, those the MLP
+                             predicts will change                                         */
 };
 /* Whatever the scheduler, a solve only terminates after a sweep that visits
  * every block and changes nothing (FP32) or less than tol (FP64). */
@@ -138,6 +146,23 @@ int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats);
 int pdfs_ctx_store(pdfs_ctx *c, double *field);
 void pdfs_ctx_destroy(pdfs_ctx *c);
 
+/* The 8^3 node blocks of a context's grid: nbx = ceil(nx/8), nby, nbz alike.
+ * Block (bx, by, bz) has index (bz*nby + by)*nbx + bx and holds interior
+ * nodes x = 8bx+1 .. 8bx+8 (and likewise in y and z). */
+int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz);
+
+/* One ordering sn (1..8) on the context's working field, continuing from the
+ * previous pdfs_ctx_sweep; the first call after pdfs_ctx_load starts from the
+ * input.  FP32 min-update if opts.precision is PDFS_PREC_FP32, else FP64
+ * min-update.  active (nullable; host or device; one byte per block): nodes
+ * of blocks with active[b] == 0 keep their values.  block_change (nullable;
+ * host or device; one float per block) receives each block's max change
+ * (FP32: relative, FP64: absolute), *max_change the sweep's.  pdfs_ctx_store
+ * reads the field.  No counterpart in the reference, which sweeps every node
+ * (phi3D_fsm.c:83-119): this is the building block of block schedulers and
+ * of the traces their models learn from. */
+int pdfs_ctx_sweep(pdfs_ctx *c, int sn, const uint8_t *active, float *block_change, double *max_change);
+
 /* Solves n independent grids together (the batched configuration): each
  * sweep is one persistent launch over the columns of every grid still
  * sweeping, each round of 8 orderings replays from a CUDA graph, and a grid
@@ -151,6 +176,72 @@ int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fields, const
 /* Times the sweep tile variants on grid g (two sweeps each, synthetic field)
  * and returns the fastest pair as an opts.tile value (FP32 id | FP64 id << 8). */
 int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o, int *tile);
+
+/* ---- learned active-block scheduler ---------------------------------------------
+ * No counterpart in the reference (it sweeps every node).  A small MLP
+ * predicts, per 8^3 block, whether the block changes by more than the
+ * phase's tolerance in the next sweep.  PDFS_SCHED_LEARNED asks it about the
+ * blocks the history rule of PDFS_SCHED_CHANGE nominates, sweeps the ones
+ * it predicts active, and certifies the answer with full sweeps.
+ *
+ * Network: 16 features -> 64 (ReLU) -> 64 (ReLU) -> 1 logit; weights and
+ * activations in bf16, every sum accumulated in FP32.  Parameter order
+ * (row-major, [out][in]): W1[64][16], b1[64], W2[64][64], b2[64], w3[64], b3.
+ * A weight blob (opts.mlp_weights) is PDFS_MLP_PARAMS floats, each a bf16
+ * value, followed by the decision threshold on the logit.
+ *
+ * Features of block b before sweep s of a phase (ordering sn, phase
+ * tolerance tol; ck = the block's max change in sweep s-k, 0 before the
+ * phase's first sweep; L(c) = clamp(log2(c/tol), -32, 32)/16 for c > 0,
+ * else -2):
+ *   0 band: log2(1 + min(field over b) / (8 h)) / 8   (h = smallest spacing)
+ *   1 L(c1)   2 L(c2)
+ *   3 age / 9: the least k in 1..8 with ck > tol, else 9
+ *   4 phase (0 FP32 bulk, 1 FP64 polish)   5 min(s, 64) / 64
+ *   6..13 one-hot of sn
+ *   14 L(max c1 of the 3 face neighbours upwind of b in ordering sn)
+ *   15 L(c8): the block's change one cycle of orderings ago
+ * Label: the block's max change in sweep s > tol. */
+#define PDFS_MLP_IN 16
+#define PDFS_MLP_HIDDEN 64
+#define PDFS_MLP_PARAMS (64 * 16 + 64 + 64 * 64 + 64 + 64 + 1)
+#define PDFS_MLP_BLOB (PDFS_MLP_PARAMS + 1)
+
+/* Trainer: collects (features, label) samples from plain solves on the GPU
+ * and fits the network with the library's own bf16 forward / backward /
+ * Adam kernels. */
+typedef struct pdfs_mlp_trainer pdfs_mlp_trainer;
+int pdfs_mlp_trainer_create(int device, unsigned seed, pdfs_mlp_trainer **out);
+/* Solves (g, field, frozen) with every block swept -- FP32 to its fixed
+ * point, then the FP64 polish to o->tol when o->precision is
+ * PDFS_PREC_FP32_POLISH64; FP64 to o->tol when it is PDFS_PREC_FP64 (the
+ * phase feature is 1 for both FP64 phases) -- and, from the ninth sweep of each phase on
+ * (where the schedulers start), records one sample per block the history
+ * rule nominates.  *samples (nullable) receives the trainer's total. */
+int pdfs_mlp_trainer_add_solve(pdfs_mlp_trainer *t, const pdfs_grid *g, const double *field, const uint8_t *frozen,
+                               const pdfs_opts *o, long long *samples);
+/* Adam over the collected samples in shuffled mini-batches; positives
+ * weigh pos_weight.  *loss (nullable) receives the last epoch's mean
+ * weighted cross-entropy. */
+int pdfs_mlp_trainer_fit(pdfs_mlp_trainer *t, int epochs, int batch, float lr, float pos_weight, float *loss);
+/* The trained weights as a blob; the threshold is set so that the given
+ * fraction of the positive samples is predicted active.  *recall_out and
+ * *active_out (nullable) receive the recall and the predicted-active
+ * fraction on the collected samples. */
+int pdfs_mlp_trainer_weights(pdfs_mlp_trainer *t, float recall, float *blob, float *recall_out, float *active_out);
+void pdfs_mlp_trainer_destroy(pdfs_mlp_trainer *t);
+
+/* Kernel-level entry points (host pointers), for gradient checks: n samples
+ * of bf16 features x[n][16] and labels y[n].  grad receives the gradient of
+ * the mean weighted cross-entropy (PDFS_MLP_PARAMS floats), loss the loss. */
+int pdfs_mlp_grad(const float *params, const uint16_t *x, const uint8_t *y, int n, float pos_weight, float *grad,
+                  float *loss);
+/* One Adam step (bias-corrected, step >= 1) on FP32 master parameters with
+ * moments m and v; params_bf16 (nullable) receives the bf16 copy. */
+int pdfs_mlp_adam(float *params, float *m, float *v, const float *grad, int step, float lr, float beta1, float beta2,
+                  float eps, uint16_t *params_bf16);
+/* Logits of n samples under a blob (the fused inference arithmetic). */
+int pdfs_mlp_infer(const float *blob, const uint16_t *x, int n, float *logits);
 
 /* ---- allocation-free sweep ----------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -20,7 +20,7 @@ PDFS_ERR_TOO_LARGE = -8
 STATIC_SCRATCH_BYTES = 32 << 20
 
 PREC_FP64, PREC_FP32, PREC_FP32_POLISH64 = 0, 1, 2
-ARITH_REFERENCE, ARITH_FAST = 0, 1
+ARITH_REFERENCE, ARITH_FAST, ARITH_MIXED = 0, 1, 2
 FREEZE_NONE, FREEZE_MASK = 0, 1
 SCHED_NONE, SCHED_CHANGE, SCHED_LEARNED = 0, 1, 2
 
@@ -30,7 +30,13 @@ EXPORTS = [
     "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_status_string", "pdfs_version",
     "run_fsm", "pdfs_vti_read", "pdfs_vti_write", "pdfs_phi_free", "pdfs_calc_dist_field",
     "pdfs_solve_batch", "pdfs_autotune", "pdfs_static_layout", "pdfs_sweep_static",
+    "pdfs_ctx_blocks", "pdfs_ctx_sweep",
+    "pdfs_mlp_trainer_create", "pdfs_mlp_trainer_add_solve", "pdfs_mlp_trainer_fit", "pdfs_mlp_trainer_weights",
+    "pdfs_mlp_trainer_destroy", "pdfs_mlp_grad", "pdfs_mlp_adam", "pdfs_mlp_infer",
 ]
+MLP_IN, MLP_HIDDEN = 16, 64
+MLP_PARAMS = MLP_HIDDEN * MLP_IN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN + 1
+MLP_BLOB = MLP_PARAMS + 1
 
 
 class Grid(C.Structure):
@@ -118,5 +124,26 @@ def load(path: str = LIB_PATH):
     L.pdfs_static_layout.restype = ip
     L.pdfs_sweep_static.argtypes = [C.POINTER(Grid), vp, ip, C.POINTER(C.c_double), vp]
     L.pdfs_sweep_static.restype = ip
+    L.pdfs_ctx_blocks.argtypes = [vp, C.POINTER(ip), C.POINTER(ip), C.POINTER(ip)]
+    L.pdfs_ctx_blocks.restype = ip
+    L.pdfs_ctx_sweep.argtypes = [vp, ip, vp, vp, C.POINTER(C.c_double)]
+    L.pdfs_ctx_sweep.restype = ip
+    fp = C.POINTER(C.c_float)
+    L.pdfs_mlp_trainer_create.argtypes = [ip, C.c_uint, C.POINTER(vp)]
+    L.pdfs_mlp_trainer_create.restype = ip
+    L.pdfs_mlp_trainer_add_solve.argtypes = [vp, C.POINTER(Grid), vp, vp, C.POINTER(Opts), C.POINTER(C.c_longlong)]
+    L.pdfs_mlp_trainer_add_solve.restype = ip
+    L.pdfs_mlp_trainer_fit.argtypes = [vp, ip, ip, C.c_float, C.c_float, fp]
+    L.pdfs_mlp_trainer_fit.restype = ip
+    L.pdfs_mlp_trainer_weights.argtypes = [vp, C.c_float, vp, fp, fp]
+    L.pdfs_mlp_trainer_weights.restype = ip
+    L.pdfs_mlp_trainer_destroy.argtypes = [vp]
+    L.pdfs_mlp_trainer_destroy.restype = None
+    L.pdfs_mlp_grad.argtypes = [vp, vp, vp, ip, C.c_float, vp, fp]
+    L.pdfs_mlp_grad.restype = ip
+    L.pdfs_mlp_adam.argtypes = [vp, vp, vp, vp, ip, C.c_float, C.c_float, C.c_float, C.c_float, vp]
+    L.pdfs_mlp_adam.restype = ip
+    L.pdfs_mlp_infer.argtypes = [vp, vp, ip, vp]
+    L.pdfs_mlp_infer.restype = ip
     _lib = L
     return L

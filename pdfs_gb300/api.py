@@ -37,12 +37,18 @@ def _check_field(field):
 
 def make_opts(precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, freeze=L.FREEZE_NONE, scheduler=L.SCHED_NONE,
               tol=0.0, max_sweeps=0, fixed_sweeps=0, first_ordering=0, tile=0, device=0, verbose=0,
-              wait_ms=0) -> L.Opts:
+              wait_ms=0, mlp_weights=None) -> L.Opts:
+    """pdfs_opts from keyword arguments.  mlp_weights: a float32 blob of
+    MLP_BLOB values (kept alive by the caller while the options are used)."""
     o = L.Opts()
     L.load().pdfs_default_opts(C.byref(o))
     o.precision, o.arith, o.freeze, o.scheduler = precision, arith, freeze, scheduler
     o.tol, o.max_sweeps, o.fixed_sweeps, o.first_ordering = tol, max_sweeps, fixed_sweeps, first_ordering
     o.tile, o.device, o.verbose, o.spin_limit = tile, device, verbose, wait_ms
+    if mlp_weights is not None:
+        if mlp_weights.dtype != np.float32 or mlp_weights.size != L.MLP_BLOB or not mlp_weights.flags.c_contiguous:
+            raise ValueError("mlp_weights must be a contiguous float32 array of MLP_BLOB values")
+        o.mlp_weights = mlp_weights.ctypes.data
     return o
 
 
@@ -148,6 +154,29 @@ class Context:
         if s != L.PDFS_OK:
             raise PdfsError(s, "pdfs_ctx_store")
 
+    def blocks(self):
+        """(nbx, nby, nbz): the grid's 8^3 node blocks."""
+        b = [C.c_int() for _ in range(3)]
+        s = self._lib.pdfs_ctx_blocks(self.h, *(C.byref(x) for x in b))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_ctx_blocks")
+        return tuple(x.value for x in b)
+
+    def sweep(self, sn: int, active=None, block_change=None) -> float:
+        """One ordering on the working field (pdfs_ctx_sweep); active and
+        block_change are uint8 / float32 arrays with one entry per block,
+        (nbz, nby, nbx), or device pointers.  Returns the max change."""
+        if isinstance(active, np.ndarray):
+            active = np.ascontiguousarray(active, dtype=np.uint8)
+        if isinstance(block_change, np.ndarray):
+            if block_change.dtype != np.float32 or not block_change.flags.c_contiguous:
+                raise ValueError("block_change must be a C-contiguous float32 array")
+        ch = C.c_double(0.0)
+        s = self._lib.pdfs_ctx_sweep(self.h, int(sn), _ptr(active), _ptr(block_change), C.byref(ch))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_ctx_sweep")
+        return ch.value
+
     def close(self):
         if getattr(self, "h", None):
             self._lib.pdfs_ctx_destroy(self.h)
@@ -164,3 +193,100 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+# ---- learned block scheduler ---------------------------------------------------------
+class Trainer:
+    """The scheduler network's trainer (pdfs_mlp_trainer_*): samples come from
+    plain solves on the GPU, fitting runs the library's bf16 kernels."""
+
+    def __init__(self, device=0, seed=0):
+        self._lib = L.load()
+        h = C.c_void_p()
+        s = self._lib.pdfs_mlp_trainer_create(int(device), int(seed), C.byref(h))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_mlp_trainer_create")
+        self.h = h
+
+    def add_solve(self, field, spacing, frozen=None, **kw) -> int:
+        _check_field(field)
+        g = _grid(field, spacing)
+        o = make_opts(**kw)
+        n = C.c_longlong(0)
+        s = self._lib.pdfs_mlp_trainer_add_solve(self.h, C.byref(g), _ptr(field), _ptr(frozen), C.byref(o),
+                                                 C.byref(n))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_mlp_trainer_add_solve")
+        return n.value
+
+    def fit(self, epochs=4, batch=8192, lr=2e-3, pos_weight=4.0) -> float:
+        loss = C.c_float(0.0)
+        s = self._lib.pdfs_mlp_trainer_fit(self.h, int(epochs), int(batch), float(lr), float(pos_weight),
+                                           C.byref(loss))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_mlp_trainer_fit")
+        return loss.value
+
+    def weights(self, recall=0.99):
+        """(blob, recall, active fraction) with the threshold set for `recall`."""
+        blob = np.zeros(L.MLP_BLOB, dtype=np.float32)
+        r, a = C.c_float(0.0), C.c_float(0.0)
+        s = self._lib.pdfs_mlp_trainer_weights(self.h, float(recall), _ptr(blob), C.byref(r), C.byref(a))
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_mlp_trainer_weights")
+        return blob, r.value, a.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.pdfs_mlp_trainer_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mlp_grad(params, x_bits, y, pos_weight=1.0):
+    """GPU gradient (pdfs_mlp_grad): params float32[MLP_PARAMS], x_bits
+    uint16[n, 16] bf16 features, y uint8[n].  Returns (grad, loss)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x_bits = np.ascontiguousarray(x_bits, dtype=np.uint16)
+    y = np.ascontiguousarray(y, dtype=np.uint8)
+    g = np.zeros(L.MLP_PARAMS, dtype=np.float32)
+    loss = C.c_float(0.0)
+    s = L.load().pdfs_mlp_grad(_ptr(params), _ptr(x_bits), _ptr(y), len(y), float(pos_weight), _ptr(g),
+                               C.byref(loss))
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_mlp_grad")
+    return g, loss.value
+
+
+def mlp_adam(params, m, v, grad, step, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+    """One GPU Adam step (pdfs_mlp_adam) on copies; returns (params, m, v, bf16 bits)."""
+    p, m, v = (np.array(a, dtype=np.float32) for a in (params, m, v))
+    grad = np.ascontiguousarray(grad, dtype=np.float32)
+    pb = np.zeros(L.MLP_PARAMS, dtype=np.uint16)
+    s = L.load().pdfs_mlp_adam(_ptr(p), _ptr(m), _ptr(v), _ptr(grad), int(step), float(lr), float(beta1),
+                               float(beta2), float(eps), _ptr(pb))
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_mlp_adam")
+    return p, m, v, pb
+
+
+def mlp_infer(blob, x_bits):
+    """Logits of bf16 features under a weight blob (pdfs_mlp_infer)."""
+    blob = np.ascontiguousarray(blob, dtype=np.float32)
+    x_bits = np.ascontiguousarray(x_bits, dtype=np.uint16)
+    out = np.zeros(len(x_bits), dtype=np.float32)
+    s = L.load().pdfs_mlp_infer(_ptr(blob), _ptr(x_bits), len(x_bits), _ptr(out))
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_mlp_infer")
+    return out

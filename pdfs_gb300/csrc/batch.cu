@@ -89,7 +89,7 @@ int batch_phase(BatchState &B, std::vector<pdfs_ctx *> &ctx, const std::vector<i
   const bool f32 = which == 0;
   const pdfs_opts &o = ctx[0]->o;
   const int tile = f32 ? ctx[0]->t32 : ctx[0]->t64;
-  const int arith = o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : ARITH_FAST;
+  const int arith = o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : (o.arith == PDFS_ARITH_MIXED ? ARITH_MIXED : ARITH_FAST);
   bool iso = true;
   // per-grid sweep arguments and tensor maps
   std::vector<SweepArgs> args(n);

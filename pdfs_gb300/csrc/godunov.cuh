@@ -6,7 +6,7 @@
 // found by sorting the minima and trying 1, 2 then 3 active terms
 // (mpi_openacc/src/phi3D_fsm.c:132-182, single_gpu_cuda/src/phi3D_fsm.cu:249-295).
 //
-// Three variants:
+// Four variants:
 //   god_ref64  -- the reference's own expanded expression trees, every
 //                 operation an explicitly rounded intrinsic so nothing is fused:
 //                 bit-identical to the reference's C compiled without contraction.
@@ -14,6 +14,8 @@
 //   god32s     -- FP32, same shifted form evaluated branch-free (the expanded
 //                 form cancels catastrophically in FP32 once m is a few
 //                 hundred cells).
+//   god_mixed64 -- FP64 minima and result, FP32 increment (god32s on the
+//                 FP64 differences to the smallest minimum).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -157,6 +159,22 @@ __device__ __forceinline__ float god32s(float m0, float m1, float m2, const GodC
     const float u3 = fmaf(B + sqrtf(fmaxf(fmaf(B, B, -(q0 + q1 + q2) * Cc), 0.0f)), k.iqsum, m0);
     return (u1 <= m1) ? u1 : ((u2 <= m2) ? u2 : u3);
   }
+}
+
+// FP64 field, FP32 increment.  The minima, the base (the smallest minimum)
+// and the result stay FP64; only the increment above the base -- at most
+// about h, so its FP32 rounding is about 1e-7 h -- is solved in FP32 from the
+// FP64 differences.  Errors of a few 1e-8 h per update accumulate along a
+// characteristic of n nodes to about 1e-7 of its length n h, so the fixed
+// point lies within about 1e-7 relative of the FP64 one, at a handful of
+// FP64 operations per update instead of a full FP64 quadratic (GB300 issues
+// FP64 at 1/64 of the FP32 rate).
+template <bool ISO>
+__device__ __forceinline__ double god_mixed64(double m0, double m1, double m2, const GodConst32 &k) {
+  const double base = fmin(fmin(m0, m1), m2);
+  if (isinf(base)) return base;  // no finite neighbour: nothing to solve (avoids inf - inf)
+  const float e0 = (float)(m0 - base), e1 = (float)(m1 - base), e2 = (float)(m2 - base);
+  return base + (double)god32s<ISO>(e0, e1, e2, k);
 }
 
 }  // namespace pdfs

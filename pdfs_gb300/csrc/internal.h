@@ -53,10 +53,11 @@ TileShape tile64(int id);
 cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
                          const void *cap, int sms, cudaStream_t st, int *grid_used);
 
-// Change-based active set: blocks (or their face neighbours) that changed by
-// more than thr in either of the last two sweeps.  *count += active blocks.
-cudaError_t sched_change(const unsigned int *chg1, const unsigned int *chg2, float thr, uint8_t *active, int nbx,
-                         int nby, int nbz, int *count, int sms, cudaStream_t st);
+// Change-based active set: blocks that changed by more than thr in any of
+// the last hist sweeps, or whose face neighbour did in the last one (ring as
+// for sched_learned).  *count += active blocks.
+cudaError_t sched_change(const unsigned int *ring, int cur, int hist, float thr, uint8_t *active, int nbx, int nby,
+                         int nbz, int *count, int sms, cudaStream_t st);
 
 // Status words a sweep writes on the device (read back after each sweep).
 struct DevStatus {
@@ -66,6 +67,30 @@ struct DevStatus {
   int pad;
 };
 
+
+// FP32 phase convergence: max relative change of a full sweep (FP32
+// rounding creep stays around 1e-7).
+constexpr float kTol32 = 4.0e-6f;
+
+// Schedulers keep the per-block max change of the current sweep and of the
+// kHist sweeps before it in a ring of kHist + 1 slots (one full cycle of
+// orderings: a block that changes again has, in practice, changed within
+// the last cycle).
+constexpr int kHist = 8;
+constexpr int kRing = kHist + 1;
+
+// Weights of the learned scheduler compiled into the library (a blob of
+// PDFS_MLP_BLOB floats), or nullptr when none were built in.
+const float *default_mlp_blob();
+// Learned scheduler (mlp.cu): per-block minimum of a working field, and the
+// fused feature + network + decision kernel (active[b], *count += actives).
+cudaError_t block_min(const void *u, bool f32, const Layout &L, const pdfs_grid &g, int nbx, int nby, int nbz,
+                      float *bmin, cudaStream_t st);
+// ring: kRing slots of nblocks change words, slot cur = the sweep about to
+// run, slot (cur - k) mod kRing = k sweeps ago, hist = sweeps of history.
+cudaError_t sched_learned(const uint16_t *w, float thr, const unsigned int *ring, int cur, int hist,
+                          const float *bmin, int nbx, int nby, int nbz, int sn, int sweep, int phase, float tol,
+                          float hmin, uint8_t *active, int *count, int sms, cudaStream_t st);
 
 // Steps per mailbox chunk (matches WsGeo::C).
 constexpr int kMailboxChunk = 4;
@@ -97,11 +122,14 @@ struct pdfs_ctx {
   // 8^3 block bookkeeping for the scheduler
   int nbx = 0, nby = 0, nbz = 0;
   long long nblocks = 0;
-  unsigned int *bchg = nullptr;  // [3][nblocks] float bits of per-block max change, rotating
+  unsigned int *bchg = nullptr;  // [kRing][nblocks] float bits of per-block max change, rotating
   uint8_t *bact = nullptr;       // [nblocks] active mask of the next sweep
+  float *bmin = nullptr;         // [nblocks] per-block field minimum (learned scheduler)
+  uint16_t *mlp_w = nullptr;     // learned scheduler: bf16 network weights
+  float mlp_thr = 0.0f;          // its decision threshold on the logit
   bool loaded = false, has_mask = false;
   int last_prec = -1;      // which working field holds the last result
-  cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr, q0 = nullptr, q1 = nullptr;
   double kern_ms = 0.0;  // accumulated sweep-kernel time since the last reset
   int launches = 0;      // kernels launched since the last reset
 };
@@ -111,6 +139,9 @@ void fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *active
                      SweepArgs *out);
 void ordering_signs(int sn, int *sx, int *sy, int *sz);
 std::vector<int> wavefront_order(int ncx, int ncy, int tx, int ty);
+// One sweep of context c (which: 0 FP32 min, 1 FP64 min, 2 FP64 replace):
+// active = block mask or nullptr, blk_chg = per-block change or nullptr.
+int ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg);
 // FP64 input -> FP32 working field / FP32 result -> FP64 polish start
 int ctx_narrow(pdfs_ctx *c);
 int ctx_widen(pdfs_ctx *c);

@@ -10,20 +10,20 @@
 
 namespace pdfs {
 
-// active[b] = block b or one of its six face neighbours changed by more than
-// thr in either of the last two sweeps.  count receives the number of active
-// blocks.
-__global__ void k_sched_change(const unsigned int *__restrict__ chg1, const unsigned int *__restrict__ chg2,
-                               float thr, uint8_t *__restrict__ active, int nbx, int nby, int nbz,
-                               int *__restrict__ count) {
+// active[b] = block b changed by more than thr in one of the last hist
+// sweeps, or one of its six face neighbours did in the last sweep.  count
+// receives the number of active blocks.
+__global__ void k_sched_change(const unsigned int *__restrict__ ring, int cur, int hist, float thr,
+                               uint8_t *__restrict__ active, int nbx, int nby, int nbz, int *__restrict__ count) {
   const long long n = (long long)nbx * nby * nbz;
+  const unsigned int *c1 = ring + (size_t)((cur - 1 + kRing) % kRing) * n;
   int local = 0;
   for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n; b += (long long)gridDim.x * blockDim.x) {
     const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long long)nbx * nby));
-    auto hot = [&](long long i) {
-      return __uint_as_float(chg1[i]) > thr || __uint_as_float(chg2[i]) > thr;
-    };
-    bool on = hot(b);
+    auto hot = [&](long long i) { return __uint_as_float(c1[i]) > thr; };
+    bool on = false;
+    for (int k = 1; k <= hist && !on; ++k)
+      on = __uint_as_float(ring[(size_t)((cur - k + kRing) % kRing) * n + b]) > thr;
     if (!on && bx > 0) on = hot(b - 1);
     if (!on && bx < nbx - 1) on = hot(b + 1);
     if (!on && by > 0) on = hot(b - nbx);
@@ -37,12 +37,12 @@ __global__ void k_sched_change(const unsigned int *__restrict__ chg1, const unsi
   if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
 }
 
-cudaError_t sched_change(const unsigned int *chg1, const unsigned int *chg2, float thr, uint8_t *active, int nbx,
-                         int nby, int nbz, int *count, int sms, cudaStream_t st) {
+cudaError_t sched_change(const unsigned int *ring, int cur, int hist, float thr, uint8_t *active, int nbx, int nby,
+                         int nbz, int *count, int sms, cudaStream_t st) {
   const long long n = (long long)nbx * nby * nbz;
   int grid = (int)std::min<long long>((n + 255) / 256, (long long)sms * 8);
   if (grid < 1) grid = 1;
-  k_sched_change<<<grid, 256, 0, st>>>(chg1, chg2, thr, active, nbx, nby, nbz, count);
+  k_sched_change<<<grid, 256, 0, st>>>(ring, cur, hist, thr, active, nbx, nby, nbz, count);
   return cudaGetLastError();
 }
 

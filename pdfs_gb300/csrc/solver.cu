@@ -214,13 +214,15 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !std::isfinite(g->dx) || !std::isfinite(g->dy) ||
       !std::isfinite(g->dz))
     return PDFS_ERR_INVALID;
-  if (o->precision < 0 || o->precision > 2 || o->arith < 0 || o->arith > 1 || o->freeze < 0 || o->freeze > 1 ||
+  if (o->precision < 0 || o->precision > 2 || o->arith < 0 || o->arith > 2 || o->freeze < 0 || o->freeze > 1 ||
       o->scheduler < 0 || o->scheduler > 2 || o->tol < 0 || !std::isfinite(o->tol) || o->fixed_sweeps < 0 ||
       o->max_sweeps < 0 || o->first_ordering < 0 || o->first_ordering > 8)
     return PDFS_ERR_INVALID;
   const int t32 = o->tile & 0xff, t64 = (o->tile >> 8) & 0xff;
   if (t32 > tile_count32() || t64 > tile_count64()) return PDFS_ERR_INVALID;
-  if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 > 2) return PDFS_ERR_INVALID;  // polish kernel: TY = 4 only
+  if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 > 2) return PDFS_ERR_INVALID;  // polish kernels: tiles 1-2
+  if (o->arith == PDFS_ARITH_MIXED && t64 > 1) return PDFS_ERR_INVALID;  // mixed kernels: tile 1
+  if (o->scheduler == PDFS_SCHED_LEARNED && !o->mlp_weights && !default_mlp_blob()) return PDFS_ERR_INVALID;
   return PDFS_OK;
 }
 
@@ -294,8 +296,22 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   c->nby = (g->ny + 7) / 8;
   c->nbz = (g->nz + 7) / 8;
   c->nblocks = (long long)c->nbx * c->nby * c->nbz;
-  if ((e = cudaMalloc(&c->bchg, (size_t)c->nblocks * 3 * 4)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&c->bchg, (size_t)c->nblocks * kRing * 4)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->bact, (size_t)c->nblocks)) != cudaSuccess) return fail(e);
+  if (o.scheduler == PDFS_SCHED_LEARNED) {
+    const float *blob = o.mlp_weights ? o.mlp_weights : default_mlp_blob();
+    std::vector<uint16_t> wb(PDFS_MLP_PARAMS);
+    for (int i = 0; i < PDFS_MLP_PARAMS; ++i) {  // bf16 values: the upper half of the float
+      uint32_t u;
+      std::memcpy(&u, &blob[i], 4);
+      wb[i] = (uint16_t)(u >> 16);
+    }
+    c->mlp_thr = blob[PDFS_MLP_PARAMS];
+    if ((e = cudaMalloc(&c->mlp_w, PDFS_MLP_PARAMS * 2)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&c->bmin, (size_t)c->nblocks * 4)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpy(c->mlp_w, wb.data(), PDFS_MLP_PARAMS * 2, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(e);
+  }
   {
     std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
                      w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
@@ -313,6 +329,8 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((e = cudaEventCreate(&c->e1)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->k0)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->k1)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->q0)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->q1)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) return fail(e);
   *out = c;
   return PDFS_OK;
@@ -335,11 +353,15 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   cudaFree(c->dstat);
   cudaFree(c->bchg);
   cudaFree(c->bact);
+  cudaFree(c->bmin);
+  cudaFree(c->mlp_w);
   if (c->hstat) cudaFreeHost(c->hstat);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
   if (c->k0) cudaEventDestroy(c->k0);
   if (c->k1) cudaEventDestroy(c->k1);
+  if (c->q0) cudaEventDestroy(c->q0);
+  if (c->q1) cudaEventDestroy(c->q1);
   if (c->st) cudaStreamDestroy(c->st);
   cudaGetLastError();
   delete c;
@@ -446,6 +468,7 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   a.maxchg = &c->dstat->chg;
   a.blk_active = active;
   a.blk_chg = blk_chg;
+  a.cap = which == 2 ? (const void *)c->in64 : nullptr;
   a.nbx = c->nbx;
   a.nby = c->nby;
   a.nbz = c->nbz;
@@ -470,6 +493,11 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   a.k32.iso_h2 = (float)(g.dx * g.dx);
 }
 
+static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg);
+int pdfs::ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
+  return run_sweep(c, which, sn, active, blk_chg, chg);
+}
+
 static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
@@ -482,7 +510,7 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
   if (blk_chg) CK(cudaMemsetAsync(blk_chg, 0, (size_t)c->nblocks * 4, c->st));
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
-  const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : ARITH_FAST;
+  const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : (c->o.arith == PDFS_ARITH_MIXED ? ARITH_MIXED : ARITH_FAST);
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
   CK(launch_sweep(which, f32 ? c->t32 : c->t64, arith, iso, a, L, which == 2 ? (const void *)c->in64 : nullptr,
@@ -556,9 +584,9 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     CK(cudaEventRecord(c->e0, c->st));
     const bool sched = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0;
     const float thr = (float)tol;
-    unsigned int *bch[3] = {c->bchg, c->bchg + c->nblocks, c->bchg + 2 * c->nblocks};
+    // per-block changes: ring slot cur = this sweep, (cur - k) mod kRing = k sweeps ago
     int cur = 0;
-    if (sched) CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * 3 * 4, c->st));
+    if (sched) CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * kRing * 4, c->st));
     bool need_full = true;
     int s = 0;
     for (;;) {
@@ -572,15 +600,33 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
       const uint8_t *act = nullptr;
       long long nact = c->nblocks;
       if (!full) {
+        CK(cudaEventRecord(c->q0, c->st));
         CK(cudaMemsetAsync(&c->dstat->active_blocks, 0, 4, c->st));
-        CK(sched_change(bch[(cur + 2) % 3], bch[(cur + 1) % 3], thr, c->bact, c->nbx, c->nby, c->nbz,
-                        &c->dstat->active_blocks, c->sms, c->st));
-        c->launches++;
+        if (o.scheduler == PDFS_SCHED_LEARNED) {
+          const bool f32 = which == 0;
+          CK(block_min(f32 ? (const void *)c->u32 : (const void *)c->u64, f32, f32 ? c->L32 : c->L64, g, c->nbx,
+                       c->nby, c->nbz, c->bmin, c->st));
+          CK(sched_learned(c->mlp_w, c->mlp_thr, c->bchg, cur, std::min(s, kHist), c->bmin, c->nbx, c->nby,
+                           c->nbz, sn, s, f32 ? 0 : 1, thr, (float)std::min(g.dx, std::min(g.dy, g.dz)), c->bact,
+                           &c->dstat->active_blocks, c->sms, c->st));
+          c->launches += 2;
+        } else {
+          CK(sched_change(c->bchg, cur, std::min(s, kHist), thr, c->bact, c->nbx, c->nby, c->nbz,
+                          &c->dstat->active_blocks, c->sms, c->st));
+          c->launches++;
+        }
+        CK(cudaEventRecord(c->q1, c->st));
         act = c->bact;
       }
-      int r = run_sweep(c, which, sn, act, sched ? bch[cur] : nullptr, &chg);
+      int r = run_sweep(c, which, sn, act, sched ? c->bchg + (size_t)cur * c->nblocks : nullptr, &chg);
       if (r) return r;
-      if (!full) nact = c->hstat->active_blocks;
+      if (!full) {
+        nact = c->hstat->active_blocks;
+        st.ms_sched += ms_between(c->q0, c->q1);
+      }
+      if (verbose(o))
+        fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e active=%lld/%lld\n", which, s, sn,
+                full ? "full" : "skip", chg, nact, c->nblocks);
       ++s;
       if (full) {
         st.full_sweeps++;
@@ -591,7 +637,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
       }
       if (o.fixed_sweeps == 0 && full && chg <= tol) break;
       need_full = !full && chg <= tol;  // a quiet skipped sweep calls for a judging full sweep
-      cur = (cur + 1) % 3;              // bch[cur] becomes the previous sweep's changes
+      cur = (cur + 1) % kRing;          // this sweep's changes become history
     }
     CK(cudaEventRecord(c->e1, c->st));
     CK(cudaEventSynchronize(c->e1));
@@ -609,8 +655,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     c->last_prec = 1;
   } else {
     if ((r = ctx_narrow(c))) return r;
-    const double tol32 = 4.0e-6;  // relative; FP32 rounding creep stays ~1e-7
-    r = phase(0, tol32, &st.sweeps_fp32, &st.ms_fp32, &st.ms_kern_fp32);
+    r = phase(0, kTol32, &st.sweeps_fp32, &st.ms_fp32, &st.ms_kern_fp32);
     c->last_prec = 0;
     if (!r && o.precision == PDFS_PREC_FP32_POLISH64 && o.fixed_sweeps == 0) {
       if ((r = ctx_widen(c))) return r;
@@ -685,6 +730,48 @@ extern "C" int pdfs_solve(const pdfs_grid *g, double *field, const uint8_t *froz
   st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats) *stats = st;
   return s;
+}
+
+extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) {
+  if (!c) return PDFS_ERR_INVALID;
+  if (nbx) *nbx = c->nbx;
+  if (nby) *nby = c->nby;
+  if (nbz) *nbz = c->nbz;
+  return PDFS_OK;
+}
+
+extern "C" int pdfs_ctx_sweep(pdfs_ctx *c, int sn, const uint8_t *active, float *block_change, double *max_change) {
+  if (!c || !c->loaded || sn < 1 || sn > 8) return PDFS_ERR_INVALID;
+  CK(cudaSetDevice(c->dev));
+  const int prec = c->o.precision == PDFS_PREC_FP32 ? 0 : 1;
+  if (c->last_prec != prec) {  // start from the loaded input
+    if (prec == 1) {
+      CK(cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st));
+    } else {
+      int r = ctx_narrow(c);
+      if (r) return r;
+    }
+    c->last_prec = prec;
+  }
+  const size_t nb = (size_t)c->nblocks;
+  const uint8_t *act = nullptr;
+  if (active) {
+    if (is_device_ptr(active)) {
+      act = active;
+    } else {
+      CK(cudaMemcpyAsync(c->bact, active, nb, cudaMemcpyHostToDevice, c->st));
+      act = c->bact;
+    }
+  }
+  unsigned int *bc = block_change ? c->bchg : nullptr;  // bits of non-negative floats
+  double chg = 0.0;
+  int r = run_sweep(c, prec == 0 ? 0 : 1, sn, act, bc, &chg);
+  if (r) return r;
+  if (block_change)
+    CK(cudaMemcpyAsync(block_change, c->bchg, nb * 4, cudaMemcpyDefault, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (max_change) *max_change = chg;
+  return PDFS_OK;
 }
 
 extern "C" int pdfs_sweep(const pdfs_grid *g, double *field, const uint8_t *frozen, int sn, const pdfs_opts *o_in,

@@ -59,18 +59,14 @@ static cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty) {
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// The three tensor maps a variant reads: field slots, cap slots, mask words.
+// The tensor maps a variant reads: field slots, (unused), mask words.
 template <class T, int TY, int R, int MODE>
 static cudaError_t encode_maps(const SweepArgs &a, const Layout &L, const void *cap, CUtensorMap m[3]) {
   using G = WsGeo<T, TY, R, MODE>;
   cudaError_t e = encode_field_map(&m[0], a.u, sizeof(T), L, a.nz + 2, G::W, G::R);
   if (e != cudaSuccess) return e;
-  if (G::CAP) {
-    e = encode_field_map(&m[1], const_cast<void *>(cap), sizeof(T), L, a.nz + 2, G::TX, TY);
-    if (e != cudaSuccess) return e;
-  } else {
-    m[1] = m[0];
-  }
+  (void)cap;  // the polish cap is read through a.cap, not a map
+  m[1] = m[0];
   if (a.fmask) {
     e = encode_mask_map(&m[2], a, TY);
     if (e != cudaSuccess) return e;
@@ -118,6 +114,10 @@ static cudaError_t launch_one(const SweepArgs &a, const Layout *L, const void *c
   case ID:                                                                                                   \
     return arith == ARITH_REF ? launch_one<double, TY, R, MODE, ARITH_REF, false>(a, L, cap, ntick, sms, st, g) \
                               : launch_one<double, TY, R, MODE, ARITH_FAST, false>(a, L, cap, ntick, sms, st, g);
+// FP64 field with FP32 increments: the TY = 4 tile only
+#define PDFS_T64M(MODE)                                                                                  \
+  return iso ? launch_one<double, 4, 1, MODE, ARITH_MIXED, true>(a, L, cap, ntick, sms, st, g)          \
+             : launch_one<double, 4, 1, MODE, ARITH_MIXED, false>(a, L, cap, ntick, sms, st, g);
 
 static cudaError_t dispatch(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout *L,
                             const void *cap, int ntick, int sms, cudaStream_t st, int *g) {
@@ -131,6 +131,13 @@ static cudaError_t dispatch(int which, int tile, int arith, bool iso, const Swee
       default:
         return cudaErrorInvalidValue;
     }
+  } else if (arith == ARITH_MIXED) {
+    if (tile != 1) return cudaErrorInvalidValue;
+    if (which == 1) {
+      PDFS_T64M(MODE_MIN)
+    } else {
+      PDFS_T64M(MODE_REPLACE)
+    }
   } else if (which == 1) {
     switch (tile) {
       PDFS_T64(1, 4, 1, MODE_MIN)
@@ -143,13 +150,14 @@ static cudaError_t dispatch(int which, int tile, int arith, bool iso, const Swee
     switch (tile) {
       PDFS_T64(1, 4, 1, MODE_REPLACE)
       PDFS_T64(2, 4, 2, MODE_REPLACE)
-      default:  // the polish kernel (cap ring) fits shared memory only with TY = 4
+      default:
         return cudaErrorInvalidValue;
     }
   }
 }
 #undef PDFS_T32
 #undef PDFS_T64
+#undef PDFS_T64M
 
 cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
                          const void *cap, int sms, cudaStream_t st, int *g) {

@@ -17,10 +17,11 @@
 //     warp ly-1 produced the upwind y value one step earlier;
 //   * warps chain through per-warp step counters in shared memory (release /
 //     acquire), so there is no CTA-wide barrier per step;
-//   * a loader warp streams planes (field, frozen-mask words and, for the
-//     polish, the per-node cap) into a ring of D shared-memory slots with TMA
-//     (cp.async.bulk.tensor, mbarrier full/empty pairs), as far ahead as the
-//     ring allows;
+//   * a loader warp streams planes (field and frozen-mask words) into a ring
+//     of D shared-memory slots with TMA (cp.async.bulk.tensor, mbarrier
+//     full/empty pairs), as far ahead as the ring allows; the polish's
+//     per-node cap is read by each lane straight from global memory a few
+//     steps ahead, so the ring (and the CTA's shared memory) stays small;
 //   * a communication warp fetches the upwind faces of the neighbouring
 //     columns (all chunks that are ready, in one round trip) and publishes
 //     this column's per-row progress, so the compute warps never wait on a
@@ -50,7 +51,7 @@
 namespace pdfs {
 
 enum { MODE_MIN = 0, MODE_REPLACE = 1 };
-enum { ARITH_REF = 0, ARITH_FAST = 1 };
+enum { ARITH_REF = 0, ARITH_FAST = 1, ARITH_MIXED = 2 };
 enum { DEV_ERR_TIMEOUT = 1, DEV_ERR_SMEM_ALIGN = 2 };
 
 struct SweepArgs {
@@ -81,6 +82,7 @@ struct SweepArgs {
   GodConst64 k64;
   GodConst32 k32;
   const struct BatchDesc *batch;  // many grids in one launch (nullptr = this grid only)
+  const void *cap;        // replace-update: per-node upper bound (the input), field layout
 };
 
 // A batched sweep: tickets enumerate (grid, local column) pairs, each grid's
@@ -110,10 +112,9 @@ struct WsGeo {
   static constexpr int C = 4;   // steps per mailbox chunk
   static constexpr int HB = sizeof(T) == 8 ? 4 : 8;  // mailbox chunk ring depth
   static constexpr int NT = (NW + 2) * 32;  // NW compute warps, a TMA loader warp, a communication warp
-  static constexpr bool CAP = MODE == MODE_REPLACE;
+  static constexpr int CP = 4;  // replace-update: caps each lane prefetches ahead (registers)
   static constexpr size_t OFF_RING = 0;
-  static constexpr size_t OFF_CAP = OFF_RING + (size_t)D * SLOT * sizeof(T);
-  static constexpr size_t OFF_FR = OFF_CAP + (CAP ? (size_t)D * TX * TY * sizeof(T) : 0);
+  static constexpr size_t OFF_FR = OFF_RING + (size_t)D * SLOT * sizeof(T);
   static constexpr int MSL = 32;  // mask words per slot: 128 bytes, a legal TMA destination
   static constexpr size_t OFF_XB = OFF_FR + (size_t)D * MSL * 4;
   static constexpr size_t OFF_YB = OFF_XB + (size_t)HB * C * TY * sizeof(T);
@@ -121,11 +122,11 @@ struct WsGeo {
   static constexpr size_t OFF_DONE = OFF_BAR + (size_t)(2 * D + 2 * HB) * 8;
   static constexpr size_t BYTES = OFF_DONE + (size_t)NW * 4 + 16;
   static_assert(TY % R_ == 0, "rows per warp must divide TY");
-  static constexpr unsigned TX_BYTES = (unsigned)(R * W * sizeof(T) + (CAP ? TX * TY * sizeof(T) : 0));
+  static constexpr unsigned TX_BYTES = (unsigned)(R * W * sizeof(T));
   static constexpr unsigned MASK_BYTES = TY * 4;
-  // every TMA destination (field slot, cap slot, mask slot) starts on 128 bytes
-  static_assert((SLOT * sizeof(T)) % 128 == 0 && OFF_CAP % 128 == 0 && OFF_FR % 128 == 0, "TMA alignment");
-  static_assert((TX * TY * sizeof(T)) % 128 == 0 && TY * 4 >= 16 && TY <= MSL, "TMA box");
+  // every TMA destination (field slot, mask slot) starts on 128 bytes
+  static_assert((SLOT * sizeof(T)) % 128 == 0 && OFF_FR % 128 == 0, "TMA alignment");
+  static_assert(TY * 4 >= 16 && TY <= MSL, "TMA box");
 };
 
 // ---- PTX helpers ---------------------------------------------------------------------
@@ -217,6 +218,17 @@ PDFS_LU64(MODE_MIN, ARITH_FAST, god_fast64)
 PDFS_LU64(MODE_REPLACE, ARITH_REF, god_ref64)
 PDFS_LU64(MODE_REPLACE, ARITH_FAST, god_fast64)
 #undef PDFS_LU64
+#define PDFS_LUMX(MODE_, ISO_)                                                                       \
+  template <>                                                                                       \
+  __device__ __forceinline__ double local_update<double, MODE_, ARITH_MIXED, ISO_>(                 \
+      double m0, double m1, double m2, const SweepArgs &a) {                                        \
+    return god_mixed64<ISO_>(m0, m1, m2, a.k32);                                                    \
+  }
+PDFS_LUMX(MODE_MIN, true)
+PDFS_LUMX(MODE_MIN, false)
+PDFS_LUMX(MODE_REPLACE, true)
+PDFS_LUMX(MODE_REPLACE, false)
+#undef PDFS_LUMX
 
 // Records a timeout and raises the abort flags (global and CTA).
 __device__ __forceinline__ void raise_timeout(const SweepArgs &a, int col, volatile int *s_abort) {
@@ -243,7 +255,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, unsigned parity, const Sw
 
 template <class T, int TY, int R, int MODE, int ARITH, bool ISO>
 __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
-                                                                     const __grid_constant__ CUtensorMap tm_cap,
+                                                                     const __grid_constant__ CUtensorMap tm_unused,
                                                                      const __grid_constant__ CUtensorMap tm_mask,
                                                                      const __grid_constant__ SweepArgs a0) {
   using G = WsGeo<T, TY, R, MODE>;
@@ -251,7 +263,6 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
   static_assert((C & (C - 1)) == 0 && (HB & (HB - 1)) == 0, "power-of-two chunk sizes");
   extern __shared__ __align__(1024) unsigned char sm[];
   T *ring = reinterpret_cast<T *>(sm + G::OFF_RING);
-  T *capr = reinterpret_cast<T *>(sm + G::OFF_CAP);
   uint32_t *fring = reinterpret_cast<uint32_t *>(sm + G::OFF_FR);
   T *xband = reinterpret_cast<T *>(sm + G::OFF_XB);
   T *yband = reinterpret_cast<T *>(sm + G::OFF_YB);
@@ -260,7 +271,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
   uint64_t *bfull = empty + D;
   uint64_t *bempty = bfull + HB;
   int *done = reinterpret_cast<int *>(sm + G::OFF_DONE);  // per compute warp: steps completed
-  __shared__ int s_ticket, s_grid, s_lc;
+  __shared__ int s_ticket, s_grid, s_lc, s_zlo, s_zhi;
   __shared__ volatile int s_abort;
   __shared__ SweepArgs s_a;  // the current column's grid
   __shared__ const CUtensorMap *s_maps;
@@ -296,6 +307,8 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         }
       }
       if (*(volatile int *)(a0.err + 1)) s_abort = 1;
+      s_zlo = 0x7fffffff;
+      s_zhi = 0;
       for (int i = 0; i < D; ++i) {
         if (ncols_done) {
           mbar_inval(full + i);
@@ -314,7 +327,6 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       }
       mbar_fence_init();
     }
-    if (tid < NW) done[tid] = 0;
     __syncthreads();
     if (s_ticket >= ntick || s_abort) break;
     if (s_grid != cur_grid) {  // stage the column's grid description in shared memory
@@ -336,7 +348,6 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       __syncthreads();
     }
     const CUtensorMap *mp_u = batch ? s_maps : &tm_u;
-    const CUtensorMap *mp_cap = batch ? s_maps + 1 : &tm_cap;
     const CUtensorMap *mp_mask = batch ? s_maps + 2 : &tm_mask;
     T *__restrict__ u = reinterpret_cast<T *>(a.u);
     T *__restrict__ xbox = reinterpret_cast<T *>(a.xbox);
@@ -356,18 +367,93 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
     const int x0 = 1 + cx * TX, y0 = 1 + cy * TY;
     const long long rowbase = (long long)cx * TX;  // internal x index of x0 - V
 
+    // Active z range [zlo, zhi) of the column, in sweep order, under a block
+    // mask: the union of its active 8^3 blocks.  Nodes outside it keep their
+    // values this sweep, so only the steps that reach the range run; the
+    // column's face items outside the range are copied from the field.
+    constexpr int SKW = TX + TY - 2;  // lane (TX-1, TY-1) trails lane (0, 0) by SKW planes
+    int zlo = 0, zhi = nz;
+    if (a.blk_active) {
+      const int bx0 = (x0 - 1) >> 3, bx1 = min(a.nbx, (x0 - 1 + TX + 7) >> 3);
+      const int by0 = (y0 - 1) >> 3, by1 = min(a.nby, (y0 - 1 + TY + 7) >> 3);
+      const int nbxf = bx1 - bx0, nbf = nbxf * (by1 - by0);
+      int lo = 0x7fffffff, hi = 0;
+      for (int i = tid; i < nbf * a.nbz; i += blockDim.x) {
+        const int bz = i / nbf, rem = i - bz * nbf;
+        const int by = by0 + rem / nbxf, bx = bx0 + rem % nbxf;
+        if (__ldg(a.blk_active + ((long long)bz * a.nby + by) * a.nbx + bx)) {
+          const int g0 = 8 * bz + 1, g1 = min(8 * bz + 8, nz);  // global z planes of the block
+          lo = min(lo, a.sz > 0 ? g0 - 1 : nz - g1);
+          hi = max(hi, (a.sz > 0 ? g1 - 1 : nz - g0) + 1);
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+      }
+      if (lane == 0) {
+        atomicMin(&s_zlo, lo);
+        atomicMax(&s_zhi, hi);
+      }
+      __syncthreads();
+      zlo = s_zlo;
+      zhi = s_zhi;
+    }
+    // steps [t_start, t_end) and planes [p_start, p_end] this column works on
+    const bool any = zlo < zhi;
+    const int t_start = any ? zlo : 0;
+    const int t_end = any ? min(tsteps, zhi + SKW + 1) : 0;
+    const int p_start = any ? max(0, t_start - SKW) : 0;
+    const int p_end = any ? min(NP - 1, t_end + 1) : -1;
+    const int kb0 = t_start / C;                          // first mailbox chunk consumed
+    const int kb_end = any ? min(NB, (t_end - 1) / C + 1) : kb0;  // one past the last
+    if (a.blk_active) {
+      // face items outside the rows the steps write: x face rows
+      // [t_start-TX+1, t_end-TX+1), y face rows [t_start-TY+1, t_end-TY+1)
+      const int xl = a.sx > 0 ? TX - 1 : 0;  // lane holding the downwind x face
+      if (has_dnx) {
+        T *xout = reinterpret_cast<T *>(a.xbox) + (long long)col * a.xstride;
+        const int w0 = any ? t_start - TX + 1 : 0, w1 = any ? t_end - TX + 1 : 0;
+        const int dmax = nz + TY - 1;
+        for (int i = tid; i < dmax * TY; i += blockDim.x) {
+          const int d = i / TY, row = i - d * TY, z = d - row;
+          if ((d >= w0 && d < w1) || z < 0 || z >= nz) continue;
+          const int gy = a.sy > 0 ? row : TY - 1 - row;
+          if (y0 + gy > a.ny) continue;
+          const int gz = a.sz > 0 ? z + 1 : nz - z;
+          xout[i] = u[(long long)gz * a.plane + (long long)(y0 + gy) * a.px + rowbase + V + xl];
+        }
+      }
+      if (has_dny) {
+        T *yout = reinterpret_cast<T *>(a.ybox) + (long long)col * a.ystride;
+        const int w0 = any ? t_start - TY + 1 : 0, w1 = any ? t_end - TY + 1 : 0;
+        const int dmax = nz + TX - 1;
+        const int gyl = a.sy > 0 ? TY - 1 : 0;
+        for (int i = tid; i < dmax * TX; i += blockDim.x) {
+          const int d = i / TX, lx = i - d * TX, z = d - lx;
+          if ((d >= w0 && d < w1) || z < 0 || z >= nz) continue;
+          const int ln = a.sx > 0 ? lx : TX - 1 - lx;
+          if (x0 + ln > a.nx) continue;
+          const int gz = a.sz > 0 ? z + 1 : nz - z;
+          yout[i] = u[(long long)gz * a.plane + (long long)(y0 + gyl) * a.px + rowbase + V + ln];
+        }
+      }
+    }
+    if (tid < NW) done[tid] = t_start;
+    __syncthreads();
+
     if (warp == NW) {
       // ---------------------------- TMA loader warp (lane 0) ----------------------------
       if (lane == 0) {
-        int pl = 0;
+        int pl = p_start;  // planes p_start..p_end go to ring slots (p - p_start) % D
         long long t_last = cycles();
-        while (pl < NP) {
-          const int s = pl % D, use = pl / D;
+        while (pl <= p_end) {
+          const int s = (pl - p_start) % D, use = (pl - p_start) / D;
           if (use == 0 || mbar_test(empty + s, (use - 1) & 1)) {
             const int gz = a.sz > 0 ? pl : nz + 1 - pl;
             mbar_arrive_tx(full + s, G::TX_BYTES + (masked ? G::MASK_BYTES : 0u));
             tma_load_3d(ring + (size_t)s * SLOT, mp_u, (int)rowbase, y0 - 1, gz, full + s);
-            if (G::CAP) tma_load_3d(capr + (size_t)s * TX * TY, mp_cap, (int)rowbase + V, y0, gz, full + s);
             if (masked) tma_load_3d(fring + s * G::MSL, mp_mask, y0 - 1, cx, gz, full + s);
             ++pl;
             t_last = cycles();
@@ -382,9 +468,9 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         }
         if (s_abort) {
           // drain the TMA loads still in flight before the CTA leaves
-          for (int q = max(0, pl - D); q < pl; ++q) {
+          for (int q = max(p_start, pl - D); q < pl; ++q) {
             const long long t0 = cycles();
-            while (!mbar_try(full + q % D, (q / D) & 1) && cycles() - t0 < 4000000000ll) {
+            while (!mbar_try(full + (q - p_start) % D, ((q - p_start) / D) & 1) && cycles() - t0 < 4000000000ll) {
             }
           }
         }
@@ -394,11 +480,11 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       // Fills the mailbox-chunk ring from the upwind columns' mailboxes (every
       // ready chunk with a free slot, in one round trip) and publishes this
       // column's per-row progress.
-      int kb = 0, pub = 0;
+      int kb = kb0, pub = 0;  // chunk k goes to slot (k - kb0) % HB
       long long t_last = cycles();
       for (;;) {
         bool moved = false;
-        if (kb < NB) {
+        if (kb < kb_end) {
           // chunk k is complete once the row's progress >= k*C + C + TX - 1
           // (x face) / + TY - 1 (y face), or once the column is done
           int rdy = NB;
@@ -413,26 +499,26 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1) rdy = min(rdy, __shfl_xor_sync(0xffffffffu, rdy, off));
           int n = 0;  // chunks to fill now: ready and with a free slot
-          while (kb + n < min(rdy, NB) && n < HB) {
-            const int k = kb + n, useb = k / HB;
-            if (useb > 0 && !mbar_test(bempty + k % HB, (useb - 1) & 1)) break;
+          while (kb + n < min(rdy, kb_end) && n < HB) {
+            const int k = kb + n, useb = (k - kb0) / HB;
+            if (useb > 0 && !mbar_test(bempty + (k - kb0) % HB, (useb - 1) & 1)) break;
             ++n;
           }
           if (n > 0) {
             if (upx >= 0)
               for (int i = lane; i < n * C * TY; i += 32) {
                 const int k = kb + i / (C * TY);
-                xband[(k % HB) * C * TY + i % (C * TY)] =
+                xband[((k - kb0) % HB) * C * TY + i % (C * TY)] =
                     __ldcg(xbox + (long long)upx * a.xstride + (long long)kb * C * TY + i);
               }
             if (upy >= 0)
               for (int i = lane; i < n * C * TX; i += 32) {
                 const int k = kb + i / (C * TX);
-                yband[(k % HB) * C * TX + i % (C * TX)] =
+                yband[((k - kb0) % HB) * C * TX + i % (C * TX)] =
                     __ldcg(ybox + (long long)upy * a.ystride + (long long)kb * C * TX + i);
               }
             __syncwarp();
-            if (lane < n) mbar_arrive(bfull + (kb + lane) % HB);
+            if (lane < n) mbar_arrive(bfull + (kb + lane - kb0) % HB);
             kb += n;
             moved = true;
           }
@@ -454,7 +540,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           }
         }
         const bool published = __all_sync(0xffffffffu, lane >= TY || pub == tsteps);
-        if (kb >= NB && published) break;
+        if (kb >= kb_end && published) break;
         if (moved) {
           t_last = cycles();
         } else {
@@ -512,13 +598,31 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       T *xout = xbox + (long long)col * a.xstride;
       T *yout = ybox + (long long)col * a.ystride;
       // ring slot of plane p = lz + 1 of row 0 at step t (per lane), and of
-      // the write-back plane of row 0 (lane TX-1's plane, uniform)
-      int s0 = (1 - lx - ly0) % D;
+      // the write-back plane of row 0 (lane TX-1's plane, uniform); plane p
+      // sits in slot (p - p_start) mod D
+      int s0 = (t_start + 1 - lx - ly0 - p_start) % D;
       if (s0 < 0) s0 += D;
-      int swb = (1 - (TX - 1) - ly0) % D;
+      int swb = (t_start + 1 - (TX - 1) - ly0 - p_start) % D;
       if (swb < 0) swb += D;
-      int qw = 0, qslot = 0, qpar = 0;  // next plane to wait for, its slot and phase parity
-      for (int t = 0; t < tsteps; ++t) {
+      int qw = p_start, qslot = 0, qpar = 0;  // next plane to wait for, its slot and phase parity
+      int rel = p_start, rslot = 0;           // next plane to release and its slot
+      bool finished = true;
+      // replace-update: the caps of my nodes for the next CP steps, per row,
+      // prefetched from global memory (lanes sit on different planes, so the
+      // cap is not worth a ring of its own)
+      const T *__restrict__ capg = reinterpret_cast<const T *>(a.cap);
+      T capq[R][G::CP];
+      auto cap_at = [&](int r, int t) -> T {
+        const int lz = t - lx - ly0 - r;
+        if (MODE != MODE_REPLACE || !valid[r] || (unsigned)lz >= (unsigned)nz) return T(0);
+        const int gz = a.sz > 0 ? lz + 1 : nz - lz;
+        return __ldg(capg + (long long)gz * a.plane + grow[r]);
+      };
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int k = 0; k < G::CP; ++k) capq[r][k] = MODE == MODE_REPLACE ? cap_at(r, t_start + k) : T(0);
+      for (int t = t_start; t < t_end; ++t) {
         if (w > 0 && ld_acquire_cta_s(done + w - 1) < t) {
           const long long t0 = cycles();
           while (ld_acquire_cta_s(done + w - 1) < t) {
@@ -528,9 +632,12 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
               break;
             }
           }
-          if (__any_sync(0xffffffffu, s_abort != 0)) break;
+          if (__any_sync(0xffffffffu, s_abort != 0)) {
+            finished = false;
+            break;
+          }
         }
-        const int qneed = min(t - ly0 + 2, NP - 1);
+        const int qneed = min(t - ly0 + 2, p_end);
         bool ok = true;
         while (ok && qw <= qneed) {
           ok = mbar_wait(full + qslot, qpar, a, col, &s_abort);
@@ -542,8 +649,13 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         }
         const int kb = t / C;
         const int tc = t & (C - 1);
-        if (ok && tc == 0 && kb < NB) ok = mbar_wait(bfull + (kb & (HB - 1)), (kb / HB) & 1, a, col, &s_abort);
-        if (!__all_sync(0xffffffffu, ok)) break;
+        const int rkb = kb - kb0;  // chunk kb sits in slot rkb % HB
+        if (ok && (tc == 0 || t == t_start) && kb < kb_end)
+          ok = mbar_wait(bfull + (rkb & (HB - 1)), (rkb / HB) & 1, a, col, &s_abort);
+        if (!__all_sync(0xffffffffu, ok)) {
+          finished = false;
+          break;
+        }
 
         // Rows of one step are independent (different planes), so the step is
         // split into a load phase, a compute phase and a store phase: the R
@@ -579,8 +691,8 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             const T *sl = ring + sx_ * SLOT + o[r];
             cv[r] = sl[0];
             T up_x = sl[xm], dn_x = sl[-xm], up_y = sl[ym], dn_y = sl[-ym];
-            if (band_x) up_x = xband[(kb & (HB - 1)) * C * TY + tc * TY + ly0 + r];
-            if (r == 0 && band_y) up_y = yband[(kb & (HB - 1)) * C * TX + tc * TX + lx];
+            if (band_x) up_x = xband[(rkb & (HB - 1)) * C * TY + tc * TY + ly0 + r];
+            if (r == 0 && band_y) up_y = yband[(rkb & (HB - 1)) * C * TX + tc * TX + lx];
             int sz_lo = sx_ + zlo_slot, sz_hi = sx_ - zlo_slot;
             sz_lo = sz_lo < 0 ? sz_lo + D : (sz_lo >= D ? sz_lo - D : sz_lo);
             sz_hi = sz_hi < 0 ? sz_hi + D : (sz_hi >= D ? sz_hi - D : sz_hi);
@@ -591,7 +703,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             m0[r] = tmin(xl, xr);
             m1[r] = tmin(yd, yu);
             m2[r] = tmin(zl, zh);
-            if (MODE == MODE_REPLACE) capv[r] = capr[sx_ * TX * TY + gy[r] * TX + lane];
+            if (MODE == MODE_REPLACE) capv[r] = capq[r][0];
           }
         }
         T nv[R];
@@ -601,6 +713,14 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           if (act[r]) {
             const T g = local_update<T, MODE, ARITH, ISO>(m0[r], m1[r], m2[r], a);
             nv[r] = MODE == MODE_REPLACE ? tmin(capv[r], g) : tmin(cv[r], g);
+          }
+        }
+        if (MODE == MODE_REPLACE) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+#pragma unroll
+            for (int k = 0; k + 1 < G::CP; ++k) capq[r][k] = capq[r][k + 1];
+            capq[r][G::CP - 1] = cap_at(r, t + G::CP);
           }
         }
 #pragma unroll
@@ -626,7 +746,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int lzw = t - (TX - 1) - ly0 - r;
-          if (valid[r] && (unsigned)lzw < (unsigned)nz) {
+          if (valid[r] && lzw >= zlo && lzw < zhi) {  // planes outside [zlo, zhi) are unchanged
             int s = swb - r;
             if (s < 0) s += D;
             const int gz = a.sz > 0 ? lzw + 1 : nz - lzw;
@@ -638,18 +758,23 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         fence_proxy_async();
         __syncwarp();
         if (lane == 0) {
-          const int q = t - (TX - 1) - ly0 - (R - 1);
-          if (q >= 0 && q < NP) {
-            int s = swb - R;
-            if (s < 0) s += D;
-            mbar_arrive(empty + s);
+          // release every plane up to q (several at the first step of a
+          // column whose range starts late: the planes below its first
+          // step's release point were loaded and waited for, never used)
+          const int q = min(t - (TX - 1) - ly0 - (R - 1), p_end);
+          while (rel <= q) {
+            mbar_arrive(empty + rslot);
+            ++rel;
+            if (++rslot == D) rslot = 0;
           }
-          if (tc == C - 1 && kb < NB) mbar_arrive(bempty + (kb & (HB - 1)));
+          if (tc == C - 1 && kb < kb_end) mbar_arrive(bempty + (rkb & (HB - 1)));
           st_release_cta_s(done + w, t + 1);
         }
         if (++s0 == D) s0 = 0;
         if (++swb == D) swb = 0;
       }
+      // the column is complete: the face items past the range were copied up front
+      if (finished && lane == 0) st_release_cta_s(done + w, tsteps);
       if (a.blk_chg) {
 #pragma unroll
         for (int r = 0; r < R; ++r)

@@ -178,6 +178,31 @@ def test_fp32_polish_fp64(freeze):
     assert rel_err(a, b, 1.0) <= 1e-10
 
 
+@pytest.mark.parametrize("spacing", [(1.0, 1.0, 1.0), (1.0, 0.8, 0.5)])
+@pytest.mark.parametrize("prec", [L.PREC_FP32_POLISH64, L.PREC_FP64])
+def test_mixed_arithmetic_within_1e6(spacing, prec):
+    """FP64 field with FP32 increments: the polish (and a plain FP64-field
+    solve) lands within 1e-6 relative of the FP64 fixed point -- the
+    accuracy target of the FP32 + polish solve; about 1e-7 is expected.
+    The increments' rounding keeps sweeps changing by about 1e-7 h, so the
+    tolerance is set above that (1e-6 h)."""
+    w = W.random_spheres(150, 120, 110, *spacing, 20, 3.0, 14.0, seed=9)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=prec, arith=L.ARITH_MIXED,
+                   tol=1e-6 * min(sp), max_sweeps=200)
+    assert st["sweeps_fp64"] > 0
+    # tolerance: 1e-6 relative (the FP32 increment's rounding, ~1e-7 h per update)
+    assert rel_err(a, b, min(sp)) <= 1e-6
+
+
+def test_mixed_arithmetic_needs_tile_one():
+    w = W.random_spheres(40, 40, 40, 1.0, 1.0, 1.0, 3, 3.0, 8.0, seed=2)
+    with pytest.raises(api.PdfsError):
+        api.solve(w.field.copy(), (1.0, 1.0, 1.0), precision=L.PREC_FP64, arith=L.ARITH_MIXED, tile=2 << 8)
+
+
 def test_run_fsm_one_round_matches_reference_product():
     """The reference's product runs one round (single_gpu_cuda/src/phi3D.c:118)."""
     meta = json.load(open(os.path.join(GOLD, "c1_sphere64.json")))
