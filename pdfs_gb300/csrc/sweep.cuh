@@ -194,24 +194,27 @@ __device__ __forceinline__ T tmin(T a, T b) {  // the reference's min macro: a <
   return a < b ? a : b;
 }
 
+// The local solver of a kernel variant.  k64 / k32 are the compute warps'
+// register copies of the per-sweep constants.
 template <class T, int MODE, int ARITH, bool ISO>
-__device__ __forceinline__ T local_update(T m0, T m1, T m2, const SweepArgs &a);
+__device__ __forceinline__ T local_update(T m0, T m1, T m2, const GodConst64 &k64, const GodConst32 &k32);
 template <>
 __device__ __forceinline__ float local_update<float, MODE_MIN, ARITH_FAST, true>(float m0, float m1, float m2,
-                                                                                  const SweepArgs &a) {
-  return god32s<true>(m0, m1, m2, a.k32);
+                                                                                  const GodConst64 &,
+                                                                                  const GodConst32 &k32) {
+  return god32s<true>(m0, m1, m2, k32);
 }
 template <>
 __device__ __forceinline__ float local_update<float, MODE_MIN, ARITH_FAST, false>(float m0, float m1, float m2,
-                                                                                   const SweepArgs &a) {
-  return god32s<false>(m0, m1, m2, a.k32);
+                                                                                   const GodConst64 &,
+                                                                                   const GodConst32 &k32) {
+  return god32s<false>(m0, m1, m2, k32);
 }
 #define PDFS_LU64(MODE_, ARITH_, FN)                                                                  \
   template <>                                                                                         \
-  __device__ __forceinline__ double local_update<double, MODE_, ARITH_, false>(double m0, double m1, \
-                                                                              double m2,             \
-                                                                              const SweepArgs &a) {  \
-    return FN(m0, m1, m2, a.k64);                                                                     \
+  __device__ __forceinline__ double local_update<double, MODE_, ARITH_, false>(                      \
+      double m0, double m1, double m2, const GodConst64 &k64, const GodConst32 &) {                  \
+    return FN(m0, m1, m2, k64);                                                                       \
   }
 PDFS_LU64(MODE_MIN, ARITH_REF, god_ref64)
 PDFS_LU64(MODE_MIN, ARITH_FAST, god_fast64)
@@ -221,8 +224,8 @@ PDFS_LU64(MODE_REPLACE, ARITH_FAST, god_fast64)
 #define PDFS_LUMX(MODE_, ISO_)                                                                       \
   template <>                                                                                       \
   __device__ __forceinline__ double local_update<double, MODE_, ARITH_MIXED, ISO_>(                 \
-      double m0, double m1, double m2, const SweepArgs &a) {                                        \
-    return god_mixed64<ISO_>(m0, m1, m2, a.k32);                                                    \
+      double m0, double m1, double m2, const GodConst64 &, const GodConst32 &k32) {                 \
+    return god_mixed64<ISO_>(m0, m1, m2, k32);                                                      \
   }
 PDFS_LUMX(MODE_MIN, true)
 PDFS_LUMX(MODE_MIN, false)
@@ -450,7 +453,9 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         long long t_last = cycles();
         while (pl <= p_end) {
           const int s = (pl - p_start) % D, use = (pl - p_start) / D;
-          if (use == 0 || mbar_test(empty + s, (use - 1) & 1)) {
+          // try_wait suspends the thread in hardware until the slot is free
+          // (or a short time limit passes), so the loader does not spin
+          if (use == 0 || mbar_try(empty + s, (use - 1) & 1)) {
             const int gz = a.sz > 0 ? pl : nz + 1 - pl;
             mbar_arrive_tx(full + s, G::TX_BYTES + (masked ? G::MASK_BYTES : 0u));
             tma_load_3d(ring + (size_t)s * SLOT, mp_u, (int)rowbase, y0 - 1, gz, full + s);
@@ -463,7 +468,6 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
               raise_timeout(a, col, &s_abort);
               break;
             }
-            __nanosleep(64);
           }
         }
         if (s_abort) {
@@ -481,6 +485,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       // ready chunk with a free slot, in one round trip) and publishes this
       // column's per-row progress.
       int kb = kb0, pub = 0;  // chunk k goes to slot (k - kb0) % HB
+      unsigned nap = 32;      // idle back-off (ns), doubled up to 1 us while nothing moves
       long long t_last = cycles();
       for (;;) {
         bool moved = false;
@@ -543,6 +548,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         if (kb >= kb_end && published) break;
         if (moved) {
           t_last = cycles();
+          nap = 32;
         } else {
           if (s_abort || *(volatile int *)(a.err + 1)) {
             s_abort = 1;
@@ -553,30 +559,43 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             s_abort = 1;
             break;
           }
-          __nanosleep(128);
+          __nanosleep(nap);
+          nap = min(nap * 2, 1024u);
         }
       }
     } else {
       // ------------------------------- compute warps -------------------------------
       // warp w owns rows ly = w*R + r (sweep order); lane = global x offset.
       // At step t, lane lx of row ly updates plane lz = t - lx - ly.
+      //
+      // The per-sweep values live in registers: the SweepArgs copy sits in
+      // shared memory and every mbarrier / fence asm is a compiler barrier,
+      // so reading it inside the loop would reload it each step.
       const int w = warp;
       const int ly0 = w * R;
-      const int lx = a.sx > 0 ? lane : TX - 1 - lane;
+      const int sxd = a.sx, syd = a.sy, szd = a.sz;
+      const long long plane = a.plane;
+      const float hmin = a.hmin;
+      const GodConst64 k64 = a.k64;
+      const GodConst32 k32 = a.k32;
+      const uint8_t *__restrict__ blk_active = a.blk_active;
+      unsigned int *__restrict__ blk_chg = a.blk_chg;
+      const int nbx = a.nbx, nby = a.nby;
+      const int lx = sxd > 0 ? lane : TX - 1 - lane;
       int o[R], gy[R];
       bool valid[R];
       long long grow[R];  // global row offset of my node (without the plane term)
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int ly = ly0 + r;
-        gy[r] = a.sy > 0 ? ly : TY - 1 - ly;
+        gy[r] = syd > 0 ? ly : TY - 1 - ly;
         valid[r] = (y0 + gy[r] <= a.ny) && (x0 + lane <= a.nx);
         o[r] = (gy[r] + 1) * W + lane + V;
         grow[r] = (long long)(y0 + gy[r]) * a.px + rowbase + V + lane;
       }
       // 8^3 block bookkeeping: x and y block indices are fixed per lane/row,
       // the z block changes every 8 planes
-      const bool track = a.blk_active != nullptr || a.blk_chg != nullptr;
+      const bool track = blk_active != nullptr || blk_chg != nullptr;
       const int bxl = (x0 - 1 + lane) >> 3;
       int byr[R], bzr[R];
       bool actb[R];
@@ -592,14 +611,17 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       const bool band_y = (w == 0) && (upy >= 0);
       const bool wr_x = (lx == TX - 1) && has_dnx;
       const bool wr_y = (w == NW - 1) && has_dny;
-      const int xm = a.sx > 0 ? -1 : 1;           // smem offset of the upwind x neighbour
-      const int ym = a.sy > 0 ? -W : W;           // smem offset of the upwind y neighbour
-      const int zlo_slot = a.sz > 0 ? -1 : 1;     // ring step to the global z-1 plane
+      const int xm = sxd > 0 ? -1 : 1;  // smem offset of the upwind x neighbour
+      // the upwind lane's node exists (a descending sweep's upwind lane lies
+      // at x+1, past nx in a ragged last column: then the ring's halo is used)
+      const bool upx_lane_ok = sxd > 0 || x0 + lane + 1 <= a.nx;
+      const int ym = syd > 0 ? -W : W;  // smem offset of the upwind y neighbour
       T *xout = xbox + (long long)col * a.xstride;
       T *yout = ybox + (long long)col * a.ystride;
       // ring slot of plane p = lz + 1 of row 0 at step t (per lane), and of
       // the write-back plane of row 0 (lane TX-1's plane, uniform); plane p
-      // sits in slot (p - p_start) mod D
+      // sits in slot (p - p_start) mod D, so the sweep's upwind z plane of a
+      // node is one slot below its own and the downwind one a slot above
       int s0 = (t_start + 1 - lx - ly0 - p_start) % D;
       if (s0 < 0) s0 += D;
       int swb = (t_start + 1 - (TX - 1) - ly0 - p_start) % D;
@@ -615,13 +637,28 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       auto cap_at = [&](int r, int t) -> T {
         const int lz = t - lx - ly0 - r;
         if (MODE != MODE_REPLACE || !valid[r] || (unsigned)lz >= (unsigned)nz) return T(0);
-        const int gz = a.sz > 0 ? lz + 1 : nz - lz;
-        return __ldg(capg + (long long)gz * a.plane + grow[r]);
+        const int gz = szd > 0 ? lz + 1 : nz - lz;
+        return __ldg(capg + (long long)gz * plane + grow[r]);
       };
 #pragma unroll
       for (int r = 0; r < R; ++r)
 #pragma unroll
         for (int k = 0; k < G::CP; ++k) capq[r][k] = MODE == MODE_REPLACE ? cap_at(r, t_start + k) : T(0);
+      // Values a step hands to the next one in registers: prev[r] is my row
+      // r's result of the previous step -- the sweep's upwind z neighbour of
+      // my next node, the upwind x neighbour of lane lx+1's next node (passed
+      // by shuffle) and, within the warp, the upwind y neighbour of row r+1's
+      // next node.  The frozen-mask word of my node's plane travels down the
+      // warp the same way: lane lx receives from lane lx-1 the word it used a
+      // step earlier, so only lane lx = 0 reads it (all lanes reading it
+      // would hit one shared-memory bank 32 times).
+      T prev[R];
+      uint32_t mw[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        prev[r] = T(0);
+        mw[r] = 0;
+      }
       for (int t = t_start; t < t_end; ++t) {
         if (w > 0 && ld_acquire_cta_s(done + w - 1) < t) {
           const long long t0 = cycles();
@@ -657,6 +694,16 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           break;
         }
 
+        // the upwind x values (lane lx-1's results of the previous step)
+        T upx_sh[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          upx_sh[r] = sxd > 0 ? __shfl_up_sync(0xffffffffu, prev[r], 1) : __shfl_down_sync(0xffffffffu, prev[r], 1);
+          if (masked)
+            mw[r] = sxd > 0 ? __shfl_up_sync(0xffffffffu, mw[r], 1) : __shfl_down_sync(0xffffffffu, mw[r], 1);
+        }
+        const bool first = t == t_start;  // registers hold no previous step yet
+
         // Rows of one step are independent (different planes), so the step is
         // split into a load phase, a compute phase and a store phase: the R
         // update chains then overlap instead of waiting on each other's stores.
@@ -671,38 +718,52 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           sr[r] = sx_;
           act[r] = valid[r] && (unsigned)lz < (unsigned)nz;
           if (track && act[r]) {
-            const int gz = a.sz > 0 ? lz + 1 : nz - lz;
+            const int gz = szd > 0 ? lz + 1 : nz - lz;
             const int bz = (gz - 1) >> 3;
             if (bz != bzr[r]) {  // entering a new z block: flush the old one, fetch the new flag
-              const long long base = ((long long)bz * a.nby + byr[r]) * a.nbx + bxl;
-              if (a.blk_chg && bzr[r] >= 0 && accb[r] > T(0))
-                atomicMax(a.blk_chg + ((long long)bzr[r] * a.nby + byr[r]) * a.nbx + bxl,
-                          __float_as_uint((float)accb[r]));
+              const long long base = ((long long)bz * nby + byr[r]) * nbx + bxl;
+              if (blk_chg && bzr[r] >= 0 && accb[r] > T(0))
+                atomicMax(blk_chg + ((long long)bzr[r] * nby + byr[r]) * nbx + bxl, __float_as_uint((float)accb[r]));
               accb[r] = T(0);
               bzr[r] = bz;
-              actb[r] = a.blk_active ? __ldg(a.blk_active + base) != 0 : true;
+              actb[r] = blk_active ? __ldg(blk_active + base) != 0 : true;
             }
             act[r] = actb[r];
           }
-          if (act[r] && masked) act[r] = !((fring[sx_ * G::MSL + gy[r]] >> lane) & 1u);
+          if (masked) {
+            if (lx == 0 || first) mw[r] = fring[sx_ * G::MSL + gy[r]];
+            if (act[r]) act[r] = !((mw[r] >> lane) & 1u);
+          }
           cv[r] = T(0);
           m0[r] = m1[r] = m2[r] = capv[r] = T(0);
           if (valid[r] && (unsigned)lz < (unsigned)nz) {
             const T *sl = ring + sx_ * SLOT + o[r];
             cv[r] = sl[0];
-            T up_x = sl[xm], dn_x = sl[-xm], up_y = sl[ym], dn_y = sl[-ym];
-            if (band_x) up_x = xband[(rkb & (HB - 1)) * C * TY + tc * TY + ly0 + r];
-            if (r == 0 && band_y) up_y = yband[(rkb & (HB - 1)) * C * TX + tc * TX + lx];
-            int sz_lo = sx_ + zlo_slot, sz_hi = sx_ - zlo_slot;
-            sz_lo = sz_lo < 0 ? sz_lo + D : (sz_lo >= D ? sz_lo - D : sz_lo);
-            sz_hi = sz_hi < 0 ? sz_hi + D : (sz_hi >= D ? sz_hi - D : sz_hi);
-            const T zl = ring[sz_lo * SLOT + o[r]], zh = ring[sz_hi * SLOT + o[r]];
+            const T dn_x = sl[-xm], dn_y = sl[-ym];
+            // upwind neighbours: registers where a previous step of this warp
+            // produced them, else the ring / the mailbox chunk
+            T up_x = upx_sh[r];
+            if (lx == 0 || first || !upx_lane_ok)
+              up_x = band_x ? xband[(rkb & (HB - 1)) * C * TY + tc * TY + ly0 + r] : sl[xm];
+            T up_y;
+            if (r > 0 && !first && valid[r > 0 ? r - 1 : 0])  // the upwind row's node exists
+              up_y = prev[r > 0 ? r - 1 : 0];
+            else if (r == 0 && band_y)
+              up_y = yband[(rkb & (HB - 1)) * C * TX + tc * TX + lx];
+            else
+              up_y = sl[ym];
+            int s_up = sx_ - 1, s_dn = sx_ + 1;
+            s_up = s_up < 0 ? s_up + D : s_up;
+            s_dn = s_dn >= D ? s_dn - D : s_dn;
+            const T z_up = (lz == 0 || first) ? ring[s_up * SLOT + o[r]] : prev[r];
+            const T z_dn = ring[s_dn * SLOT + o[r]];
             // the reference's minima keep global orientation: min(u[x-1], u[x+1])
-            const T xl = a.sx > 0 ? up_x : dn_x, xr = a.sx > 0 ? dn_x : up_x;
-            const T yd = a.sy > 0 ? up_y : dn_y, yu = a.sy > 0 ? dn_y : up_y;
+            const T xl = sxd > 0 ? up_x : dn_x, xr = sxd > 0 ? dn_x : up_x;
+            const T yd = syd > 0 ? up_y : dn_y, yu = syd > 0 ? dn_y : up_y;
+            const T zd = szd > 0 ? z_up : z_dn, zu = szd > 0 ? z_dn : z_up;
             m0[r] = tmin(xl, xr);
             m1[r] = tmin(yd, yu);
-            m2[r] = tmin(zl, zh);
+            m2[r] = tmin(zd, zu);
             if (MODE == MODE_REPLACE) capv[r] = capq[r][0];
           }
         }
@@ -711,9 +772,10 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
         for (int r = 0; r < R; ++r) {
           nv[r] = cv[r];
           if (act[r]) {
-            const T g = local_update<T, MODE, ARITH, ISO>(m0[r], m1[r], m2[r], a);
+            const T g = local_update<T, MODE, ARITH, ISO>(m0[r], m1[r], m2[r], k64, k32);
             nv[r] = MODE == MODE_REPLACE ? tmin(capv[r], g) : tmin(cv[r], g);
           }
+          prev[r] = nv[r];
         }
         if (MODE == MODE_REPLACE) {
 #pragma unroll
@@ -730,7 +792,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             ring[sr[r] * SLOT + o[r]] = nv[r];
             T d;
             if (sizeof(T) == 4)
-              d = (T)__fdividef(fabsf((float)cv[r] - (float)nv[r]), fmaxf((float)nv[r], a.hmin));
+              d = (T)__fdividef(fabsf((float)cv[r] - (float)nv[r]), fmaxf((float)nv[r], hmin));
             else
               d = (T)fabs((double)cv[r] - (double)nv[r]);
             tmax = fmax(tmax, d);
@@ -749,8 +811,8 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           if (valid[r] && lzw >= zlo && lzw < zhi) {  // planes outside [zlo, zhi) are unchanged
             int s = swb - r;
             if (s < 0) s += D;
-            const int gz = a.sz > 0 ? lzw + 1 : nz - lzw;
-            u[(long long)gz * a.plane + grow[r]] = ring[s * SLOT + o[r]];
+            const int gz = szd > 0 ? lzw + 1 : nz - lzw;
+            u[(long long)gz * plane + grow[r]] = ring[s * SLOT + o[r]];
           }
         }
         // ring plane t-(TX-1)-ly0-(R-1) is no longer touched by this warp; a
@@ -775,11 +837,11 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
       }
       // the column is complete: the face items past the range were copied up front
       if (finished && lane == 0) st_release_cta_s(done + w, tsteps);
-      if (a.blk_chg) {
+      if (blk_chg) {
 #pragma unroll
         for (int r = 0; r < R; ++r)
           if (bzr[r] >= 0 && accb[r] > T(0))
-            atomicMax(a.blk_chg + ((long long)bzr[r] * a.nby + byr[r]) * a.nbx + bxl, __float_as_uint((float)accb[r]));
+            atomicMax(blk_chg + ((long long)bzr[r] * nby + byr[r]) * nbx + bxl, __float_as_uint((float)accb[r]));
       }
     }
     // the column's max change -> its grid's counter (one atomic per compute warp)
