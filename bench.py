@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--polish-arith", default="mixed", choices=["mixed", "fast"],
                    help="polish arithmetic: FP64 field with FP32 increments, or all FP64")
     p.add_argument("--no-sched-table", action="store_true", help="skip timing the three schedulers")
+    p.add_argument("--configs", action="store_true",
+                   help="accuracy report: every config's FP32 + polish solve against the plain FP64 FSM")
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--fixed-sweeps", type=int, default=0, help="profiling: run exactly this many sweeps")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 FSM comparison solve")
@@ -288,9 +290,53 @@ def run_batch(args, rank, world, pg, device):
         print(json.dumps(line), flush=True)
 
 
+def run_configs(args, device):
+    """One JSON line per config (C1..C4): the FP32 + mixed-polish solve and
+    the FP32-only solve against the plain FP64 FSM on the same input -- max
+    and RMS relative error, sweeps and times.  C1 also runs the FP64
+    reference arithmetic (bit-exact with the reference at tol 1e-12)."""
+    from pdfs_gb300 import _lib as L
+    from pdfs_gb300 import api
+    from pdfs_gb300 import workloads as W
+    for name in ("C1", "C2", "C3", "C4"):
+        w = W.config(name)
+        sp = (w.dx, w.dy, w.dz)
+        h = min(sp)
+        fz = dict(frozen=w.frozen, freeze=L.FREEZE_MASK, device=device)
+        ref = w.field.copy()
+        t0 = time.perf_counter()
+        ps = api.solve(ref, sp, precision=L.PREC_FP64, arith=L.ARITH_FAST, tol=1e-12, **fz)
+        t_plain = time.perf_counter() - t0
+        i = (slice(1, -1),) * 3
+        den = np.maximum(np.abs(ref[i]), h)
+        out = {"config": name, "workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "spacing": list(sp),
+               "plain_fp64": {"sweeps": ps["sweeps_fp64"], "time_s": t_plain}}
+        cases = [("fp32_polish_mixed", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_MIXED, tol=1e-5 * h)),
+                 ("fp32_only", dict(precision=L.PREC_FP32))]
+        if name == "C1":
+            cases.append(("fp64_reference_arith", dict(precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, tol=1e-12)))
+        for label, kw in cases:
+            f = w.field.copy()
+            t0 = time.perf_counter()
+            st = api.solve(f, sp, **kw, **fz)
+            t = time.perf_counter() - t0
+            e = np.abs(f[i] - ref[i]) / den
+            out[label] = {"max_rel_err": float(e.max()), "rms_rel_err": float(np.sqrt(np.mean(e * e))),
+                          "sweeps_fp32": st["sweeps_fp32"], "sweeps_fp64": st["sweeps_fp64"], "time_s": t,
+                          "speedup_vs_plain": t_plain / t}
+        print(json.dumps(out), flush=True)
+        del w, ref
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_init(args)
+    if args.configs:
+        from pdfs_gb300 import build as B
+        B.build()
+        if rank == 0:
+            run_configs(args, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world, pg)
         return

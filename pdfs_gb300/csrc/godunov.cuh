@@ -169,12 +169,54 @@ __device__ __forceinline__ float god32s(float m0, float m1, float m2, const GodC
 // point lies within about 1e-7 relative of the FP64 one, at a handful of
 // FP64 operations per update instead of a full FP64 quadratic (GB300 issues
 // FP64 at 1/64 of the FP32 rate).
+//
+// GB300 runs every FP64 instruction -- add, compare, min/max and the
+// double <-> float conversions alike -- at about 2 lane operations per clock
+// per SM (measured), 1/64 of FP32.  So the mixed path does its compares on
+// order-preserving integer keys and its conversions with integer bit
+// arithmetic, and keeps exactly four FP64 additions per update: the two
+// differences below, the final add, and the change in the sweep kernel.
+
+// Integer key with the order of the doubles (-0 sorts below +0; no NaN here).
+__device__ __forceinline__ long long dkey(double v) {
+  const long long b = __double_as_longlong(v);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double kmin(double a, double b) { return dkey(a) < dkey(b) ? a : b; }
+
+// x >= 0 (or +inf) to the nearest float (ties away from zero), by bit
+// arithmetic; values below the float range flush to 0.
+__device__ __forceinline__ float d2f_nonneg(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int de = (int)(hi >> 20);  // biased double exponent (sign bit is 0)
+  const int fe = de - 1023 + 127;
+  if (de == 0x7ff || fe >= 255) return __uint_as_float(0x7f800000u);
+  if (fe <= 0) return 0.0f;
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  return __uint_as_float((((unsigned)fe << 23) | mant) + ((lo >> 28) & 1u));
+}
+
+// v >= 0 (a float) to the same value as a double, by bit arithmetic (exact;
+// values below the normal float range flush to 0).
+__device__ __forceinline__ double f2d_nonneg(float v) {
+  const unsigned b = __float_as_uint(v);
+  if (b < 0x00800000u) return 0.0;
+  if (b >= 0x7f800000u) return __hiloint2double(0x7ff00000, 0);
+  const unsigned de = (b >> 23) + (1023 - 127), m = b & 0x7fffffu;
+  return __hiloint2double((int)((de << 20) | (m >> 3)), (int)(m << 29));
+}
+
 template <bool ISO>
 __device__ __forceinline__ double god_mixed64(double m0, double m1, double m2, const GodConst32 &k) {
-  const double base = fmin(fmin(m0, m1), m2);
-  if (isinf(base)) return base;  // no finite neighbour: nothing to solve (avoids inf - inf)
-  const float e0 = (float)(m0 - base), e1 = (float)(m1 - base), e2 = (float)(m2 - base);
-  return base + (double)god32s<ISO>(e0, e1, e2, k);
+  const long long k0 = dkey(m0), k1 = dkey(m1), k2 = dkey(m2);
+  const bool b0 = k0 <= k1 && k0 <= k2, b1 = !b0 && k1 <= k2;  // which axis holds the base
+  const double base = b0 ? m0 : (b1 ? m1 : m2);
+  if (((unsigned)__double2hiint(base) & 0x7ff00000u) == 0x7ff00000u) return base;  // no finite neighbour
+  // the two other minima, in axis order; their differences to the base
+  const double pa = b0 ? m1 : m0, pb = (b0 || b1) ? m2 : m1;
+  const float ea = d2f_nonneg(pa - base), eb = d2f_nonneg(pb - base);
+  const float e0 = b0 ? 0.0f : ea, e1 = b0 ? ea : (b1 ? 0.0f : eb), e2 = (b0 || b1) ? eb : 0.0f;
+  return base + f2d_nonneg(god32s<ISO>(e0, e1, e2, k));
 }
 
 }  // namespace pdfs

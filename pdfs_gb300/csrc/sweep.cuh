@@ -194,6 +194,30 @@ __device__ __forceinline__ T tmin(T a, T b) {  // the reference's min macro: a <
   return a < b ? a : b;
 }
 
+// Minimum, "changed" test and running max of a variant: the mixed FP64
+// kernels do them on integer keys / bit patterns, off the FP64 pipe.
+template <class T, int ARITH>
+__device__ __forceinline__ T vmin(T a, T b) {
+  if constexpr (sizeof(T) == 8 && ARITH == ARITH_MIXED)
+    return kmin(a, b);
+  else
+    return tmin(a, b);
+}
+template <class T, int ARITH>
+__device__ __forceinline__ bool vdiffers(T a, T b) {
+  if constexpr (sizeof(T) == 8 && ARITH == ARITH_MIXED)
+    return __double_as_longlong(a) != __double_as_longlong(b);
+  else
+    return a != b;
+}
+template <class T, int ARITH>
+__device__ __forceinline__ T vmax_nonneg(T a, T b) {  // a, b >= 0
+  if constexpr (sizeof(T) == 8 && ARITH == ARITH_MIXED)
+    return __double_as_longlong(a) < __double_as_longlong(b) ? b : a;
+  else
+    return fmax(a, b);
+}
+
 // The local solver of a kernel variant.  k64 / k32 are the compute warps'
 // register copies of the per-sweep constants.
 template <class T, int MODE, int ARITH, bool ISO>
@@ -761,9 +785,9 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             const T xl = sxd > 0 ? up_x : dn_x, xr = sxd > 0 ? dn_x : up_x;
             const T yd = syd > 0 ? up_y : dn_y, yu = syd > 0 ? dn_y : up_y;
             const T zd = szd > 0 ? z_up : z_dn, zu = szd > 0 ? z_dn : z_up;
-            m0[r] = tmin(xl, xr);
-            m1[r] = tmin(yd, yu);
-            m2[r] = tmin(zd, zu);
+            m0[r] = vmin<T, ARITH>(xl, xr);
+            m1[r] = vmin<T, ARITH>(yd, yu);
+            m2[r] = vmin<T, ARITH>(zd, zu);
             if (MODE == MODE_REPLACE) capv[r] = capq[r][0];
           }
         }
@@ -773,7 +797,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
           nv[r] = cv[r];
           if (act[r]) {
             const T g = local_update<T, MODE, ARITH, ISO>(m0[r], m1[r], m2[r], k64, k32);
-            nv[r] = MODE == MODE_REPLACE ? tmin(capv[r], g) : tmin(cv[r], g);
+            nv[r] = MODE == MODE_REPLACE ? vmin<T, ARITH>(capv[r], g) : vmin<T, ARITH>(cv[r], g);
           }
           prev[r] = nv[r];
         }
@@ -788,15 +812,15 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int lz = t - lx - ly0 - r;
-          if (act[r] && nv[r] != cv[r]) {
+          if (act[r] && vdiffers<T, ARITH>(nv[r], cv[r])) {
             ring[sr[r] * SLOT + o[r]] = nv[r];
             T d;
             if (sizeof(T) == 4)
               d = (T)__fdividef(fabsf((float)cv[r] - (float)nv[r]), fmaxf((float)nv[r], hmin));
             else
               d = (T)fabs((double)cv[r] - (double)nv[r]);
-            tmax = fmax(tmax, d);
-            accb[r] = fmax(accb[r], d);
+            tmax = vmax_nonneg<T, ARITH>(tmax, d);
+            accb[r] = vmax_nonneg<T, ARITH>(accb[r], d);
           }
           if (valid[r] && (unsigned)lz < (unsigned)nz) {
             if (wr_x) xout[(long long)(t - (TX - 1)) * TY + ly0 + r] = nv[r];
