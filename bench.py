@@ -437,9 +437,11 @@ def main():
         per_launch = w.interior * (16 + 8 + mask_b) if prec == L.PREC_FP32_POLISH64 else w.interior * (16 + mask_b)
         dur = k64 / max(s64, 1)
     achieved = per_launch / (dur / 1e3) / 1e9 if dur > 0 else 0.0
-    kname = "ws_sweep_kernel<float, 8, 2, MIN, FAST>" if dominant == "fp32" else \
-        "ws_sweep_kernel<double, 4, 1, %s, %s>" % ("REPLACE" if prec == L.PREC_FP32_POLISH64 else "MIN",
-                                                  {L.ARITH_MIXED: "MIXED", L.ARITH_FAST: "FAST"}.get(arith, "REF"))
+    ty32 = {1: (8, 2), 2: (8, 4), 3: (16, 4), 4: (8, 1), 5: (4, 2), 6: (6, 1)}.get(st["tile"] & 0xff, (0, 0))
+    ty64 = {1: (4, 1), 2: (4, 2), 3: (8, 2), 4: (6, 1)}.get(st["tile"] >> 8, (0, 0))
+    kname = "ws_sweep_kernel<float, %d, %d, MIN, FAST>" % ty32 if dominant == "fp32" else \
+        "ws_sweep_kernel<double, %d, %d, %s, %s>" % (ty64 + ("REPLACE" if prec == L.PREC_FP32_POLISH64 else "MIN",
+                                                     {L.ARITH_MIXED: "MIXED", L.ARITH_FAST: "FAST"}.get(arith, "REF")))
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": traffic_per_launch(dominant, prec, w.interior), "kernel": kname,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s",

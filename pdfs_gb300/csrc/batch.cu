@@ -391,9 +391,14 @@ extern "C" int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o_in, int *til
     }
   }
   b = 1e30;
-  // the polish kernel exists for the first two FP64 tiles only
-  const int n64 = o.precision == PDFS_PREC_FP32_POLISH64 ? 2 : tile_count64();
-  for (int t = 1; t <= n64; ++t) {
+  // FP64 candidates: the tiles valid for the arithmetic (see validate() in solver.cu)
+  std::vector<int> c64;
+  if (o.arith == PDFS_ARITH_MIXED)
+    c64 = {1, 4};
+  else
+    for (int t = 1; t <= (o.precision == PDFS_PREC_FP32_POLISH64 ? 2 : 3); ++t) c64.push_back(t);
+  if (o.arith == PDFS_ARITH_FAST) c64.push_back(4);
+  for (int t : c64) {
     double ms = 0;
     if (time_tile(PDFS_PREC_FP64, t, &ms) == PDFS_OK && ms < b) {
       b = ms;

@@ -220,8 +220,14 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
     return PDFS_ERR_INVALID;
   const int t32 = o->tile & 0xff, t64 = (o->tile >> 8) & 0xff;
   if (t32 > tile_count32() || t64 > tile_count64()) return PDFS_ERR_INVALID;
-  if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 > 2) return PDFS_ERR_INVALID;  // polish kernels: tiles 1-2
-  if (o->arith == PDFS_ARITH_MIXED && t64 > 1) return PDFS_ERR_INVALID;  // mixed kernels: tile 1
+  // FP64 kernels: tiles 1 and 4 for the mixed arithmetic; 1-3 for the
+  // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4)
+  if (o->arith == PDFS_ARITH_MIXED) {
+    if (t64 != 0 && t64 != 1 && t64 != 4) return PDFS_ERR_INVALID;
+  } else {
+    if (t64 == 4 && o->arith != PDFS_ARITH_FAST) return PDFS_ERR_INVALID;
+    if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 == 3) return PDFS_ERR_INVALID;
+  }
   if (o->scheduler == PDFS_SCHED_LEARNED && !o->mlp_weights && !default_mlp_blob()) return PDFS_ERR_INVALID;
   return PDFS_OK;
 }
@@ -230,10 +236,14 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
 // FP32: 32 x 8 columns with one row per compute warp (8 compute warps; 7.9
 // ms per 768^3 sweep against 10.0 ms for two rows per warp: the sweep is
 // latency-bound and more resident warps hide more of it).
+// FP64: the mixed arithmetic is latency-bound like FP32 and takes 32 x 6
+// columns (tile 4: 15.9 ms per 768^3 polish sweep against 20.4 ms for 32 x 4);
+// the reference and fast arithmetic are bound by the FP64 pipe (55 ms on
+// either tile) and keep 32 x 4.
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
   c->t32 = t32 ? t32 : 4;
-  c->t64 = t64 ? t64 : 1;
+  c->t64 = t64 ? t64 : (c->o.arith == PDFS_ARITH_MIXED ? 4 : 1);
 }
 
 extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_ctx **out) {

@@ -10,8 +10,9 @@ namespace pdfs {
 
 // Tile variants: columns are 32 nodes wide (one warp lane per x); TY rows,
 // R rows per compute warp.  {tx, ty, rows per warp}
-static const TileShape kT32[] = {{32, 8, 2}, {32, 8, 4}, {32, 16, 4}, {32, 8, 1}, {32, 4, 2}};
-static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}};
+static const TileShape kT32[] = {{32, 8, 2}, {32, 8, 4}, {32, 16, 4}, {32, 8, 1}, {32, 4, 2}, {32, 6, 1}};
+// tile 4 (32 x 6, one row per warp) exists for the fast and mixed arithmetic
+static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}, {32, 6, 1}};
 
 int tile_count32() { return (int)(sizeof(kT32) / sizeof(kT32[0])); }
 int tile_count64() { return (int)(sizeof(kT64) / sizeof(kT64[0])); }
@@ -45,7 +46,8 @@ cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// Frozen-mask map: 32-bit words, dims {fy, fw, nz+2}, box {TY, 1, 1}.
+// Frozen-mask map: 32-bit words, dims {fy, fw, nz+2}, box {MBOX, 1, 1} (the
+// column's TY rows rounded up to a 16-byte box).
 static cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty) {
   auto fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
@@ -68,7 +70,7 @@ static cudaError_t encode_maps(const SweepArgs &a, const Layout &L, const void *
   (void)cap;  // the polish cap is read through a.cap, not a map
   m[1] = m[0];
   if (a.fmask) {
-    e = encode_mask_map(&m[2], a, TY);
+    e = encode_mask_map(&m[2], a, G::MBOX);
     if (e != cudaSuccess) return e;
   } else {
     m[2] = m[0];
@@ -114,10 +116,10 @@ static cudaError_t launch_one(const SweepArgs &a, const Layout *L, const void *c
   case ID:                                                                                                   \
     return arith == ARITH_REF ? launch_one<double, TY, R, MODE, ARITH_REF, false>(a, L, cap, ntick, sms, st, g) \
                               : launch_one<double, TY, R, MODE, ARITH_FAST, false>(a, L, cap, ntick, sms, st, g);
-// FP64 field with FP32 increments: the TY = 4 tile only
-#define PDFS_T64M(MODE)                                                                                  \
-  return iso ? launch_one<double, 4, 1, MODE, ARITH_MIXED, true>(a, L, cap, ntick, sms, st, g)          \
-             : launch_one<double, 4, 1, MODE, ARITH_MIXED, false>(a, L, cap, ntick, sms, st, g);
+// FP64 field with FP32 increments: tiles 1 (TY = 4) and 4 (TY = 6), one row per warp
+#define PDFS_T64M(TY, MODE)                                                                              \
+  return iso ? launch_one<double, TY, 1, MODE, ARITH_MIXED, true>(a, L, cap, ntick, sms, st, g)         \
+             : launch_one<double, TY, 1, MODE, ARITH_MIXED, false>(a, L, cap, ntick, sms, st, g);
 
 static cudaError_t dispatch(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout *L,
                             const void *cap, int ntick, int sms, cudaStream_t st, int *g) {
@@ -128,16 +130,29 @@ static cudaError_t dispatch(int which, int tile, int arith, bool iso, const Swee
       PDFS_T32(3, 16, 4)
       PDFS_T32(4, 8, 1)
       PDFS_T32(5, 4, 2)
+      PDFS_T32(6, 6, 1)
       default:
         return cudaErrorInvalidValue;
     }
   } else if (arith == ARITH_MIXED) {
-    if (tile != 1) return cudaErrorInvalidValue;
-    if (which == 1) {
-      PDFS_T64M(MODE_MIN)
-    } else {
-      PDFS_T64M(MODE_REPLACE)
+    if (tile == 1) {
+      if (which == 1) {
+        PDFS_T64M(4, MODE_MIN)
+      } else {
+        PDFS_T64M(4, MODE_REPLACE)
+      }
+    } else if (tile == 4) {
+      if (which == 1) {
+        PDFS_T64M(6, MODE_MIN)
+      } else {
+        PDFS_T64M(6, MODE_REPLACE)
+      }
     }
+    return cudaErrorInvalidValue;
+  } else if (tile == 4) {  // fast arithmetic only (validated by the caller)
+    if (which == 1)
+      return launch_one<double, 6, 1, MODE_MIN, ARITH_FAST, false>(a, L, cap, ntick, sms, st, g);
+    return launch_one<double, 6, 1, MODE_REPLACE, ARITH_FAST, false>(a, L, cap, ntick, sms, st, g);
   } else if (which == 1) {
     switch (tile) {
       PDFS_T64(1, 4, 1, MODE_MIN)
@@ -186,6 +201,7 @@ cudaError_t encode_sweep_maps(int which, int tile, const SweepArgs &a, const Lay
       PDFS_M32(3, 16, 4)
       PDFS_M32(4, 8, 1)
       PDFS_M32(5, 4, 2)
+      PDFS_M32(6, 6, 1)
       default:
         return cudaErrorInvalidValue;
     }
@@ -194,6 +210,7 @@ cudaError_t encode_sweep_maps(int which, int tile, const SweepArgs &a, const Lay
       PDFS_M64(1, 4, 1, MODE_MIN)
       PDFS_M64(2, 4, 2, MODE_MIN)
       PDFS_M64(3, 8, 2, MODE_MIN)
+      PDFS_M64(4, 6, 1, MODE_MIN)
       default:
         return cudaErrorInvalidValue;
     }
@@ -201,6 +218,7 @@ cudaError_t encode_sweep_maps(int which, int tile, const SweepArgs &a, const Lay
     switch (tile) {
       PDFS_M64(1, 4, 1, MODE_REPLACE)
       PDFS_M64(2, 4, 2, MODE_REPLACE)
+      PDFS_M64(4, 6, 1, MODE_REPLACE)
       default:
         return cudaErrorInvalidValue;
     }

@@ -123,10 +123,14 @@ struct WsGeo {
   static constexpr size_t BYTES = OFF_DONE + (size_t)NW * 4 + 16;
   static_assert(TY % R_ == 0, "rows per warp must divide TY");
   static constexpr unsigned TX_BYTES = (unsigned)(R * W * sizeof(T));
-  static constexpr unsigned MASK_BYTES = TY * 4;
+  // mask words per plane load: the column's rows, from a 16-byte aligned
+  // start (a TMA copy's innermost coordinate must be a 16-byte multiple, so
+  // a TY that is not a multiple of 4 reads from (y0-1) rounded down to 4)
+  static constexpr int MBOX = TY % 4 == 0 ? TY : (TY + 6) / 4 * 4;
+  static constexpr unsigned MASK_BYTES = MBOX * 4;
   // every TMA destination (field slot, mask slot) starts on 128 bytes
   static_assert((SLOT * sizeof(T)) % 128 == 0 && OFF_FR % 128 == 0, "TMA alignment");
-  static_assert(TY * 4 >= 16 && TY <= MSL, "TMA box");
+  static_assert(MBOX * 4 >= 16 && MBOX <= MSL, "TMA box");
 };
 
 // ---- PTX helpers ---------------------------------------------------------------------
@@ -393,6 +397,8 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
     const bool has_dnx = lcx < a.ncx - 1, has_dny = lcy < a.ncy - 1;
     const int x0 = 1 + cx * TX, y0 = 1 + cy * TY;
     const long long rowbase = (long long)cx * TX;  // internal x index of x0 - V
+    const int mstart = TY % 4 == 0 ? y0 - 1 : (y0 - 1) & ~3;  // first mask word a plane load reads
+    const int moff = (y0 - 1) - mstart;                        // this column's first row within it
 
     // Active z range [zlo, zhi) of the column, in sweep order, under a block
     // mask: the union of its active 8^3 blocks.  Nodes outside it keep their
@@ -483,7 +489,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             const int gz = a.sz > 0 ? pl : nz + 1 - pl;
             mbar_arrive_tx(full + s, G::TX_BYTES + (masked ? G::MASK_BYTES : 0u));
             tma_load_3d(ring + (size_t)s * SLOT, mp_u, (int)rowbase, y0 - 1, gz, full + s);
-            if (masked) tma_load_3d(fring + s * G::MSL, mp_mask, y0 - 1, cx, gz, full + s);
+            if (masked) tma_load_3d(fring + s * G::MSL, mp_mask, mstart, cx, gz, full + s);
             ++pl;
             t_last = cycles();
           } else {
@@ -755,7 +761,7 @@ __global__ void __launch_bounds__((TY / R + 2) * 32) ws_sweep_kernel(const __gri
             act[r] = actb[r];
           }
           if (masked) {
-            if (lx == 0 || first) mw[r] = fring[sx_ * G::MSL + gy[r]];
+            if (lx == 0 || first) mw[r] = fring[sx_ * G::MSL + moff + gy[r]];
             if (act[r]) act[r] = !((mw[r] >> lane) & 1u);
           }
           cv[r] = T(0);

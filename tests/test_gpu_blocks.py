@@ -139,3 +139,27 @@ def test_masked_sweep_equals_frozen_sweep_fp32(grid, sn):
     assert got[keep].tobytes() == exp[keep].tobytes()
     sk = (off == 1) & (w.frozen == 0)
     assert got[sk].tobytes() == w.field[sk].astype(np.float32).astype(np.float64).tobytes()
+
+
+@pytest.mark.parametrize("sn", [2, 7])
+def test_masked_sweep_mixed_tile6(grid, sn):
+    """The 32 x 6 FP64 tile (mixed arithmetic): its frozen-mask words are
+    loaded from a 16-byte aligned start and indexed from the column's
+    offset; a masked sweep must equal the same kernel with the inactive
+    blocks frozen, bit for bit."""
+    w = grid
+    rng = np.random.default_rng(300 + sn)
+    kw = dict(precision=L.PREC_FP64, arith=L.ARITH_MIXED, tile=4 << 8)
+    with ctx_for(w, **kw) as c:
+        nb = c.blocks()[::-1]
+        act = patterned_mask(nb, rng)
+        c.sweep(sn, act)
+        got = np.empty_like(w.field)
+        c.store(got)
+    fz = (w.frozen | node_mask(act, w.field.shape)).astype(np.uint8)
+    with api.Context(w.nx, w.ny, w.nz, (w.dx, w.dy, w.dz), freeze=L.FREEZE_MASK, **kw) as c2:
+        c2.load(w.field, fz)
+        c2.sweep(sn)
+        exp = np.empty_like(w.field)
+        c2.store(exp)
+    assert got.tobytes() == exp.tobytes()

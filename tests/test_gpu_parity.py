@@ -37,7 +37,7 @@ def rel_err(a, b, h):
 
 
 TILES64 = [t << 8 for t in (1, 2, 3)]
-TILES32 = [1, 2, 3, 4, 5]
+TILES32 = [1, 2, 3, 4, 5, 6]
 
 
 def test_godunov_known_answers_on_gpu():
@@ -197,10 +197,39 @@ def test_mixed_arithmetic_within_1e6(spacing, prec):
     assert rel_err(a, b, min(sp)) <= 1e-6
 
 
-def test_mixed_arithmetic_needs_tile_one():
+@pytest.mark.parametrize("shape", [(97, 121, 53), (40, 7, 31)])
+def test_mixed_tile6_within_1e6(shape):
+    """The 32 x 6 FP64 tile of the mixed arithmetic on ragged grids (ny not a
+    multiple of 6), polish and FP64-field solve."""
+    w = W.random_spheres(*shape, 1.0, 1.0, 1.0, 6, 2.0, 9.0, seed=13)
+    sp = (w.dx, w.dy, w.dz)
+    b = w.field.copy()
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    for prec in (L.PREC_FP32_POLISH64, L.PREC_FP64):
+        a = w.field.copy()
+        api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=prec, arith=L.ARITH_MIXED,
+                  tol=1e-6, max_sweeps=200, tile=4 << 8)
+        # tolerance: 1e-6 relative, as for the other mixed tiles
+        assert rel_err(a, b, 1.0) <= 1e-6
+
+
+def test_fp64_tile_validation():
+    """The mixed arithmetic runs on FP64 tiles 1 and 4 only; tile 4 (32 x 6)
+    exists for the fast and mixed arithmetic, not the reference one."""
     w = W.random_spheres(40, 40, 40, 1.0, 1.0, 1.0, 3, 3.0, 8.0, seed=2)
     with pytest.raises(api.PdfsError):
         api.solve(w.field.copy(), (1.0, 1.0, 1.0), precision=L.PREC_FP64, arith=L.ARITH_MIXED, tile=2 << 8)
+    with pytest.raises(api.PdfsError):
+        api.solve(w.field.copy(), (1.0, 1.0, 1.0), precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, tile=4 << 8)
+
+
+def test_fast_fp64_tile6_within_1e12():
+    w = W.random_spheres(97, 121, 53, 1.0, 1.0, 1.0, 8, 3.0, 12.0, seed=15)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, arith=L.ARITH_FAST, tol=0.0, tile=4 << 8)
+    assert rel_err(a, b, 1.0) <= 1e-12
 
 
 def test_run_fsm_one_round_matches_reference_product():
