@@ -10,6 +10,9 @@
  *   --tol T        convergence tolerance on the max change (FP64)
  *   --fp32         FP32 sweeps;   --polish   FP32 sweeps + FP64 polish
  *   --fast         shifted-form FP64 arithmetic instead of the reference's
+ *   --mixed        FP64 field with FP32 increments (with --polish: the fast
+ *                  polish; set --tol to at least 1e-6 of the spacing)
+ *   --sched S      block scheduler: none, change or learned
  *   --device D     CUDA device
  * Exit status 0 on success, 1 on any error (message on stderr).
  */
@@ -21,8 +24,8 @@
 
 static int usage(const char *argv0)
 {
-  printf("Usage: %s <file.vti> <prefix> [--rounds N | --converge] [--tol T] [--fp32 | --polish] [--fast] "
-         "[--device D]\n",
+  printf("Usage: %s <file.vti> <prefix> [--rounds N | --converge] [--tol T] [--fp32 | --polish] "
+         "[--fast | --mixed] [--sched none|change|learned] [--device D]\n",
          argv0);
   return 1;
 }
@@ -46,9 +49,21 @@ int main(int argc, char *argv[])
       o.precision = PDFS_PREC_FP32;
     } else if (!strcmp(argv[i], "--polish")) {
       o.precision = PDFS_PREC_FP32_POLISH64;
-      o.arith = PDFS_ARITH_FAST;
+      if (o.arith == PDFS_ARITH_REFERENCE) o.arith = PDFS_ARITH_FAST;
     } else if (!strcmp(argv[i], "--fast")) {
       o.arith = PDFS_ARITH_FAST;
+    } else if (!strcmp(argv[i], "--mixed")) {
+      o.arith = PDFS_ARITH_MIXED;
+    } else if (!strcmp(argv[i], "--sched") && i + 1 < argc) {
+      const char *v = argv[++i];
+      if (!strcmp(v, "none"))
+        o.scheduler = PDFS_SCHED_NONE;
+      else if (!strcmp(v, "change"))
+        o.scheduler = PDFS_SCHED_CHANGE;
+      else if (!strcmp(v, "learned"))
+        o.scheduler = PDFS_SCHED_LEARNED;
+      else
+        return usage(argv[0]);
     } else if (!strcmp(argv[i], "--device") && i + 1 < argc) {
       o.device = atoi(argv[++i]);
     } else {

@@ -10,7 +10,7 @@ namespace pdfs {
 
 // Tile variants: columns are 32 nodes wide (one warp lane per x); TY rows,
 // R rows per compute warp.  {tx, ty, rows per warp}
-static const TileShape kT32[] = {{32, 8, 2}, {32, 8, 4}, {32, 16, 4}, {32, 8, 1}, {32, 4, 2}, {32, 6, 1}};
+static const TileShape kT32[] = {{32, 8, 2}, {32, 8, 4}, {32, 16, 4}, {32, 8, 1}, {32, 4, 2}, {32, 6, 1}, {32, 10, 1}};
 // tile 4 (32 x 6, one row per warp) exists for the fast and mixed arithmetic
 static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}, {32, 6, 1}};
 
@@ -131,6 +131,7 @@ static cudaError_t dispatch(int which, int tile, int arith, bool iso, const Swee
       PDFS_T32(4, 8, 1)
       PDFS_T32(5, 4, 2)
       PDFS_T32(6, 6, 1)
+      PDFS_T32(7, 10, 1)
       default:
         return cudaErrorInvalidValue;
     }
@@ -202,6 +203,7 @@ cudaError_t encode_sweep_maps(int which, int tile, const SweepArgs &a, const Lay
       PDFS_M32(4, 8, 1)
       PDFS_M32(5, 4, 2)
       PDFS_M32(6, 6, 1)
+      PDFS_M32(7, 10, 1)
       default:
         return cudaErrorInvalidValue;
     }

@@ -37,7 +37,7 @@ def rel_err(a, b, h):
 
 
 TILES64 = [t << 8 for t in (1, 2, 3)]
-TILES32 = [1, 2, 3, 4, 5, 6]
+TILES32 = [1, 2, 3, 4, 5, 6, 7]
 
 
 def test_godunov_known_answers_on_gpu():

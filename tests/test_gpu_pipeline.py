@@ -97,3 +97,23 @@ def test_cli_converge_and_errors(tmp_path):
     assert r.returncode == 1 and "Unable to read file" in r.stdout
     r = subprocess.run([CLI], capture_output=True, text=True)
     assert r.returncode == 1 and "Usage" in r.stdout
+
+
+def test_cli_fast_polish_and_scheduler_options(tmp_path):
+    """--polish --mixed with the learned scheduler: the distance file agrees
+    with the converged plain FP64 run to the writer's 6 decimals (plus the
+    mixed arithmetic's ~1e-7 relative); an unknown scheduler is a usage error."""
+    src = os.path.join(GOLD, "sphere_in.vti")
+    r = subprocess.run([CLI, src, str(tmp_path / "c"), "--converge"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([CLI, src, str(tmp_path / "p"), "--polish", "--mixed", "--tol", "1e-6", "--sched", "learned"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    _, _, a = VT.read_output(str(tmp_path / "c_distfield.vti"))
+    _, _, b = VT.read_output(str(tmp_path / "p_distfield.vti"))
+    fin = np.isfinite(a)
+    assert np.array_equal(fin, np.isfinite(b))
+    # tolerance: two units of the writer's last decimal, plus 1e-6 relative
+    assert np.all(np.abs(a[fin] - b[fin]) <= 2e-6 + 1e-6 * np.abs(a[fin]))
+    r = subprocess.run([CLI, src, str(tmp_path / "q"), "--sched", "sometimes"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage" in r.stdout
