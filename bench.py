@@ -227,7 +227,8 @@ def run_reference(args, rank, world, pg):
 
 def run_batch(args, rank, world, pg, device):
     """C5: 256 independent grids (per-axis sizes log-uniform 32..256, 1..20
-    spheres) solved in one batched solve -- persistent launches over a
+    spheres; under torchrun every rank solves its own batch, so value is the
+    whole job's grids/s) solved in one batched solve -- persistent launches over a
     per-grid ticket table, rounds replayed from a CUDA graph -- against
     looping the plain FP64 solver (and our own single-grid solve) over them.
     Host buffers on both sides (the batch API takes host or device fields)."""
@@ -269,7 +270,7 @@ def run_batch(args, rank, world, pg, device):
     if rank == 0:
         line = {
             "metric": "grids/s of the batched FP32 + FP64-polish solve (256 grids) vs looping the plain FP64 solver",
-            "value": len(ws) / t_batch, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
+            "value": world * len(ws) / t_batch, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded spheres)",
             "config": {"workload": "C5_256_grids_32-256", "grids": len(ws), "interior_nodes": nodes,
@@ -281,9 +282,9 @@ def run_batch(args, rank, world, pg, device):
             "speedup_vs_plain_loop": t_plain / t_batch, "max_rel_err_vs_plain": err,
             "sweeps_per_grid": {"fp32": float(np.mean([x["sweeps_fp32"] for x in st])),
                                 "fp64": float(np.mean([x["sweeps_fp64"] for x in st]))},
-            "e2e": {"value": len(ws) / t_batch, "unit": "grids/s",
-                    "h2d_bytes_per_step": int(sum(w.field.nbytes + w.frozen.nbytes for w in ws)),
-                    "d2h_bytes_per_step": int(sum(w.field.nbytes for w in ws))},
+            "e2e": {"value": world * len(ws) / t_batch, "unit": "grids/s",
+                    "h2d_bytes_per_step": int(world * sum(w.field.nbytes + w.frozen.nbytes for w in ws)),
+                    "d2h_bytes_per_step": int(world * sum(w.field.nbytes for w in ws))},
             "roofline": None, "cpu_baseline": None,
             "gpu_launches": int(max(x["launches"] for x in st)),  # one batched launch serves every grid
         }
@@ -398,7 +399,9 @@ def main():
         plain = {"sweeps": ps["sweeps_fp64"], "time_s": (ps["ms_fp64"] + 0.0) / 1e3,
                  "kernel_ms": ps["ms_kern_fp64"], "max_rel_err_vs_plain": err}
     plain_sweeps = plain["sweeps"] if plain else (st["sweeps_fp32"] + st["sweeps_fp64"])
-    value = w.interior * plain_sweeps / t_step / 1e9
+    # whole-job aggregate: every rank solves its own replica of the workload
+    # (a single grid does not shard), timed by the slowest rank
+    value = world * w.interior * plain_sweeps / t_step / 1e9
 
     # e2e through pdfs_solve with pinned host buffers
     e2e = None
@@ -418,10 +421,10 @@ def main():
             t1 = time.perf_counter()
             api.solve(f_np, sp, frozen=m_np, **opts)
             ts.append(time.perf_counter() - t1)
-        te = min(ts)
-        e2e = {"value": w.interior * plain_sweeps / te / 1e9, "unit": "Gvox-updates/s",
-               "h2d_bytes_per_step": int(w.field.nbytes + w.frozen.nbytes),
-               "d2h_bytes_per_step": int(w.field.nbytes), "time_to_converge_s": te}
+        te = max_over_ranks(pg, min(ts))
+        e2e = {"value": world * w.interior * plain_sweeps / te / 1e9, "unit": "Gvox-updates/s",
+               "h2d_bytes_per_step": int(world * (w.field.nbytes + w.frozen.nbytes)),
+               "d2h_bytes_per_step": int(world * w.field.nbytes), "time_to_converge_s": te}
 
     # roofline of the dominant kernel
     pk = peaks()
