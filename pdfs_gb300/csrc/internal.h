@@ -64,7 +64,7 @@ struct DevStatus {
   int err[4];
   unsigned long long chg;
   int active_blocks;  // blocks the scheduler activated for this sweep
-  int pad;
+  int sched_err;      // the learned scheduler's inference gave up (a bounded wait)
 };
 
 
@@ -88,9 +88,11 @@ cudaError_t block_min(const void *u, bool f32, const Layout &L, const pdfs_grid 
                       float *bmin, cudaStream_t st);
 // ring: kRing slots of nblocks change words, slot cur = the sweep about to
 // run, slot (cur - k) mod kRing = k sweeps ago, hist = sweeps of history.
+// The network runs on the tensor cores (tcgen05); *err is set if one of its
+// accumulator waits gives up.
 cudaError_t sched_learned(const uint16_t *w, float thr, const unsigned int *ring, int cur, int hist,
                           const float *bmin, int nbx, int nby, int nbz, int sn, int sweep, int phase, float tol,
-                          float hmin, uint8_t *active, int *count, int sms, cudaStream_t st);
+                          float hmin, uint8_t *active, int *count, int *err, int sms, cudaStream_t st);
 
 // Steps per mailbox chunk (matches WsGeo::C).
 constexpr int kMailboxChunk = 4;

@@ -1,6 +1,7 @@
-// mlp.cu -- the learned active-block scheduler: features, fused inference,
-// and the bf16 training kernels (forward, backward, Adam) with FP32
-// accumulation, plus the trainer that learns from plain-sweep traces.
+// mlp.cu -- the learned active-block scheduler: features, the fused
+// inference on the tensor cores (tcgen05 MMAs into TMEM), the bf16 training
+// kernels (forward, backward, Adam) with FP32 accumulation, and the trainer
+// that learns from plain-sweep traces.
 //
 // The reference has no scheduler: every ordering visits every node
 // (single_gpu_cuda/src/phi3D_fsm.cu:144-189, mpi_openacc/src/phi3D_fsm.c:83-119).
@@ -190,42 +191,209 @@ __global__ void k_append(const uint16_t *__restrict__ xin, const uint8_t *__rest
   }
 }
 
-// Fused inference: for every block the history rule nominates, features +
-// network + decision (the network prunes the rule's candidates).
-__global__ void __launch_bounds__(128, 4) k_mlp_schedule(const uint16_t *__restrict__ w, float thr, FeatArgs f,
-                                                         uint8_t *__restrict__ active, int *__restrict__ count) {
-  extern __shared__ float sw[];
-  load_weights(sw, w);
-  __syncthreads();
-  const long long n = (long long)f.nbx * f.nby * f.nbz;
-  int local = 0;
-  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n; b += (long long)gridDim.x * blockDim.x) {
-    bool on = history_rule(f, b);
-    if (on) {
-      float x[NI], h1[NH];
-      block_features(f, b, x);
-      on = mlp_forward(sw, x, h1, nullptr, nullptr) > thr;
-    }
-    active[b] = on ? 1 : 0;
-    local += on ? 1 : 0;
-  }
+// ---- fused inference on the tensor cores (tcgen05, accumulators in TMEM) ---------------
+// A persistent loop over tiles of 128 rows (blocks, or given samples).  Row r
+// of a tile belongs to thread r: it writes its 16 bf16 features into the A
+// tile, reads its row of each accumulator back from TMEM (warp w owns TMEM
+// lanes 32w..32w+31) and finishes the 64 -> 1 output layer on the CUDA cores.
+//   layer 1: D1[128 x 64] = X[128 x 16] W1^T    one K = 16 MMA
+//   layer 2: D2[128 x 64] = H1[128 x 64] W2^T   four K = 16 MMAs
+// Operands are bf16 in the canonical K-major layout without swizzle: core
+// matrices of 8 rows x 16 bytes (rows contiguous), 128 bytes apart along K
+// (leading byte offset) and 16 K bytes apart along M / N (stride byte offset).
+// Accumulation is FP32; h1 is rounded to bf16 on its way back to shared
+// memory, as in the training kernels.
+namespace tc {
+constexpr int TM = 128;              // rows per tile (the MMA's M)
+constexpr uint32_t TMEM_COLS = 128;  // D1 in columns 0..63, D2 in 64..127
+constexpr size_t OFF_B1 = 0, OFF_B2 = OFF_B1 + NH * NI * 2, OFF_A1 = OFF_B2 + NH * NH * 2,
+                 OFF_A2 = OFF_A1 + TM * NI * 2, OFF_P = OFF_A2 + TM * NH * 2;
+constexpr size_t SMEM = OFF_P + (3 * NH + 1) * 4;
+// requested dynamic shared memory: at most 3 CTAs per SM, so their TMEM
+// allocations (3 x 128 of 512 columns) never wait on each other
+constexpr size_t SMEM_ALLOC = 64 * 1024;
+static_assert(SMEM <= SMEM_ALLOC, "tile layout");
+// kind::f16 instruction descriptor: D FP32 (bits 4-5), A and B bf16 (bits
+// 7-9, 10-12), both K-major, N / 8 at bits 17-22, M / 16 at bits 24-28
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NH >> 3) << 17) |
+                           ((uint32_t)(TM >> 4) << 24);
+}  // namespace tc
+
+// Byte offset of element (row, k) of a K-major operand with K columns.
+__device__ __forceinline__ uint32_t kmaj(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (16 * K) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+// Shared-memory matrix descriptor: start, leading and stride byte offsets
+// (each >> 4, 14 bits), descriptor version 1 at bit 46, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr_, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr_ >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// 16 consecutive accumulator columns of this thread's TMEM lane; the wait is
+// in the same statement so no use of the registers can move above it.
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float v[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) local += __shfl_xor_sync(0xffffffffu, local, off);
-  if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+// Bounded wait on an mbarrier phase (SM cycles).
+__device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity))
+    if (clock64() - t0 > 4000000000ll) return false;
+  return true;
 }
 
-// Logits of given samples (same arithmetic as k_mlp_schedule).
-__global__ void __launch_bounds__(128, 4) k_mlp_logits(const uint16_t *__restrict__ w, const uint16_t *__restrict__ x, long long n,
-                             float *__restrict__ out) {
-  extern __shared__ float sw[];
-  load_weights(sw, w);
-  __syncthreads();
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    float xf[NI], h1[NH];
-#pragma unroll
-    for (int k = 0; k < NI; ++k) xf[k] = bf2f(x[i * NI + k]);
-    out[i] = mlp_forward(sw, xf, h1, nullptr, nullptr);
+// SCHED: rows are the grid's blocks -- features, history rule, network and
+// decision (active[b], *count += actives).  Otherwise rows are the samples
+// xin[n][16] and the logits go to out.  *err is set if an accumulator wait
+// ever gives up (the CTA then stops and frees its TMEM).
+template <bool SCHED>
+__global__ void __launch_bounds__(128) k_mlp_tc(const uint16_t *__restrict__ w, float thr, FeatArgs f,
+                                                const uint16_t *__restrict__ xin, long long n,
+                                                uint8_t *__restrict__ active, int *__restrict__ count,
+                                                float *__restrict__ out, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char *B1 = sm + tc::OFF_B1, *B2 = sm + tc::OFF_B2, *A1 = sm + tc::OFF_A1, *A2 = sm + tc::OFF_A2;
+  float *pb = reinterpret_cast<float *>(sm + tc::OFF_P);  // b1 | b2 | w3 | b3
+  for (int i = tid; i < NH * NI; i += blockDim.x) *reinterpret_cast<uint16_t *>(B1 + kmaj(i / NI, i % NI, NI)) = w[OW1 + i];
+  for (int i = tid; i < NH * NH; i += blockDim.x) *reinterpret_cast<uint16_t *>(B2 + kmaj(i / NH, i % NH, NH)) = w[OW2 + i];
+  for (int i = tid; i < NH; i += blockDim.x) {
+    pb[i] = bf2f(w[OB1 + i]);
+    pb[NH + i] = bf2f(w[OB2 + i]);
+    pb[2 * NH + i] = bf2f(w[OW3 + i]);
   }
+  if (tid == 0) {
+    pb[3 * NH] = bf2f(w[OB3]);
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(&s_tmem)),
+                 "r"(tc::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_proxy_async();  // the weight tiles, written by threads, are read by the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  uint32_t par = 0;
+  int local = 0;
+  bool failed = false;
+  for (long long base = (long long)blockIdx.x * tc::TM; base < n; base += (long long)gridDim.x * tc::TM) {
+    const long long b = base + tid;
+    const bool valid = b < n;
+    float x[NI];
+    bool rule = false;
+#pragma unroll
+    for (int k = 0; k < NI; ++k) x[k] = 0.0f;
+    if (valid) {
+      if (SCHED) {
+        rule = history_rule(f, b);
+        block_features(f, b, x);
+      } else {
+#pragma unroll
+        for (int k = 0; k < NI; ++k) x[k] = bf2f(xin[b * NI + k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NI; ++k) *reinterpret_cast<uint16_t *>(A1 + kmaj(tid, k, NI)) = f2bf(x[k]);
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      tc_mma(tmem, sdesc(saddr(A1), 128, 16 * NI), sdesc(saddr(B1), 128, 16 * NI), tc::IDESC, 0);
+      tc_commit(&bar);
+    }
+    if (__syncthreads_or(!tc_wait(&bar, par))) {
+      failed = true;
+      break;
+    }
+    par ^= 1;
+    tc_fence_after();
+    // h1 = bf16(relu(D1 + b1)) -> row tid of the layer-2 operand
+#pragma unroll
+    for (int c = 0; c < NH; c += 16) {
+      float v[16];
+      tc_ld16(tmem + lane_base + c, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        *reinterpret_cast<uint16_t *>(A2 + kmaj(tid, c + i, NH)) = f2bf(fmaxf(v[i] + pb[c + i], 0.0f));
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int kk = 0; kk < NH / 16; ++kk)
+        tc_mma(tmem + NH, sdesc(saddr(A2) + kk * 256, 128, 16 * NH), sdesc(saddr(B2) + kk * 256, 128, 16 * NH),
+               tc::IDESC, kk > 0);
+      tc_commit(&bar);
+    }
+    if (__syncthreads_or(!tc_wait(&bar, par))) {
+      failed = true;
+      break;
+    }
+    par ^= 1;
+    tc_fence_after();
+    float z = pb[3 * NH];
+#pragma unroll
+    for (int c = 0; c < NH; c += 16) {
+      float v[16];
+      tc_ld16(tmem + lane_base + NH + c, v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) z = fmaf(pb[2 * NH + c + i], bfr(fmaxf(v[i] + pb[NH + c + i], 0.0f)), z);
+    }
+    if (SCHED) {
+      const bool on = valid && rule && z > thr;
+      if (valid) active[b] = on ? 1 : 0;
+      local += on ? 1 : 0;
+    } else if (valid) {
+      out[b] = z;
+    }
+    tc_fence_before();
+    __syncthreads();  // the next tile overwrites the operand tiles and the accumulators
+  }
+  if (SCHED) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) local += __shfl_xor_sync(0xffffffffu, local, off);
+    if ((tid & 31) == 0 && local) atomicAdd(count, local);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(tc::TMEM_COLS) : "memory");
+  if (failed && tid == 0) atomicExch(err, 1);
 }
 
 // ---- training ----------------------------------------------------------------------
@@ -407,9 +575,19 @@ struct DBuf {
 cudaError_t set_smem_attrs() {
   cudaError_t e = cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRAIN_SMEM);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_mlp_schedule, cudaFuncAttributeMaxDynamicSharedMemorySize, NP * 4);
+  e = cudaFuncSetAttribute(k_mlp_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_ALLOC);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_mlp_logits, cudaFuncAttributeMaxDynamicSharedMemorySize, NP * 4);
+  return cudaFuncSetAttribute(k_mlp_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_ALLOC);
+}
+
+// Logits of n samples (bf16 features) on the tensor cores; *err as k_mlp_tc.
+cudaError_t mlp_logits(const uint16_t *w, const uint16_t *x, long long n, float *out, int *err, int sms,
+                       cudaStream_t st) {
+  const int grid = (int)std::max<long long>(1, std::min<long long>((n + tc::TM - 1) / tc::TM, (long long)sms * 3));
+  FeatArgs none;
+  std::memset(&none, 0, sizeof(none));
+  k_mlp_tc<false><<<grid, 128, tc::SMEM_ALLOC, st>>>(w, 0.0f, none, x, n, nullptr, nullptr, out, err);
+  return cudaGetLastError();
 }
 
 // Gradient of the mean loss over n samples (in order) into grad (cleared here).
@@ -484,7 +662,7 @@ static FeatArgs feat_args(const unsigned int *ring, int cur, int hist, const flo
 
 cudaError_t sched_learned(const uint16_t *w, float thr, const unsigned int *ring, int cur, int hist,
                           const float *bmin, int nbx, int nby, int nbz, int sn, int sweep, int phase, float tol,
-                          float hmin, uint8_t *active, int *count, int sms, cudaStream_t st) {
+                          float hmin, uint8_t *active, int *count, int *err, int sms, cudaStream_t st) {
   static bool attrs = false;
   if (!attrs) {
     cudaError_t e = set_smem_attrs();
@@ -493,9 +671,8 @@ cudaError_t sched_learned(const uint16_t *w, float thr, const unsigned int *ring
   }
   const FeatArgs f = feat_args(ring, cur, hist, bmin, nbx, nby, nbz, sn, sweep, phase, tol, hmin);
   const long long n = (long long)nbx * nby * nbz;
-  int grid = (int)std::min<long long>((n + 127) / 128, (long long)sms * 4);
-  if (grid < 1) grid = 1;
-  k_mlp_schedule<<<grid, 128, NP * 4, st>>>(w, thr, f, active, count);
+  const int grid = (int)std::max<long long>(1, std::min<long long>((n + tc::TM - 1) / tc::TM, (long long)sms * 3));
+  k_mlp_tc<true><<<grid, 128, tc::SMEM_ALLOC, st>>>(w, thr, f, nullptr, n, active, count, nullptr, err);
   return cudaGetLastError();
 }
 
@@ -750,14 +927,20 @@ extern "C" int pdfs_mlp_trainer_weights(pdfs_mlp_trainer *t, float recall, float
   MK(cudaMemcpy2DAsync(xs.p, NI * 2, t->x, (size_t)stride * NI * 2, NI * 2, (size_t)ns, cudaMemcpyDeviceToDevice,
                        t->st));
   MK(cudaMemcpy2DAsync(ys.p, 1, t->y, (size_t)stride, 1, (size_t)ns, cudaMemcpyDeviceToDevice, t->st));
-  const int grid = (int)std::min<long long>((ns + 127) / 128, 4096);
-  k_mlp_logits<<<grid, 128, NP * 4, t->st>>>(t->pb, xs.p, ns, lg.p);
-  MK(cudaGetLastError());
+  DBuf<int> derr;
+  MK(derr.alloc(1));
+  MK(cudaMemsetAsync(derr.p, 0, 4, t->st));
+  int sms = 0;
+  MK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
+  MK(mlp_logits(t->pb, xs.p, ns, lg.p, derr.p, sms, t->st));
+  int herr = 0;
+  MK(cudaMemcpyAsync(&herr, derr.p, 4, cudaMemcpyDeviceToHost, t->st));
   std::vector<float> hl((size_t)ns);
   std::vector<uint8_t> hy((size_t)ns);
   MK(cudaMemcpyAsync(hl.data(), lg.p, (size_t)ns * 4, cudaMemcpyDeviceToHost, t->st));
   MK(cudaMemcpyAsync(hy.data(), ys.p, (size_t)ns, cudaMemcpyDeviceToHost, t->st));
   MK(cudaStreamSynchronize(t->st));
+  if (herr) return PDFS_ERR_TIMEOUT;
   std::vector<float> pos;
   for (long long i = 0; i < ns; ++i)
     if (hy[i]) pos.push_back(hl[i]);
@@ -860,9 +1043,16 @@ extern "C" int pdfs_mlp_infer(const float *blob, const uint16_t *x, int n, float
   MK(cudaMemcpy(dp.p, blob, NP * 4, cudaMemcpyHostToDevice));
   MK(cudaMemcpy(dx.p, x, (size_t)n * NI * 2, cudaMemcpyHostToDevice));
   k_to_bf16<<<(NP + 255) / 256, 256>>>(dp.p, dpb.p, NP);
-  const int grid = std::min((n + 127) / 128, 4096);
-  k_mlp_logits<<<grid, 128, NP * 4>>>(dpb.p, dx.p, n, dl.p);
-  MK(cudaGetLastError());
+  DBuf<int> derr;
+  MK(derr.alloc(1));
+  MK(cudaMemset(derr.p, 0, 4));
+  int dev = 0, sms = 0;
+  MK(cudaGetDevice(&dev));
+  MK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MK(mlp_logits(dpb.p, dx.p, n, dl.p, derr.p, sms, 0));
+  int herr = 0;
+  MK(cudaMemcpy(&herr, derr.p, 4, cudaMemcpyDeviceToHost));
+  if (herr) return PDFS_ERR_TIMEOUT;
   MK(cudaMemcpy(logits, dl.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
   return PDFS_OK;
 }

@@ -599,7 +599,10 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     const float thr = (float)tol;
     // per-block changes: ring slot cur = this sweep, (cur - k) mod kRing = k sweeps ago
     int cur = 0;
-    if (sched) CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * kRing * 4, c->st));
+    if (sched) {
+      CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * kRing * 4, c->st));
+      CK(cudaMemsetAsync(&c->dstat->sched_err, 0, 4, c->st));
+    }
     bool need_full = true;
     int s = 0;
     for (;;) {
@@ -621,7 +624,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
                        c->nby, c->nbz, c->bmin, c->st));
           CK(sched_learned(c->mlp_w, c->mlp_thr, c->bchg, cur, std::min(s, kHist), c->bmin, c->nbx, c->nby,
                            c->nbz, sn, s, f32 ? 0 : 1, thr, (float)std::min(g.dx, std::min(g.dy, g.dz)), c->bact,
-                           &c->dstat->active_blocks, c->sms, c->st));
+                           &c->dstat->active_blocks, &c->dstat->sched_err, c->sms, c->st));
           c->launches += 2;
         } else {
           CK(sched_change(c->bchg, cur, std::min(s, kHist), thr, c->bact, c->nbx, c->nby, c->nbz,
@@ -636,6 +639,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
       if (!full) {
         nact = c->hstat->active_blocks;
         st.ms_sched += ms_between(c->q0, c->q1);
+        if (c->hstat->sched_err) return PDFS_ERR_TIMEOUT;
       }
       if (verbose(o))
         fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e active=%lld/%lld\n", which, s, sn,

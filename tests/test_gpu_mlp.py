@@ -1,7 +1,7 @@
 """The learned scheduler's GPU kernels against the CPU oracle
 (oracle/mlp_oracle.py), through the C ABI: the bf16 forward/backward
-gradient, the Adam step and the fused inference arithmetic; then the
-trainer on real sweep traces."""
+gradient, the Adam step and the tensor-core (tcgen05) inference; then the
+trainer on real sweep traces and the ablation against the plain sweeps."""
 import numpy as np
 import pytest
 
@@ -118,8 +118,8 @@ def test_learned_scheduler_gain():
     base = res["none"][0]
     for name in ("change", "learned"):
         # tolerance: a different visiting order reaches the FP64 fixed point to rounding
-        assert np.max(np.abs(res[name][0] - base)[1:-1, 1:-1, 1:-1] /
-                      np.maximum(np.abs(base[1:-1, 1:-1, 1:-1]), 1.0)) <= 1e-13
+        got, ref = res[name][0][1:-1, 1:-1, 1:-1], base[1:-1, 1:-1, 1:-1]
+        assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) <= 1e-13
     upd = {k: v[1]["voxel_updates"] for k, v in res.items()}
     assert upd["learned"] <= 0.7 * upd["none"]
     assert upd["learned"] <= 1.10 * upd["change"]
