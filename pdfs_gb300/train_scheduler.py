@@ -12,6 +12,10 @@ by the library's own bf16 forward / backward / Adam kernels; the decision
 threshold keeps `recall` of the positive samples.
 
     python -m pdfs_gb300.train_scheduler [--grids 64] [--size 256] [--out PATH]
+
+`--infer-rows N` instead runs the inference entry point (pdfs_mlp_infer) twice
+on N seeded random feature rows and prints the wall time of the second call,
+host copies included; it is the workload of the inference kernel's profile.
 """
 from __future__ import annotations
 
@@ -80,6 +84,22 @@ def write_header(blob, info, path):
         f.write(f"static const float kDefaultMlpBlob[PDFS_MLP_BLOB] = {{\n  {vals}}};\n")
 
 
+def infer_rows(n, seed=0):
+    """Two pdfs_mlp_infer calls on n random bf16 feature rows; wall seconds of the second."""
+    rng = np.random.default_rng(seed)
+
+    def bits(a):  # bf16 bit patterns by truncation: any bf16 values do for timing
+        return (np.ascontiguousarray(a, dtype=np.float32).view(np.uint32) >> 16).astype(np.uint16)
+
+    w = (bits(rng.normal(0.0, 0.25, L.MLP_PARAMS)).astype(np.uint32) << 16).view(np.float32)
+    blob = np.concatenate([w, np.zeros(1, np.float32)])
+    x = bits(rng.uniform(-2.0, 2.0, (n, L.MLP_IN)))
+    api.mlp_infer(blob, x)
+    t0 = time.perf_counter()
+    api.mlp_infer(blob, x)
+    return time.perf_counter() - t0
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--grids", type=int, default=64)
@@ -88,7 +108,12 @@ def main():
     p.add_argument("--recall", type=float, default=0.9999)
     p.add_argument("--seed", type=int, default=7)
     p.add_argument("--out", default=os.path.join(HERE, "csrc", "mlp_default.h"))
+    p.add_argument("--infer-rows", type=int, default=0)
     a = p.parse_args()
+    if a.infer_rows:
+        dt = infer_rows(a.infer_rows)
+        print(f"pdfs_mlp_infer: {a.infer_rows} rows in {dt * 1e3:.2f} ms (host copies included)")
+        return
     B.build()
     blob, info = train(a.grids, a.size, a.epochs, a.recall, a.seed)
     assert blob.size == L.MLP_BLOB
