@@ -165,16 +165,43 @@ def peaks():
         return {}
 
 
-def traffic_per_launch(kind, prec, nodes):
+# sweep kernel variants by tile id: columns (TY, rows per warp) or bricks (BZ)
+COLUMNS32 = {1: (8, 2), 2: (8, 4), 3: (16, 4), 4: (8, 1), 5: (4, 2), 6: (6, 1), 7: (10, 1)}
+COLUMNS64 = {1: (4, 1), 2: (4, 2), 3: (8, 2), 4: (6, 1)}
+BRICKS32 = {8: 16, 9: 32}
+BRICKS64 = {5: 16}
+
+
+def is_brick(kind, tile):
+    return (tile & 0xff) in BRICKS32 if kind == "fp32" else (tile >> 8) in BRICKS64
+
+
+def kernel_name(kind, tile, prec, arith):
+    """The dominant sweep kernel's template name, as ncu lists it."""
+    from pdfs_gb300 import _lib as L
+    mode = "MIN" if kind == "fp32" or prec != L.PREC_FP32_POLISH64 else "REPLACE"
+    ar = "FAST" if kind == "fp32" else {L.ARITH_MIXED: "MIXED", L.ARITH_FAST: "FAST"}.get(arith, "REF")
+    t = "float" if kind == "fp32" else "double"
+    if is_brick(kind, tile):
+        bz = BRICKS32[tile & 0xff] if kind == "fp32" else BRICKS64[tile >> 8]
+        return "t3_sweep_kernel<%s, %d, %s, %s>" % (t, bz, mode, ar)
+    ty = COLUMNS32.get(tile & 0xff, (0, 0)) if kind == "fp32" else COLUMNS64.get(tile >> 8, (0, 0))
+    return "ws_sweep_kernel<%s, %d, %d, %s, %s>" % ((t,) + ty + (mode, ar))
+
+
+def traffic_per_launch(kind, prec, nodes, tile):
     """DRAM bytes of one launch of the dominant sweep kernel: the per-update
     traffic an ncu capture measured (profiles/traffic.json, dram__bytes_read
     + dram__bytes_write over the capture's voxel updates) times this
     launch's updates; None without a capture for that kernel."""
+    from pdfs_gb300 import _lib as L
     try:
         t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     except (OSError, ValueError):
         return None
-    key = "fp32" if kind == "fp32" else ("fp64_replace" if prec == 2 else "fp64_min")
+    key = "fp32" if kind == "fp32" else ("fp64_replace" if prec == L.PREC_FP32_POLISH64 else "fp64_min")
+    if is_brick(kind, tile):
+        key += "_brick"
     e = t.get(key)
     return None if not e else float(e["dram_bytes_per_update"]) * nodes
 
@@ -440,13 +467,9 @@ def main():
         per_launch = w.interior * (16 + 8 + mask_b) if prec == L.PREC_FP32_POLISH64 else w.interior * (16 + mask_b)
         dur = k64 / max(s64, 1)
     achieved = per_launch / (dur / 1e3) / 1e9 if dur > 0 else 0.0
-    ty32 = {1: (8, 2), 2: (8, 4), 3: (16, 4), 4: (8, 1), 5: (4, 2), 6: (6, 1)}.get(st["tile"] & 0xff, (0, 0))
-    ty64 = {1: (4, 1), 2: (4, 2), 3: (8, 2), 4: (6, 1)}.get(st["tile"] >> 8, (0, 0))
-    kname = "ws_sweep_kernel<float, %d, %d, MIN, FAST>" % ty32 if dominant == "fp32" else \
-        "ws_sweep_kernel<double, %d, %d, %s, %s>" % (ty64 + ("REPLACE" if prec == L.PREC_FP32_POLISH64 else "MIN",
-                                                     {L.ARITH_MIXED: "MIXED", L.ARITH_FAST: "FAST"}.get(arith, "REF")))
+    kname = kernel_name(dominant, st["tile"], prec, arith)
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": traffic_per_launch(dominant, prec, w.interior), "kernel": kname,
+            "traffic": traffic_per_launch(dominant, prec, w.interior, st["tile"]), "kernel": kname,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s",
             "bytes_per_update": per_launch / w.interior}
     fp32_roof = None

@@ -61,7 +61,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
                        "--expt-relaxed-constexpr"]
     # the sweep kernels' FP32 arithmetic uses approximate sqrt/divide (the
     # FP64 polish removes the difference); FP64 arithmetic is unaffected
-    per_tu = {"sweep.cu": ["-prec-sqrt=false", "-prec-div=false"]}
+    fast = ["-prec-sqrt=false", "-prec-div=false"]
+    per_tu = {"sweep.cu": fast, "tile3d.cu": fast}
     for src in cu:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
         objs.append(obj)

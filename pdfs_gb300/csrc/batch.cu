@@ -257,6 +257,14 @@ extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fi
     pdfs_default_opts(&o);
   if (o.fixed_sweeps != 0) return PDFS_ERR_INVALID;  // the batch runs whole rounds to convergence
   o.scheduler = PDFS_SCHED_NONE;
+  {
+    // a batched launch runs the column kernels (one ticket space across the
+    // grids); brick tiles and the default choice map to the column defaults
+    int t32 = o.tile & 0xff, t64 = (o.tile >> 8) & 0xff;
+    if (t32 == 0 || tile32(t32).bz) t32 = 4;
+    if (t64 == 0 || tile64(t64).bz) t64 = o.arith == PDFS_ARITH_MIXED ? 4 : 1;
+    o.tile = t32 | (t64 << 8);
+  }
   std::vector<pdfs_ctx *> ctx(n, nullptr);
   std::vector<pdfs_stats> st(n);
   std::memset(st.data(), 0, sizeof(pdfs_stats) * n);
@@ -398,6 +406,7 @@ extern "C" int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o_in, int *til
   else
     for (int t = 1; t <= (o.precision == PDFS_PREC_FP32_POLISH64 ? 2 : 3); ++t) c64.push_back(t);
   if (o.arith == PDFS_ARITH_FAST) c64.push_back(4);
+  c64.push_back(5);  // bricks: every arithmetic
   for (int t : c64) {
     double ms = 0;
     if (time_tile(PDFS_PREC_FP64, t, &ms) == PDFS_OK && ms < b) {

@@ -37,9 +37,11 @@ struct MaskLayout {
 };
 MaskLayout make_mask_layout(const pdfs_grid &g);
 
-// A sweep kernel variant: element type, tile, chunk depth.
+// A sweep kernel variant: a column tile (tx x ty, c rows per compute warp,
+// bz = 0) or a brick (tx x ty x bz, tile3d.cuh).
 struct TileShape {
   int tx, ty, c;
+  int bz = 0;
 };
 // Tile ids (1-based) for FP32 and FP64 kernels.
 int tile_count32();
@@ -52,6 +54,14 @@ TileShape tile64(int id);
 // (cap = upper bound field in the same layout).
 cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
                          const void *cap, int sms, cudaStream_t st, int *grid_used);
+// One sweep by the brick kernel (tile3d.cu): bricks of 16 x 16 x bz, a.tflag /
+// a.torder / a.ntx.. / a.epoch filled in.
+cudaError_t launch_sweep_bricks(int which, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
+                                cudaStream_t st, int *grid_used);
+// Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
+std::vector<int> brick_order(int ntx, int nty, int ntz);
+cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by,
+                             int bz);
 
 // Change-based active set: blocks that changed by more than thr in any of
 // the last hist sweeps, or whose face neighbour did in the last one (ring as
@@ -116,6 +126,10 @@ struct pdfs_ctx {
   void *stage = nullptr;    // reference-layout staging buffer for host transfers
   size_t stage_bytes = 0;
   int *order32 = nullptr, *order64 = nullptr, *progress = nullptr, *ticket = nullptr;
+  // brick tiles (tile3d.cuh): per-brick completion epochs, ticket orders, brick grids
+  int *tflag = nullptr, *tord32 = nullptr, *tord64 = nullptr;
+  int nt32[3] = {0, 0, 0}, nt64[3] = {0, 0, 0};
+  int epoch = 0;  // flag value of the last brick sweep
   void *mailbox = nullptr;  // x- and y-face mailboxes of every column
   size_t mailbox_bytes = 0;
   size_t progress_ints = 0;

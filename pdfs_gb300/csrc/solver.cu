@@ -221,9 +221,10 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   const int t32 = o->tile & 0xff, t64 = (o->tile >> 8) & 0xff;
   if (t32 > tile_count32() || t64 > tile_count64()) return PDFS_ERR_INVALID;
   // FP64 kernels: tiles 1 and 4 for the mixed arithmetic; 1-3 for the
-  // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4)
+  // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4);
+  // bricks (tile 5) for every arithmetic
   if (o->arith == PDFS_ARITH_MIXED) {
-    if (t64 != 0 && t64 != 1 && t64 != 4) return PDFS_ERR_INVALID;
+    if (t64 != 0 && t64 != 1 && t64 != 4 && t64 != 5) return PDFS_ERR_INVALID;
   } else {
     if (t64 == 4 && o->arith != PDFS_ARITH_FAST) return PDFS_ERR_INVALID;
     if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 == 3) return PDFS_ERR_INVALID;
@@ -232,18 +233,17 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   return PDFS_OK;
 }
 
-// Default tile choice (the autotuner in sched.cu may override through opts.tile).
-// FP32: 32 x 8 columns with one row per compute warp (8 compute warps; 7.9
-// ms per 768^3 sweep against 10.0 ms for two rows per warp: the sweep is
-// latency-bound and more resident warps hide more of it).
-// FP64: the mixed arithmetic is latency-bound like FP32 and takes 32 x 6
-// columns (tile 4: 15.9 ms per 768^3 polish sweep against 20.4 ms for 32 x 4);
-// the reference and fast arithmetic are bound by the FP64 pipe (55 ms on
-// either tile) and keep 32 x 4.
+// Default tile choice (pdfs_autotune may override through opts.tile).
+// FP32: 16 x 16 x 32 bricks (tile 9: 4.2 ms per 768^3 sweep against 7.9 ms
+// for the best column tile, 32 x 8 with one row per compute warp).
+// FP64: bricks (tile 5) for the mixed arithmetic (14.4 ms per 768^3 polish
+// sweep against 15.9 ms for 32 x 6 columns); the reference and fast
+// arithmetic are bound by the FP64 pipe and keep 32 x 4 columns unless
+// PDFS_BRICKS64 asks for bricks.
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
-  c->t32 = t32 ? t32 : 4;
-  c->t64 = t64 ? t64 : (c->o.arith == PDFS_ARITH_MIXED ? 4 : 1);
+  c->t32 = t32 ? t32 : 9;
+  c->t64 = t64 ? t64 : ((c->o.arith == PDFS_ARITH_MIXED || getenv("PDFS_BRICKS64")) ? 5 : 1);
 }
 
 extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_ctx **out) {
@@ -326,6 +326,27 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
       return fail(e);
   }
   {
+    // brick tiles: ticket orders and the completion flags (epoch 0 = never)
+    size_t nflags = 0;
+    for (int k = 0; k < 2; ++k) {
+      const TileShape ts = k ? s64 : s32;
+      if (ts.bz == 0) continue;
+      int *nt = k ? c->nt64 : c->nt32;
+      nt[0] = (g->nx + ts.tx - 1) / ts.tx;
+      nt[1] = (g->ny + ts.ty - 1) / ts.ty;
+      nt[2] = (g->nz + ts.bz - 1) / ts.bz;
+      std::vector<int> bo = brick_order(nt[0], nt[1], nt[2]);
+      int **dst = k ? &c->tord64 : &c->tord32;
+      if ((e = cudaMalloc(dst, bo.size() * 4)) != cudaSuccess) return fail(e);
+      if ((e = cudaMemcpy(*dst, bo.data(), bo.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+      nflags = std::max(nflags, bo.size());
+    }
+    if (nflags) {
+      if ((e = cudaMalloc(&c->tflag, nflags * 4)) != cudaSuccess) return fail(e);
+      if ((e = cudaMemset(c->tflag, 0, nflags * 4)) != cudaSuccess) return fail(e);
+    }
+  }
+  {
     std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
                      w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
     if ((e = cudaMalloc(&c->order32, w32.size() * 4)) != cudaSuccess) return fail(e);
@@ -360,6 +381,9 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   cudaFree(c->stage);
   cudaFree(c->order32);
   cudaFree(c->order64);
+  cudaFree(c->tflag);
+  cudaFree(c->tord32);
+  cudaFree(c->tord64);
   cudaFree(c->progress);
   cudaFree(c->mailbox);
   cudaFree(c->ticket);
@@ -486,6 +510,13 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   a.nby = c->nby;
   a.nbz = c->nbz;
   a.hmin = (float)std::min(g.dx, std::min(g.dy, g.dz));
+  const int *nt = f32 ? c->nt32 : c->nt64;
+  a.tflag = c->tflag;
+  a.torder = f32 ? c->tord32 : c->tord64;
+  a.ntx = nt[0];
+  a.nty = nt[1];
+  a.ntz = nt[2];
+  a.epoch = c->epoch;
   long long wait_ms = c->o.spin_limit > 0 ? c->o.spin_limit : 4000;
   if (getenv("PDFS_WAIT_MS")) wait_ms = atoll(getenv("PDFS_WAIT_MS"));
   a.wait_cycles = wait_ms * 1000000LL * 21 / 10;  // at most 2.07 GHz: never shorter than wait_ms
@@ -519,15 +550,22 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   fill_sweep_args(c, which, sn, active, blk_chg, &a);
   const bool iso = g.dx == g.dy && g.dy == g.dz;
 
-  CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
+  const int tile = f32 ? c->t32 : c->t64;
+  const TileShape ts = f32 ? tile32(tile) : tile64(tile);
+  if (ts.bz == 0) CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
   if (blk_chg) CK(cudaMemsetAsync(blk_chg, 0, (size_t)c->nblocks * 4, c->st));
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
   const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : (c->o.arith == PDFS_ARITH_MIXED ? ARITH_MIXED : ARITH_FAST);
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
-  CK(launch_sweep(which, f32 ? c->t32 : c->t64, arith, iso, a, L, which == 2 ? (const void *)c->in64 : nullptr,
-                  c->sms, c->st, &grid));
+  if (ts.bz > 0) {
+    a.epoch = ++c->epoch;  // the flags of every earlier sweep are below it
+    CK(launch_sweep_bricks(which, ts.bz, arith, iso, a, L, c->sms, c->st, &grid));
+  } else {
+    CK(launch_sweep(which, tile, arith, iso, a, L, which == 2 ? (const void *)c->in64 : nullptr, c->sms, c->st,
+                    &grid));
+  }
   CK(cudaEventRecord(c->k1, c->st));
   CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));

@@ -8,11 +8,13 @@
 
 namespace pdfs {
 
-// Tile variants: columns are 32 nodes wide (one warp lane per x); TY rows,
-// R rows per compute warp.  {tx, ty, rows per warp}
-static const TileShape kT32[] = {{32, 8, 2}, {32, 8, 4}, {32, 16, 4}, {32, 8, 1}, {32, 4, 2}, {32, 6, 1}, {32, 10, 1}};
+// Tile variants.  Columns (sweep.cuh) are 32 nodes wide (one warp lane per
+// x); TY rows, R rows per compute warp: {tx, ty, rows per warp}.  Bricks
+// (tile3d.cuh) are 16 x 16 x BZ: {16, 16, 0, BZ}.
+static const TileShape kT32[] = {{32, 8, 2},  {32, 8, 4}, {32, 16, 4}, {32, 8, 1},      {32, 4, 2},
+                                 {32, 6, 1},  {32, 10, 1}, {16, 16, 0, 16}, {16, 16, 0, 32}};
 // tile 4 (32 x 6, one row per warp) exists for the fast and mixed arithmetic
-static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}, {32, 6, 1}};
+static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}, {32, 6, 1}, {16, 16, 0, 16}};
 
 int tile_count32() { return (int)(sizeof(kT32) / sizeof(kT32[0])); }
 int tile_count64() { return (int)(sizeof(kT64) / sizeof(kT64[0])); }
@@ -32,13 +34,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D tiled map over an internal-layout field: dims {px, ry, nz+2}, box {bx, by, 1}.
-cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by) {
+// 3-D tiled map over an internal-layout field: dims {px, ry, nz+2}, box {bx, by, bz}.
+cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by,
+                             int bz) {
   auto fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
   cuuint64_t dims[3] = {(cuuint64_t)L.px, (cuuint64_t)L.ry, (cuuint64_t)nplanes};
   cuuint64_t strides[2] = {(cuuint64_t)L.px * esize, (cuuint64_t)L.plane * esize};
-  cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+  cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
   cuuint32_t es[3] = {1, 1, 1};
   CUresult r = fn(m, esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims,
                   strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -65,7 +68,7 @@ static cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty) {
 template <class T, int TY, int R, int MODE>
 static cudaError_t encode_maps(const SweepArgs &a, const Layout &L, const void *cap, CUtensorMap m[3]) {
   using G = WsGeo<T, TY, R, MODE>;
-  cudaError_t e = encode_field_map(&m[0], a.u, sizeof(T), L, a.nz + 2, G::W, G::R);
+  cudaError_t e = encode_field_map(&m[0], a.u, sizeof(T), L, a.nz + 2, G::W, G::R, 1);
   if (e != cudaSuccess) return e;
   (void)cap;  // the polish cap is read through a.cap, not a map
   m[1] = m[0];

@@ -83,6 +83,11 @@ struct SweepArgs {
   GodConst32 k32;
   const struct BatchDesc *batch;  // many grids in one launch (nullptr = this grid only)
   const void *cap;        // replace-update: per-node upper bound (the input), field layout
+  // 3-D brick sweep (tile3d.cuh)
+  int *tflag;             // per brick: epoch of the last sweep that completed it
+  const int *torder;      // ticket -> local brick id in sweep order, wavefront order
+  int ntx, nty, ntz;      // brick grid
+  int epoch;              // this sweep's flag value (increases every launch)
 };
 
 // A batched sweep: tickets enumerate (grid, local column) pairs, each grid's

@@ -1,0 +1,73 @@
+// tile3d.cu -- instantiations and launcher of the brick sweep kernel (tile3d.cuh).
+#include <algorithm>
+
+#include "internal.h"
+#include "tile3d.cuh"
+
+namespace pdfs {
+
+std::vector<int> brick_order(int ntx, int nty, int ntz) {
+  std::vector<int> o((size_t)ntx * nty * ntz);
+  for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
+  // a brick waits for one brick a level below in each axis: ordering by level
+  // lists all three first, which is all the deadlock argument needs
+  std::stable_sort(o.begin(), o.end(), [&](int a, int b) {
+    const int la = a % ntx + (a / ntx) % nty + a / (ntx * nty);
+    const int lb = b % ntx + (b / ntx) % nty + b / (ntx * nty);
+    return la < lb;
+  });
+  return o;
+}
+
+template <class T, int BZ, int MODE, int ARITH, bool ISO>
+static cudaError_t launch_t3(const SweepArgs &a, const Layout &L, int sms, cudaStream_t st, int *grid_used) {
+  using G = T3Geo<T, BZ>;
+  auto kern = t3_sweep_kernel<T, BZ, MODE, ARITH, ISO>;
+  CUtensorMap m;
+  cudaError_t e = encode_field_map(&m, a.u, sizeof(T), L, a.nz + 2, G::W, G::RY, G::RZ);
+  if (e != cudaSuccess) return e;
+  const size_t smem = G::BYTES;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, G::NT, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int ntile = a.ntx * a.nty * a.ntz;
+  int grid = std::min(per_sm * sms, ntile);
+  if (grid < 1) grid = 1;
+  kern<<<grid, G::NT, smem, st>>>(m, a);
+  if (grid_used) *grid_used = grid;
+  return cudaGetLastError();
+}
+
+template <int BZ>
+static cudaError_t dispatch_t3(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
+                               cudaStream_t st, int *g) {
+  if (which == 0)
+    return iso ? launch_t3<float, BZ, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)
+               : launch_t3<float, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
+  if constexpr (BZ == 16) {
+    if (which == 1) {
+      if (arith == ARITH_REF) return launch_t3<double, BZ, MODE_MIN, ARITH_REF, false>(a, L, sms, st, g);
+      if (arith == ARITH_FAST) return launch_t3<double, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
+      return iso ? launch_t3<double, BZ, MODE_MIN, ARITH_MIXED, true>(a, L, sms, st, g)
+                 : launch_t3<double, BZ, MODE_MIN, ARITH_MIXED, false>(a, L, sms, st, g);
+    }
+    if (arith == ARITH_REF) return launch_t3<double, BZ, MODE_REPLACE, ARITH_REF, false>(a, L, sms, st, g);
+    if (arith == ARITH_FAST) return launch_t3<double, BZ, MODE_REPLACE, ARITH_FAST, false>(a, L, sms, st, g);
+    return iso ? launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, true>(a, L, sms, st, g)
+               : launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, false>(a, L, sms, st, g);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_sweep_bricks(int which, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
+                                cudaStream_t st, int *g) {
+  if (!a.tflag || !a.torder || a.ntx < 1 || a.nty < 1 || a.ntz < 1) return cudaErrorInvalidValue;
+  if (bz == 16) return dispatch_t3<16>(which, arith, iso, a, L, sms, st, g);
+  if (bz == 32) return dispatch_t3<32>(which, arith, iso, a, L, sms, st, g);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace pdfs

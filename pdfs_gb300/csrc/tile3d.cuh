@@ -1,0 +1,343 @@
+// tile3d.cuh -- the 3-D tile sweep: each CTA sweeps a 16 x 16 x BZ brick of
+// the grid held whole in shared memory, hyperplane by hyperplane.
+//
+// The reference sweeps one hyperplane x+y+z = level of the whole grid per
+// kernel launch (single_gpu_cuda/src/phi3D_fsm.cu:161-185,
+// mpi_openacc/src/phi3D_fsm.c:92-117).  Any topological order of an
+// ordering's dependency DAG gives the same result (each node reads the new
+// values of its three upwind neighbours and the old values of its three
+// downwind ones), so this kernel cuts the grid into bricks and orders them
+// twice over:
+//   * inside a brick, level by level: thread (lx, ly) -- brick-local
+//     coordinates in sweep order -- updates node (lx, ly, L - lx - ly) at
+//     level L, and a CTA barrier separates levels.  A level reads the
+//     previous level's results and the next level's old values straight from
+//     the shared-memory copy of the brick;
+//   * across bricks, by per-brick completion flags in global memory: a brick
+//     starts its levels once its (at most three) upwind bricks have published
+//     this sweep's epoch, and publishes its own after its stores are visible.
+//     Persistent CTAs take bricks by ticket in wavefront order (every upwind
+//     brick holds a smaller ticket), so the wait always ends.
+//
+// A brick's old values do not depend on its upwind bricks, so its whole box
+// (the brick and a one-node halo, rounded out to 16-byte rows) is requested
+// by one TMA copy as soon as the ticket is taken; only the upwind halo faces
+// are read again, from L2, after the flags.  Updated nodes are stored to
+// global memory as they are computed (unchanged nodes are not written).
+//
+// Against the column kernel (sweep.cuh) this trades the cross-column
+// mailboxes, the plane ring and the per-step warp hand-offs for one barrier
+// per level and a 1.5-2x halo read, and it keeps a brick's every level in
+// one CTA's shared memory.
+//
+// Every wait is bounded (SweepArgs::wait_cycles): on expiry the kernel
+// records DEV_ERR_TIMEOUT, raises the abort flag, lets its own TMA copy land
+// and returns.
+#pragma once
+#include "sweep.cuh"
+
+namespace pdfs {
+
+template <class T, int BZ>
+struct T3Geo {
+  static constexpr int BX = 16, BY = 16;
+  static constexpr int V = 16 / (int)sizeof(T);
+  static constexpr int W = BX + 2 * V;    // box row: x0-V .. x0+BX+V-1 (16-byte aligned start)
+  static constexpr int RY = BY + 2;       // box rows: y0-1 .. y0+BY
+  static constexpr int RZ = BZ + 2;       // box planes: z0-1 .. z0+BZ
+  static constexpr int PL = RY * W;       // plane stride in shared memory
+  static constexpr int NL = BX + BY + BZ - 2;  // levels of one brick
+  static constexpr int NT = BX * BY;      // one thread per (x, y) of the brick
+  static constexpr int NZB = BZ / 8;      // 8^3 scheduler blocks per brick column
+  static constexpr int CP = 4;            // replace-update: caps prefetched ahead (registers)
+  static constexpr unsigned BOX_BYTES = (unsigned)(W * RY * RZ * sizeof(T));
+  static constexpr size_t OFF_MASK = ((size_t)BOX_BYTES + 127) & ~size_t(127);
+  static constexpr size_t OFF_BAR = OFF_MASK + (size_t)BZ * BY * 4;
+  static constexpr size_t BYTES = OFF_BAR + 16;
+  static_assert(BZ % 8 == 0, "bricks hold whole 8^3 blocks in z");
+  static_assert((W * sizeof(T)) % 16 == 0, "TMA rows are 16-byte multiples");
+};
+
+__device__ __forceinline__ void st_release_gpu(int *p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+template <class T, int BZ, int MODE, int ARITH, bool ISO>
+__global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
+                                                       const __grid_constant__ SweepArgs a) {
+  using G = T3Geo<T, BZ>;
+  constexpr int BX = G::BX, BY = G::BY, V = G::V, W = G::W, PL = G::PL, NL = G::NL, NZB = G::NZB, CP = G::CP;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  T *box = reinterpret_cast<T *>(sm);
+  uint32_t *smask = reinterpret_cast<uint32_t *>(sm + G::OFF_MASK);  // [BZ][BY] frozen words of the brick
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + G::OFF_BAR);
+  __shared__ int s_next;
+  __shared__ volatile int s_abort;
+
+  if ((saddr(sm) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
+    if (threadIdx.x == 0) {
+      atomicCAS(a.err, 0, DEV_ERR_SMEM_ALIGN);
+      atomicExch(a.err + 1, 1);
+    }
+    return;
+  }
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int lx = tid & (BX - 1), ly = tid / BX;  // brick-local x, y in sweep order
+  const int sxd = a.sx, syd = a.sy, szd = a.sz;
+  const int gxl = sxd > 0 ? lx : BX - 1 - lx;    // brick-local x, y in grid order
+  const int gyl = syd > 0 ? ly : BY - 1 - ly;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int ntx = a.ntx, nty = a.nty, ntz = a.ntz;
+  const int ntile = ntx * nty * ntz;
+  const long long plane = a.plane, px = a.px;
+  const float hmin = a.hmin;
+  const GodConst64 k64 = a.k64;
+  const GodConst32 k32 = a.k32;
+  const uint8_t *__restrict__ blk_active = a.blk_active;
+  unsigned int *__restrict__ blk_chg = a.blk_chg;
+  const bool masked = a.fmask != nullptr;
+  T *__restrict__ u = reinterpret_cast<T *>(a.u);
+  const T *__restrict__ capg = reinterpret_cast<const T *>(a.cap);
+  const int epoch = a.epoch;
+  T tmax = T(0);
+
+  if (tid == 0) {
+    s_abort = 0;
+    mbar_init(bar, 1);
+    mbar_fence_init();
+    s_next = atomicAdd(a.ticket, 1);
+  }
+  __syncthreads();
+  unsigned par = 0;  // phase parity of the box barrier
+  for (;;) {
+    const int tk = s_next;
+    // a uniform decision (s_abort may change under the reads); the barrier
+    // also orders every read of s_next before its next write
+    if (__syncthreads_or(tk >= ntile || s_abort)) break;
+    const int lt = a.torder[tk];  // local brick id in sweep order: (lk * nty + lj) * ntx + li
+    const int li = lt % ntx, lj = (lt / ntx) % nty, lk = lt / (ntx * nty);
+    const int bi = sxd > 0 ? li : ntx - 1 - li;
+    const int bj = syd > 0 ? lj : nty - 1 - lj;
+    const int bk = szd > 0 ? lk : ntz - 1 - lk;
+    const int tile = (bk * nty + bj) * ntx + bi;
+    const int x0 = 1 + bi * BX, y0 = 1 + bj * BY, z0 = 1 + bk * BZ;
+
+    // block mask: a brick none of whose 8^3 blocks is active keeps its values
+    // and publishes at once (its faces are the old values its neighbours need)
+    bool run = true;
+    if (blk_active) {
+      bool act = false;
+      if (tid < 4 * NZB) {
+        const int bx = 2 * bi + (tid & 1), by = 2 * bj + ((tid >> 1) & 1), bz = bk * NZB + (tid >> 2);
+        if (bx < a.nbx && by < a.nby && bz < a.nbz)
+          act = __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0;
+      }
+      run = __syncthreads_or(act) != 0;
+    }
+    if (tid == 32) s_next = atomicAdd(a.ticket, 1);  // the next brick's ticket, fetched ahead
+    if (!run) {
+      if (tid == 0 && tile != a.poison_col) st_release_gpu(a.tflag + tile, epoch);
+      __syncthreads();
+      continue;
+    }
+
+    // the box: TMA from (x0 - V, y0 - 1, z0 - 1); out-of-range rows and planes read 0 (never used)
+    fence_proxy_async();  // this CTA's generic accesses to the box come before the copy's writes
+    __syncthreads();
+    if (tid == 0) {
+      mbar_arrive_tx(bar, G::BOX_BYTES);
+      tma_load_3d(box, &tm_u, bi * BX, y0 - 1, z0 - 1, bar);
+    }
+    const bool vxy = (x0 + gxl <= nx) && (y0 + gyl <= ny);
+    const int zcnt = min(BZ, nz - z0 + 1);  // planes of the brick inside the grid
+    // frozen words of the brick's rows: node bit (x0 - 1 + gx) & 31
+    if (masked) {
+      for (int q = tid; q < BZ * BY; q += G::NT) {
+        const int p = q / BY, r = q % BY;
+        uint32_t w = 0;
+        if (p < zcnt && y0 + r <= ny)
+          w = __ldg(a.fmask + (long long)(z0 + p) * (a.mask_fy * a.mask_fw) + (long long)(bi >> 1) * a.mask_fy +
+                    (y0 - 1 + r));
+        smask[q] = w;
+      }
+    }
+    const int mshift = 16 * (bi & 1) + gxl;
+    // active 8^3 blocks of my (x, y) column, one bit per z block of the brick
+    unsigned actz = (1u << NZB) - 1u;
+    if (blk_active && vxy) {
+      actz = 0;
+      const int bx = (x0 - 1 + gxl) >> 3, by = (y0 - 1 + gyl) >> 3;
+#pragma unroll
+      for (int q = 0; q < NZB; ++q) {
+        const int bz = bk * NZB + q;
+        if (bz < a.nbz && __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx)) actz |= 1u << q;
+      }
+    }
+    const long long gbase = (long long)z0 * plane + (long long)(y0 + gyl) * px + (x0 + gxl) + (V - 1);
+    // replace-update caps of my first CP nodes (sweep order)
+    T capq[CP];
+    auto cap_at = [&](int lz) -> T {
+      const int gz = szd > 0 ? lz : BZ - 1 - lz;
+      if (MODE != MODE_REPLACE || !vxy || lz >= BZ || gz >= zcnt) return T(0);
+      return __ldg(capg + gbase + (long long)gz * plane);
+    };
+#pragma unroll
+    for (int q = 0; q < CP; ++q) capq[q] = cap_at(q);
+
+    // wait for the upwind bricks (lanes 0..2 of warp 0, one each)
+    bool ok = true;
+    if (tid < 3) {
+      int up = -1;
+      if (tid == 0 && li > 0) up = tile - sxd;
+      if (tid == 1 && lj > 0) up = tile - syd * ntx;
+      if (tid == 2 && lk > 0) up = tile - szd * ntx * nty;
+      if (up >= 0 && ld_acquire_gpu(a.tflag + up) < epoch) {
+        const long long t0 = cycles();
+        unsigned nap = 32;
+        while (ld_acquire_gpu(a.tflag + up) < epoch) {
+          if (s_abort || *(volatile int *)(a.err + 1)) {
+            s_abort = 1;
+            ok = false;
+            break;
+          }
+          if (cycles() - t0 > a.wait_cycles) {
+            raise_timeout(a, tile, &s_abort);
+            ok = false;
+            break;
+          }
+          __nanosleep(nap);
+          nap = min(nap * 2, 256u);
+        }
+      }
+    }
+    ok = __syncthreads_and(ok) != 0;
+    // the box copy has landed (bounded wait; on abort it is still drained below)
+    bool landed = mbar_wait(bar, par, a, tile, &s_abort);
+    if (!__syncthreads_and(ok && landed)) {
+      if (!landed && tid == 0) {  // let the copy land before the CTA leaves
+        const long long t0 = cycles();
+        while (!mbar_try(bar, par) && cycles() - t0 < 4000000000ll) {
+        }
+      }
+      break;
+    }
+    par ^= 1u;
+    // upwind halo faces: this sweep's values, written by the upwind bricks (L2)
+    if (li > 0) {  // x face
+      const int xu = sxd > 0 ? x0 - 1 : x0 + BX;
+      const int sxo = sxd > 0 ? V - 1 : V + BX;
+      for (int q = tid; q < BZ * BY; q += G::NT) {
+        const int p = q / BY, r = q % BY;
+        if (p < zcnt && y0 + r <= ny)
+          box[(1 + p) * PL + (1 + r) * W + sxo] =
+              __ldcg(u + (long long)(z0 + p) * plane + (long long)(y0 + r) * px + xu + (V - 1));
+      }
+    }
+    if (lj > 0) {  // y face
+      const int yu = syd > 0 ? y0 - 1 : y0 + BY;
+      const int syo = syd > 0 ? 0 : BY + 1;
+      for (int q = tid; q < BZ * BX; q += G::NT) {
+        const int p = q / BX, xx = q % BX;
+        if (p < zcnt && x0 + xx <= nx)
+          box[(1 + p) * PL + syo * W + V + xx] =
+              __ldcg(u + (long long)(z0 + p) * plane + (long long)yu * px + x0 + xx + (V - 1));
+      }
+    }
+    if (lk > 0) {  // z face
+      const int zu = szd > 0 ? z0 - 1 : z0 + BZ;
+      const int szo = szd > 0 ? 0 : BZ + 1;
+      for (int q = tid; q < BY * BX; q += G::NT) {
+        const int r = q / BX, xx = q % BX;
+        if (y0 + r <= ny && x0 + xx <= nx)
+          box[szo * PL + (1 + r) * W + V + xx] =
+              __ldcg(u + (long long)zu * plane + (long long)(y0 + r) * px + x0 + xx + (V - 1));
+      }
+    }
+    __syncthreads();
+
+    // the levels: node (lx, ly, lz = L - lx - ly), sweep order
+    const int obase = (1 + gyl) * W + V + gxl + (szd > 0 ? PL : BZ * PL);  // lz = 0
+    const int dzo = szd > 0 ? PL : -PL;
+    T accb[NZB];
+#pragma unroll
+    for (int q = 0; q < NZB; ++q) accb[q] = T(0);
+    const int lxy = lx + ly;
+    for (int L = 0; L < NL; ++L) {
+      const int lz = L - lxy;
+      if ((unsigned)lz < (unsigned)BZ) {
+        const int gz = szd > 0 ? lz : BZ - 1 - lz;
+        if (vxy && gz < zcnt) {
+          const int o = obase + lz * dzo;
+          const T cv = box[o];
+          // the reference's minima keep grid orientation: min(u[x-1], u[x+1])
+          const T m0 = vmin<T, ARITH>(box[o - 1], box[o + 1]);
+          const T m1 = vmin<T, ARITH>(box[o - W], box[o + W]);
+          const T m2 = vmin<T, ARITH>(box[o - PL], box[o + PL]);
+          bool act = (actz >> (gz >> 3)) & 1u;
+          if (masked && act) act = !((smask[gz * BY + gyl] >> mshift) & 1u);
+          if (act) {
+            const T g = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
+            const T nv = MODE == MODE_REPLACE ? vmin<T, ARITH>(capq[0], g) : vmin<T, ARITH>(cv, g);
+            if (vdiffers<T, ARITH>(nv, cv)) {
+              box[o] = nv;
+              u[gbase + (long long)gz * plane] = nv;
+              T d;
+              if (sizeof(T) == 4)
+                d = (T)__fdividef(fabsf((float)cv - (float)nv), fmaxf((float)nv, hmin));
+              else
+                d = (T)fabs((double)cv - (double)nv);
+              tmax = vmax_nonneg<T, ARITH>(tmax, d);
+#pragma unroll
+              for (int q = 0; q < NZB; ++q)
+                if ((gz >> 3) == q) accb[q] = vmax_nonneg<T, ARITH>(accb[q], d);
+            }
+          }
+        }
+        if (MODE == MODE_REPLACE) {
+#pragma unroll
+          for (int q = 0; q + 1 < CP; ++q) capq[q] = capq[q + 1];
+          capq[CP - 1] = cap_at(lz + CP);
+        }
+      }
+      __syncthreads();
+    }
+    // per-block change: lanes of one warp with the same 8^3 block are lx in
+    // [0, 8) or [8, 16) of the warp's two rows
+    if (blk_chg) {
+#pragma unroll
+      for (int q = 0; q < NZB; ++q) {
+        T v = accb[q];
+#pragma unroll
+        for (int off = 1; off <= 16; off <<= 1) {
+          if (off == 8) continue;
+          const T w2 = __shfl_xor_sync(0xffffffffu, v, off);
+          v = vmax_nonneg<T, ARITH>(v, w2);
+        }
+        // only nodes inside the grid change, so v > 0 names a block of the grid
+        const int bz = bk * NZB + q;
+        if ((lane == 0 || lane == 8) && v > T(0) && bz < a.nbz) {
+          const int bx = (x0 - 1 + gxl) >> 3, by = (y0 - 1 + gyl) >> 3;
+          atomicMax(blk_chg + ((long long)bz * a.nby + by) * a.nbx + bx, __float_as_uint((float)v));
+        }
+      }
+    }
+    // publish: every store of the brick is visible before the flag
+    __threadfence();
+    __syncthreads();
+    if (tid == 0 && tile != a.poison_col) st_release_gpu(a.tflag + tile, epoch);
+  }
+  // the CTA's max change -> the grid's counter (one atomic per warp)
+  {
+    T v = tmax;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if (lane == 0 && v > T(0)) {
+      if (sizeof(T) == 4)
+        atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint((float)v));
+      else
+        atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg), (unsigned long long)__double_as_longlong((double)v));
+    }
+  }
+}
+
+}  // namespace pdfs

@@ -1,0 +1,179 @@
+"""The brick sweep kernel (16 x 16 x BZ bricks held in shared memory, swept
+level by level, ordered across bricks by completion flags) through the C
+ABI.  Its update order is another topological order of each ordering's
+dependency DAG, so FP64 reference arithmetic must match the oracle bit for
+bit, and every arithmetic must match the column kernels bit for bit; block
+masks must equal freezing the inactive blocks' nodes; a brick that never
+publishes must end in the bounded-wait error."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pdfs_gb300 import _lib as L
+from pdfs_gb300 import api
+from pdfs_gb300 import workloads as W
+from test_gpu_blocks import block_max, node_mask, patterned_mask
+
+pytestmark = pytest.mark.gpu
+
+B64 = 5 << 8     # FP64 bricks, 16 x 16 x 16
+B32 = (8, 9)     # FP32 bricks, 16 x 16 x 16 and 16 x 16 x 32
+
+
+def same(a, b):
+    return a.tobytes() == b.tobytes()
+
+
+def inner(a):
+    return a[1:-1, 1:-1, 1:-1]
+
+
+# ragged in every axis, bricks of one node, single rows, exact multiples
+SHAPES = [(1, 1, 1), (2, 3, 5), (16, 16, 16), (17, 16, 15), (1, 40, 1), (70, 1, 1), (1, 1, 33), (33, 17, 9),
+          (65, 31, 47), (48, 50, 35)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_bricks_bit_exact_odd_shapes(shape):
+    nx, ny, nz = shape
+    f = W.random_field(nx, ny, nz, seed=nx * 5 + ny * 11 + nz, frac_known=0.1)
+    for sp in [(1.0, 1.0, 1.0), (0.7, 1.3, 0.4)]:
+        a, b = f.copy(), f.copy()
+        s, _ = O.solve(b, sp, tol=0.0, threads=8)
+        st = api.solve(a, sp, tol=0.0, tile=B64)
+        assert same(a, b)
+        assert st["sweeps_fp64"] == s
+        assert st["tile"] >> 8 == 5
+
+
+@pytest.mark.parametrize("sn", range(1, 9))
+def test_brick_orderings_multisphere_frozen(sn):
+    """One sweep of each ordering on a frozen-mask multi-sphere grid whose
+    sizes are not brick multiples."""
+    w = W.random_spheres(75, 41, 38, 1.0, 1.0, 0.5, 6, 3.0, 12.0, seed=40 + sn)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    api.sweep(a, sp, sn, frozen=w.frozen, freeze=L.FREEZE_MASK, tile=B64)
+    O.sweep(b, sp, sn, frozen=w.frozen)
+    assert same(a, b)
+
+
+@pytest.fixture(scope="module", params=[37, 150])
+def grid(request):
+    return W.random_spheres(70, 45, request.param, 1.0, 1.0, 1.0, 5, 3.0, 12.0, seed=23)
+
+
+def ctx_for(w, **kw):
+    c = api.Context(w.nx, w.ny, w.nz, (w.dx, w.dy, w.dz), freeze=L.FREEZE_MASK, **kw)
+    c.load(w.field, w.frozen)
+    return c
+
+
+@pytest.mark.parametrize("sn", range(1, 9))
+def test_brick_masked_sweep_equals_frozen_fp64(grid, sn):
+    w = grid
+    rng = np.random.default_rng(500 + sn)
+    with ctx_for(w, precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, tile=B64) as c:
+        nb = c.blocks()[::-1]
+        act = patterned_mask(nb, rng)
+        bc = np.zeros(nb, np.float32)
+        ch = c.sweep(sn, act, bc)
+        got = np.empty_like(w.field)
+        c.store(got)
+    exp = w.field.copy()
+    O.sweep(exp, (w.dx, w.dy, w.dz), sn, frozen=w.frozen | node_mask(act, w.field.shape))
+    assert same(got, exp)
+    diff = np.abs(exp - w.field)
+    assert ch == float(inner(diff).max())
+    assert np.array_equal(bc, block_max(diff, nb))
+    assert not bc[act == 0].any()
+
+
+def test_brick_masked_chain_and_empty(grid):
+    """Eight masked orderings in a row on one context (the brick flags carry
+    increasing epochs across launches), then an all-inactive sweep."""
+    w = grid
+    rng = np.random.default_rng(9)
+    exp = w.field.copy()
+    with ctx_for(w, precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, tile=B64) as c:
+        nb = c.blocks()[::-1]
+        for sn in range(1, 9):
+            act = patterned_mask(nb, rng)
+            c.sweep(sn, act)
+            O.sweep(exp, (w.dx, w.dy, w.dz), sn, frozen=w.frozen | node_mask(act, w.field.shape))
+        assert c.sweep(3, np.zeros(nb, np.uint8)) == 0.0
+        got = np.empty_like(w.field)
+        c.store(got)
+    assert same(got, exp)
+
+
+@pytest.mark.parametrize("tile", B32)
+@pytest.mark.parametrize("sn", [1, 6])
+def test_brick_fp32_equals_column_fp32(grid, tile, sn):
+    """FP32 sweeps: the bricks and the 32 x 8 columns run the same local
+    solver on the same inputs, so results agree bit for bit, masked too."""
+    w = grid
+    outs = []
+    for t in (tile, 4):
+        with ctx_for(w, precision=L.PREC_FP32, tile=t) as c:
+            nb = c.blocks()[::-1]
+            act = patterned_mask(nb, np.random.default_rng(600 + sn))
+            for k in range(3):
+                c.sweep((sn + k - 1) % 8 + 1, act if k == 1 else None)
+            got = np.empty_like(w.field)
+            c.store(got)
+            outs.append(got)
+    assert same(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("iso", [True, False])
+def test_brick_mixed_polish_equals_column(iso):
+    """FP32 bulk + mixed FP64 polish on bricks against the column kernels
+    (bit for bit) and against the FP64 oracle (1e-6 relative)."""
+    sz = 0.5 if not iso else 1.0
+    w = W.random_spheres(80, 66, 52, 1.0, 1.0, sz, 8, 3.0, 14.0, seed=77)
+    sp = (w.dx, w.dy, w.dz)
+    res = []
+    for tile in (8 | (5 << 8), 4 | (4 << 8)):
+        a = w.field.copy()
+        api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
+                  arith=L.ARITH_MIXED, tol=1e-6 * min(sp), max_sweeps=200, tile=tile)
+        res.append(a)
+    assert same(res[0], res[1])
+    b = w.field.copy()
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    h = min(sp)
+    err = float(np.max(np.abs(inner(res[0]) - inner(b)) / np.maximum(np.abs(inner(b)), h)))
+    assert err <= 1e-6, err
+
+
+@pytest.mark.parametrize("sched", [L.SCHED_CHANGE, L.SCHED_LEARNED])
+def test_brick_schedulers_same_fixed_point(sched):
+    """Scheduled solves skip inactive bricks; the fixed point is the plain one."""
+    w = W.random_spheres(96, 80, 72, 1.0, 1.0, 1.0, 6, 3.0, 16.0, seed=5)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, arith=L.ARITH_FAST, tol=0.0,
+                   scheduler=sched, tile=B64)
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    h = min(sp)
+    err = float(np.max(np.abs(inner(a) - inner(b)) / np.maximum(np.abs(inner(b)), h)))
+    assert err <= 1e-13, err
+    assert st["blocks_skipped"] > 0
+
+
+def test_brick_bounded_wait_times_out_cleanly(monkeypatch):
+    """A brick that never publishes (test hook) makes its downwind bricks give
+    up after the wait bound: PDFS_ERR_TIMEOUT, and the device stays usable."""
+    w = W.random_spheres(64, 64, 48, 1.0, 1.0, 1.0, 4, 3.0, 10.0, seed=2)
+    sp = (w.dx, w.dy, w.dz)
+    monkeypatch.setenv("PDFS_TEST_POISON_COLUMN", "0")
+    a = w.field.copy()
+    with pytest.raises(api.PdfsError) as ei:
+        api.solve(a, sp, tol=0.0, wait_ms=200, tile=B64)
+    assert ei.value.status == L.PDFS_ERR_TIMEOUT
+    monkeypatch.delenv("PDFS_TEST_POISON_COLUMN")
+    a, b = w.field.copy(), w.field.copy()
+    api.solve(a, sp, tol=0.0, tile=B64)
+    O.solve(b, sp, tol=0.0, threads=8)
+    assert same(a, b)
