@@ -44,8 +44,9 @@ def parse():
     p.add_argument("--mode", default="polish", choices=["polish", "fp32", "fp64", "fp64ref"])
     p.add_argument("--scheduler", default="none", choices=["none", "change", "learned"])
     p.add_argument("--tol", type=float, default=1e-5, help="FP64 polish tolerance (max change)")
-    p.add_argument("--polish-arith", default="mixed", choices=["mixed", "fast"],
-                   help="polish arithmetic: FP64 field with FP32 increments, or all FP64")
+    p.add_argument("--polish-arith", default="mixed", choices=["mixed", "pair", "fast"],
+                   help="polish arithmetic: FP32 increments over an FP64 field (mixed) or an FP32-pair "
+                        "field (pair), or all FP64 (fast)")
     p.add_argument("--no-sched-table", action="store_true", help="skip timing the three schedulers")
     p.add_argument("--configs", action="store_true",
                    help="accuracy report: every config's FP32 + polish solve against the plain FP64 FSM")
@@ -180,7 +181,8 @@ def kernel_name(kind, tile, prec, arith):
     """The dominant sweep kernel's template name, as ncu lists it."""
     from pdfs_gb300 import _lib as L
     mode = "MIN" if kind == "fp32" or prec != L.PREC_FP32_POLISH64 else "REPLACE"
-    ar = "FAST" if kind == "fp32" else {L.ARITH_MIXED: "MIXED", L.ARITH_FAST: "FAST"}.get(arith, "REF")
+    ar = "FAST" if kind == "fp32" else {L.ARITH_MIXED: "MIXED", L.ARITH_PAIR: "PAIR",
+                                        L.ARITH_FAST: "FAST"}.get(arith, "REF")
     t = "float" if kind == "fp32" else "double"
     if is_brick(kind, tile):
         bz = BRICKS32[tile & 0xff] if kind == "fp32" else BRICKS64[tile >> 8]
@@ -265,7 +267,7 @@ def run_batch(args, rank, world, pg, device):
     ws = W.batch_c5()
     sps = [(w.dx, w.dy, w.dz) for w in ws]
     nodes = sum(w.interior for w in ws)
-    arith = L.ARITH_MIXED if args.polish_arith == "mixed" else L.ARITH_FAST
+    arith = {"mixed": L.ARITH_MIXED, "pair": L.ARITH_PAIR}.get(args.polish_arith, L.ARITH_FAST)
     kw = dict(freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=arith, tol=args.tol, device=device)
     for _ in range(max(1, args.warmup)):
         api.solve_batch([w.field.copy() for w in ws], sps, frozen=[w.frozen for w in ws], **kw)
@@ -386,8 +388,8 @@ def main():
     prec = {"polish": L.PREC_FP32_POLISH64, "fp32": L.PREC_FP32, "fp64": L.PREC_FP64,
             "fp64ref": L.PREC_FP64}[args.mode]
     arith = L.ARITH_REFERENCE if args.mode == "fp64ref" else L.ARITH_FAST
-    if args.mode == "polish" and args.polish_arith == "mixed":
-        arith = L.ARITH_MIXED
+    if args.mode == "polish" and args.polish_arith in ("mixed", "pair"):
+        arith = L.ARITH_MIXED if args.polish_arith == "mixed" else L.ARITH_PAIR
     sched = {"none": L.SCHED_NONE, "change": L.SCHED_CHANGE, "learned": L.SCHED_LEARNED}[args.scheduler]
     if args.mode in ("fp64", "fp64ref"):
         sched = L.SCHED_NONE

@@ -55,6 +55,11 @@ enum {
                                point, a few FP64 operations per update (tile 1 only).  The
                                increments' rounding keeps sweeps changing by ~1e-7 h: use
                                a tol of 1e-6 h or more                                    */
+  PDFS_ARITH_PAIR = 3,      /* as MIXED, with the field, minima and update held as FP32
+                               pairs hi + lo (48 significant bits, Knuth/Dekker error-free
+                               sums) instead of FP64: no FP64 instruction in the sweeps.
+                               FP64 bricks only (tile 5, the default); frozen nodes and
+                               the halo come back as the exact FP64 input.  Same tol rule */
 };
 
 /* Which nodes are updated. */

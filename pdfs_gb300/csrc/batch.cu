@@ -262,6 +262,8 @@ extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fi
     // grids); brick tiles and the default choice map to the column defaults
     int t32 = o.tile & 0xff, t64 = (o.tile >> 8) & 0xff;
     if (t32 == 0 || tile32(t32).bz) t32 = 4;
+    // FP32 pairs live on bricks only: the batch polishes in the mixed arithmetic
+    if (o.arith == PDFS_ARITH_PAIR) o.arith = PDFS_ARITH_MIXED;
     if (t64 == 0 || tile64(t64).bz) t64 = o.arith == PDFS_ARITH_MIXED ? 4 : 1;
     o.tile = t32 | (t64 << 8);
   }

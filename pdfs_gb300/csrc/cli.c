@@ -12,6 +12,7 @@
  *   --fast         shifted-form FP64 arithmetic instead of the reference's
  *   --mixed        FP64 field with FP32 increments (with --polish: the fast
  *                  polish; set --tol to at least 1e-6 of the spacing)
+ *   --pair         the same with an FP32-pair field (no FP64 instructions)
  *   --sched S      block scheduler: none, change or learned
  *   --device D     CUDA device
  * Exit status 0 on success, 1 on any error (message on stderr).
@@ -25,7 +26,7 @@
 static int usage(const char *argv0)
 {
   printf("Usage: %s <file.vti> <prefix> [--rounds N | --converge] [--tol T] [--fp32 | --polish] "
-         "[--fast | --mixed] [--sched none|change|learned] [--device D]\n",
+         "[--fast | --mixed | --pair] [--sched none|change|learned] [--device D]\n",
          argv0);
   return 1;
 }
@@ -54,6 +55,8 @@ int main(int argc, char *argv[])
       o.arith = PDFS_ARITH_FAST;
     } else if (!strcmp(argv[i], "--mixed")) {
       o.arith = PDFS_ARITH_MIXED;
+    } else if (!strcmp(argv[i], "--pair")) {
+      o.arith = PDFS_ARITH_PAIR;
     } else if (!strcmp(argv[i], "--sched") && i + 1 < argc) {
       const char *v = argv[++i];
       if (!strcmp(v, "none"))

@@ -6,7 +6,7 @@
 // found by sorting the minima and trying 1, 2 then 3 active terms
 // (mpi_openacc/src/phi3D_fsm.c:132-182, single_gpu_cuda/src/phi3D_fsm.cu:249-295).
 //
-// Four variants:
+// Five variants:
 //   god_ref64  -- the reference's own expanded expression trees, every
 //                 operation an explicitly rounded intrinsic so nothing is fused:
 //                 bit-identical to the reference's C compiled without contraction.
@@ -16,6 +16,7 @@
 //                 hundred cells).
 //   god_mixed64 -- FP64 minima and result, FP32 increment (god32s on the
 //                 FP64 differences to the smallest minimum).
+//   god_pair    -- the same with FP32-pair (48-bit) minima and result.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -217,6 +218,58 @@ __device__ __forceinline__ double god_mixed64(double m0, double m1, double m2, c
   const float ea = d2f_nonneg(pa - base), eb = d2f_nonneg(pb - base);
   const float e0 = b0 ? 0.0f : ea, e1 = b0 ? ea : (b1 ? 0.0f : eb), e2 = (b0 || b1) ? eb : 0.0f;
   return base + f2d_nonneg(god32s<ISO>(e0, e1, e2, k));
+}
+
+// ---- FP32 pairs ("double-float") --------------------------------------------------
+// A value v is held as two floats hi + lo: hi is v rounded to float, |lo| <=
+// ulp(hi) / 2, 48 significant bits in all.  A pair fills the 64 bits of an
+// FP64 slot, hi in the low word and lo in the high word, so the FP64 layouts,
+// tensor maps and kernels carry it unchanged.  The exact float sums are
+// Knuth's TwoSum and Dekker's Fast2Sum (D. E. Knuth, TAOCP vol. 2, 4.2.2;
+// T. J. Dekker, "A floating-point technique for extending the available
+// precision", Numer. Math. 18, 1971); every operation is an explicitly
+// rounded float intrinsic so none of them is contracted into an FMA.
+__device__ __forceinline__ float p_hi(double v) { return __int_as_float(__double2loint(v)); }
+__device__ __forceinline__ float p_lo(double v) { return __int_as_float(__double2hiint(v)); }
+__device__ __forceinline__ double p_make(float hi, float lo) {
+  return __hiloint2double(__float_as_int(lo), __float_as_int(hi));
+}
+// a < b for normalised pairs (hi = the value rounded to float)
+__device__ __forceinline__ bool p_lt(double a, double b) {
+  const float ah = p_hi(a), bh = p_hi(b);
+  return ah < bh || (ah == bh && p_lo(a) < p_lo(b));
+}
+// the reference's min(a, b) = a < b ? a : b, on pairs
+__device__ __forceinline__ double pmin(double a, double b) { return p_lt(a, b) ? a : b; }
+// a - b rounded to float (a, b not both infinite)
+__device__ __forceinline__ float p_sub(double a, double b) {
+  return __fadd_rn(__fsub_rn(p_hi(a), p_hi(b)), __fsub_rn(p_lo(a), p_lo(b)));
+}
+// b + x for a finite pair b and a float x >= 0: TwoSum of the high parts,
+// the error folded into the low part, renormalised by Fast2Sum
+__device__ __forceinline__ double p_add(double b, float x) {
+  const float bh = p_hi(b), bl = p_lo(b);
+  const float s = __fadd_rn(bh, x);
+  const float bb = __fsub_rn(s, bh);
+  const float e = __fadd_rn(__fsub_rn(bh, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  const float t = __fadd_rn(bl, e);
+  const float hi = __fadd_rn(s, t);
+  return p_make(hi, __fsub_rn(t, __fsub_rn(hi, s)));
+}
+
+// FP32-pair field, FP32 increment: god_mixed64's scheme with the base, the
+// minima and the result in pairs.  The differences to the base and the
+// final sum run on the FP32 pipe, so no FP64 instruction is left.
+template <bool ISO>
+__device__ __forceinline__ double god_pair(double m0, double m1, double m2, const GodConst32 &k) {
+  const bool b0 = !p_lt(m1, m0) && !p_lt(m2, m0);  // which axis holds the base
+  const bool b1 = !b0 && !p_lt(m2, m1);
+  const double base = b0 ? m0 : (b1 ? m1 : m2);
+  if (!(p_hi(base) < INFINITY)) return base;  // no finite neighbour
+  const double pa = b0 ? m1 : m0, pb = (b0 || b1) ? m2 : m1;
+  const float ea = p_sub(pa, base), eb = p_sub(pb, base);
+  const float e0 = b0 ? 0.0f : ea, e1 = b0 ? ea : (b1 ? 0.0f : eb), e2 = (b0 || b1) ? eb : 0.0f;
+  return p_add(base, god32s<ISO>(e0, e1, e2, k));
 }
 
 }  // namespace pdfs

@@ -94,7 +94,8 @@ constexpr int kRing = kHist + 1;
 const float *default_mlp_blob();
 // Learned scheduler (mlp.cu): per-block minimum of a working field, and the
 // fused feature + network + decision kernel (active[b], *count += actives).
-cudaError_t block_min(const void *u, bool f32, const Layout &L, const pdfs_grid &g, int nbx, int nby, int nbz,
+// kind: 0 FP32 field, 1 FP64 field, 2 FP32-pair field
+cudaError_t block_min(const void *u, int kind, const Layout &L, const pdfs_grid &g, int nbx, int nby, int nbz,
                       float *bmin, cudaStream_t st);
 // ring: kRing slots of nblocks change words, slot cur = the sweep about to
 // run, slot (cur - k) mod kRing = k sweeps ago, hist = sweeps of history.
@@ -120,7 +121,8 @@ struct pdfs_ctx {
   pdfs::Layout L32, L64;
   pdfs::MaskLayout M;
   double *in64 = nullptr;   // exact input, internal FP64 layout (also the polish cap)
-  double *u64 = nullptr;    // FP64 working field
+  double *u64 = nullptr;    // FP64 working field (FP32 pairs under PDFS_ARITH_PAIR)
+  double *cap2 = nullptr;   // the polish cap as FP32 pairs (PDFS_ARITH_PAIR)
   float *u32 = nullptr;     // FP32 working field
   uint32_t *fmask = nullptr;
   void *stage = nullptr;    // reference-layout staging buffer for host transfers
@@ -161,6 +163,8 @@ int ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsign
 // FP64 input -> FP32 working field / FP32 result -> FP64 polish start
 int ctx_narrow(pdfs_ctx *c);
 int ctx_widen(pdfs_ctx *c);
+// the FP64 working field <- the input (a copy, or its pairs)
+int ctx_fp64_start(pdfs_ctx *c);
 // Tensor maps of one grid for a sweep kernel variant: field, cap, mask.
 cudaError_t encode_sweep_maps(int which, int tile, const SweepArgs &a, const Layout &L, const void *cap,
                               CUtensorMap maps[3]);

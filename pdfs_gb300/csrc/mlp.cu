@@ -142,7 +142,7 @@ __device__ __forceinline__ bool history_rule(const FeatArgs &f, long long b) {
 
 // Per-block minimum of a working field (interior nodes): one warp covers
 // four blocks along x, lane = node x offset.
-template <class T>
+template <class T, bool PAIR = false>
 __global__ void k_block_min(const T *__restrict__ u, Layout L, int nx, int ny, int nz, int nbx, int nby, int nbz,
                             float *__restrict__ bmin) {
   const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -154,7 +154,15 @@ __global__ void k_block_min(const T *__restrict__ u, Layout L, int nx, int ny, i
   float m = INFINITY;
   if (x <= nx) {
     for (int z = 1 + bz * 8; z <= min(nz, bz * 8 + 8); ++z)
-      for (int y = 1 + by * 8; y <= min(ny, by * 8 + 8); ++y) m = fminf(m, (float)u[L.index(x, y, z)]);
+      for (int y = 1 + by * 8; y <= min(ny, by * 8 + 8); ++y) {
+        const T v = u[L.index(x, y, z)];
+        float f;
+        if constexpr (PAIR)
+          f = p_hi(v);
+        else
+          f = (float)v;
+        m = fminf(m, f);
+      }
   }
 #pragma unroll
   for (int off = 1; off < 8; off <<= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, off));
@@ -629,12 +637,14 @@ const float *default_mlp_blob() { return kDefaultMlpBlob; }
 const float *default_mlp_blob() { return nullptr; }
 #endif
 
-cudaError_t block_min(const void *u, bool f32, const Layout &L, const pdfs_grid &g, int nbx, int nby, int nbz,
+cudaError_t block_min(const void *u, int kind, const Layout &L, const pdfs_grid &g, int nbx, int nby, int nbz,
                       float *bmin, cudaStream_t st) {
   const long long warps = (long long)((nbx + 3) / 4) * nby * nbz;
   const int grid = (int)((warps * 32 + 255) / 256);
-  if (f32)
+  if (kind == 0)
     k_block_min<float><<<grid, 256, 0, st>>>((const float *)u, L, g.nx, g.ny, g.nz, nbx, nby, nbz, bmin);
+  else if (kind == 2)
+    k_block_min<double, true><<<grid, 256, 0, st>>>((const double *)u, L, g.nx, g.ny, g.nz, nbx, nby, nbz, bmin);
   else
     k_block_min<double><<<grid, 256, 0, st>>>((const double *)u, L, g.nx, g.ny, g.nz, nbx, nby, nbz, bmin);
   return cudaGetLastError();
@@ -801,7 +811,8 @@ static int trace_phase(pdfs_mlp_trainer *t, pdfs_ctx *c, int which, float tol, f
       int r = trainer_grow(t, nb);
       if (r) return r;
       MK(cudaMemcpyAsync(t->count, &t->n, 8, cudaMemcpyHostToDevice, c->st));
-      MK(block_min(f32 ? (const void *)c->u32 : (const void *)c->u64, f32, f32 ? c->L32 : c->L64, c->g, c->nbx,
+      MK(block_min(f32 ? (const void *)c->u32 : (const void *)c->u64,
+                   f32 ? 0 : (c->o.arith == PDFS_ARITH_PAIR ? 2 : 1), f32 ? c->L32 : c->L64, c->g, c->nbx,
                    c->nby, c->nbz, bmin, c->st));
       const FeatArgs f = feat_args(c->bchg, cur, kHist, bmin, c->nbx, c->nby, c->nbz, sn, s, f32 ? 0 : 1, tol, hmin);
       k_features<<<grid, 256, 0, c->st>>>(f, tx, cand);
@@ -853,10 +864,7 @@ extern "C" int pdfs_mlp_trainer_add_solve(pdfs_mlp_trainer *t, const pdfs_grid *
       break;
     }
     if (fp64) {  // plain FP64 solve to o.tol
-      if (cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st) != cudaSuccess) {
-        s = PDFS_ERR_CUDA;
-        break;
-      }
+      if ((s = ctx_fp64_start(c)) != PDFS_OK) break;
       s = trace_phase(t, c, 1, (float)o.tol, bmin, tx, cand);
       break;
     }

@@ -104,6 +104,58 @@ __global__ void k_widen(const float *__restrict__ u32, Layout L32, const double 
   }
 }
 
+// FP32 pairs (godunov.cuh): the pair nearest a double, and its value
+__device__ __forceinline__ double to_pair(double d) {
+  const float hi = (float)d;
+  if (!(fabsf(hi) < INFINITY)) return p_make(hi, 0.0f);  // infinite, or beyond the float range
+  return p_make(hi, (float)(d - (double)hi));
+}
+
+// every element of an FP64 buffer -> the pair nearest it (the polish cap; the
+// start of an FP64-precision solve in pair arithmetic)
+__global__ void k_to_pair(const double *__restrict__ src, double *__restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = to_pair(src[i]);
+}
+
+// FP32 working field -> pair working field (polish start): (u32, 0) for the
+// nodes the sweeps update, the input's nearest pair for frozen nodes and the halo
+__global__ void k_widen_pair(const float *__restrict__ u32, Layout L32, const double *__restrict__ in64,
+                             double *__restrict__ u64, Layout L64, const uint32_t *__restrict__ fmask, MaskLayout M,
+                             int nx, int ny, int nz) {
+  const int y = blockIdx.x, z = blockIdx.y;
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
+    const long long i64 = L64.index(x, y, z);
+    const bool interior = x >= 1 && x <= nx && y >= 1 && y <= ny && z >= 1 && z <= nz;
+    bool frz = !interior;
+    if (interior && fmask) {
+      const uint32_t w = fmask[M.word(x, y, z)];
+      frz = (w >> ((x - 1) & 31)) & 1u;
+    }
+    u64[i64] = frz ? to_pair(in64[i64]) : p_make(u32[L32.index(x, y, z)], 0.0f);
+  }
+}
+
+// pair working field -> reference layout: hi + lo (exact in FP64) for the
+// updated nodes; frozen nodes and the halo take the exact FP64 input
+__global__ void k_unpack_pair(const double *__restrict__ src, Layout L, const double *__restrict__ in64,
+                              const uint32_t *__restrict__ fmask, MaskLayout M, double *__restrict__ ref, int nx,
+                              int ny, int nz) {
+  const int y = blockIdx.x, z = blockIdx.y;
+  double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
+    const long long i = L.index(x, y, z);
+    const bool interior = x >= 1 && x <= nx && y >= 1 && y <= ny && z >= 1 && z <= nz;
+    bool frz = !interior;
+    if (interior && fmask) {
+      const uint32_t w = fmask[M.word(x, y, z)];
+      frz = (w >> ((x - 1) & 31)) & 1u;
+    }
+    const double v = src[i];
+    row[x] = frz ? in64[i] : (double)p_hi(v) + (double)p_lo(v);
+  }
+}
+
 // uint8 mask in the reference layout -> frozen bitmask (interior nodes only)
 __global__ void k_pack_mask(const uint8_t *__restrict__ m, uint32_t *__restrict__ bits, MaskLayout M, int nx,
                             int ny) {
@@ -214,7 +266,7 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !std::isfinite(g->dx) || !std::isfinite(g->dy) ||
       !std::isfinite(g->dz))
     return PDFS_ERR_INVALID;
-  if (o->precision < 0 || o->precision > 2 || o->arith < 0 || o->arith > 2 || o->freeze < 0 || o->freeze > 1 ||
+  if (o->precision < 0 || o->precision > 2 || o->arith < 0 || o->arith > 3 || o->freeze < 0 || o->freeze > 1 ||
       o->scheduler < 0 || o->scheduler > 2 || o->tol < 0 || !std::isfinite(o->tol) || o->fixed_sweeps < 0 ||
       o->max_sweeps < 0 || o->first_ordering < 0 || o->first_ordering > 8)
     return PDFS_ERR_INVALID;
@@ -223,7 +275,9 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   // FP64 kernels: tiles 1 and 4 for the mixed arithmetic; 1-3 for the
   // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4);
   // bricks (tile 5) for every arithmetic
-  if (o->arith == PDFS_ARITH_MIXED) {
+  if (o->arith == PDFS_ARITH_PAIR) {
+    if (t64 != 0 && t64 != 5) return PDFS_ERR_INVALID;  // FP32 pairs: bricks only
+  } else if (o->arith == PDFS_ARITH_MIXED) {
     if (t64 != 0 && t64 != 1 && t64 != 4 && t64 != 5) return PDFS_ERR_INVALID;
   } else {
     if (t64 == 4 && o->arith != PDFS_ARITH_FAST) return PDFS_ERR_INVALID;
@@ -237,13 +291,13 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
 // FP32: 16 x 16 x 32 bricks (tile 9: 4.2 ms per 768^3 sweep against 7.9 ms
 // for the best column tile, 32 x 8 with one row per compute warp).
 // FP64: bricks (tile 5) for the mixed arithmetic (14.4 ms per 768^3 polish
-// sweep against 15.9 ms for 32 x 6 columns); the reference and fast
-// arithmetic are bound by the FP64 pipe and keep 32 x 4 columns unless
-// PDFS_BRICKS64 asks for bricks.
+// sweep against 15.9 ms for 32 x 6 columns) and for FP32 pairs (bricks
+// only); the reference and fast arithmetic are bound by the FP64 pipe and
+// run 2.3x faster on 32 x 4 columns (16 against 36 ms per 384^3 sweep).
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
   c->t32 = t32 ? t32 : 9;
-  c->t64 = t64 ? t64 : ((c->o.arith == PDFS_ARITH_MIXED || getenv("PDFS_BRICKS64")) ? 5 : 1);
+  c->t64 = t64 ? t64 : ((c->o.arith == PDFS_ARITH_MIXED || c->o.arith == PDFS_ARITH_PAIR) ? 5 : 1);
 }
 
 extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_ctx **out) {
@@ -285,6 +339,10 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   const bool need64 = o.precision != PDFS_PREC_FP32 || true;  // FP64 input always resident
   if (need64 && (e = cudaMalloc(&c->in64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
   if ((o.precision != PDFS_PREC_FP32) && (e = cudaMalloc(&c->u64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
+  // FP32-pair polish: the cap (the input) as pairs
+  if (o.arith == PDFS_ARITH_PAIR && o.precision == PDFS_PREC_FP32_POLISH64 &&
+      (e = cudaMalloc(&c->cap2, c->L64.elems * 8)) != cudaSuccess)
+    return fail(e);
   if (need32 && (e = cudaMalloc(&c->u32, c->L32.elems * 4)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->fmask, c->M.words * 4)) != cudaSuccess) return fail(e);
   {
@@ -376,6 +434,7 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   if (c->st) cudaStreamSynchronize(c->st);
   cudaFree(c->in64);
   cudaFree(c->u64);
+  cudaFree(c->cap2);
   cudaFree(c->u32);
   cudaFree(c->fmask);
   cudaFree(c->stage);
@@ -457,6 +516,10 @@ static int load_impl(pdfs_ctx *c, const double *field, const uint8_t *frozen, do
     k_pack_mask<<<mg, 64, 0, c->st>>>(m, c->fmask, c->M, g.nx, g.ny);
     CK(cudaGetLastError());
   }
+  if (c->cap2) {
+    k_to_pair<<<4 * c->sms, 256, 0, c->st>>>(c->in64, c->cap2, c->L64.elems);
+    CK(cudaGetLastError());
+  }
   CK(cudaEventRecord(c->e1, c->st));
   CK(cudaStreamSynchronize(c->st));
   if (ms_h2d) *ms_h2d = ms_between(c->e0, c->e1);
@@ -505,7 +568,7 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   a.maxchg = &c->dstat->chg;
   a.blk_active = active;
   a.blk_chg = blk_chg;
-  a.cap = which == 2 ? (const void *)c->in64 : nullptr;
+  a.cap = which == 2 ? (c->cap2 ? (const void *)c->cap2 : (const void *)c->in64) : nullptr;
   a.nbx = c->nbx;
   a.nby = c->nby;
   a.nbz = c->nbz;
@@ -556,7 +619,10 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
   if (blk_chg) CK(cudaMemsetAsync(blk_chg, 0, (size_t)c->nblocks * 4, c->st));
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
-  const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF : (c->o.arith == PDFS_ARITH_MIXED ? ARITH_MIXED : ARITH_FAST);
+  const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF
+                    : c->o.arith == PDFS_ARITH_MIXED   ? ARITH_MIXED
+                    : c->o.arith == PDFS_ARITH_PAIR    ? ARITH_PAIR
+                                                       : ARITH_FAST;
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
   if (ts.bz > 0) {
@@ -591,9 +657,27 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   return PDFS_OK;
 }
 
+int pdfs::ctx_fp64_start(pdfs_ctx *c) {  // FP64 working field <- the input
+  if (c->o.arith == PDFS_ARITH_PAIR) {
+    k_to_pair<<<4 * c->sms, 256, 0, c->st>>>(c->in64, c->u64, c->L64.elems);
+    c->launches++;
+    CK(cudaGetLastError());
+  } else {
+    CK(cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st));
+  }
+  return PDFS_OK;
+}
+
 int pdfs::ctx_widen(pdfs_ctx *c) {
   const pdfs_grid &g = c->g;
   dim3 grid(g.ny + 2, g.nz + 2);
+  if (c->o.arith == PDFS_ARITH_PAIR) {
+    k_widen_pair<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64,
+                                          c->has_mask ? c->fmask : nullptr, c->M, g.nx, g.ny, g.nz);
+    c->launches++;
+    CK(cudaGetLastError());
+    return PDFS_OK;
+  }
   k_widen<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64, c->has_mask ? c->fmask : nullptr, c->M,
                                    g.nx, g.ny, g.nz);
   c->launches++;
@@ -658,8 +742,8 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         CK(cudaMemsetAsync(&c->dstat->active_blocks, 0, 4, c->st));
         if (o.scheduler == PDFS_SCHED_LEARNED) {
           const bool f32 = which == 0;
-          CK(block_min(f32 ? (const void *)c->u32 : (const void *)c->u64, f32, f32 ? c->L32 : c->L64, g, c->nbx,
-                       c->nby, c->nbz, c->bmin, c->st));
+          CK(block_min(f32 ? (const void *)c->u32 : (const void *)c->u64, f32 ? 0 : (o.arith == PDFS_ARITH_PAIR ? 2 : 1),
+                       f32 ? c->L32 : c->L64, g, c->nbx, c->nby, c->nbz, c->bmin, c->st));
           CK(sched_learned(c->mlp_w, c->mlp_thr, c->bchg, cur, std::min(s, kHist), c->bmin, c->nbx, c->nby,
                            c->nbz, sn, s, f32 ? 0 : 1, thr, (float)std::min(g.dx, std::min(g.dy, g.dz)), c->bact,
                            &c->dstat->active_blocks, &c->dstat->sched_err, c->sms, c->st));
@@ -705,7 +789,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
 
   int r = PDFS_OK;
   if (o.precision == PDFS_PREC_FP64) {
-    CK(cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st));
+    if ((r = ctx_fp64_start(c))) return r;
     r = phase(1, o.tol, &st.sweeps_fp64, &st.ms_fp64, &st.ms_kern_fp64);
     c->last_prec = 1;
   } else {
@@ -743,7 +827,9 @@ static int store_impl(pdfs_ctx *c, double *field, double *ms_d2h) {
   CK(cudaEventRecord(c->e0, c->st));
   dim3 grid(g.ny + 2, g.nz + 2);
   const uint32_t *fm = c->has_mask ? c->fmask : nullptr;
-  if (c->last_prec == 1)
+  if (c->last_prec == 1 && c->o.arith == PDFS_ARITH_PAIR)
+    k_unpack_pair<<<grid, 128, 0, c->st>>>(c->u64, c->L64, c->in64, fm, c->M, dst, g.nx, g.ny, g.nz);
+  else if (c->last_prec == 1)
     k_unpack<double><<<grid, 128, 0, c->st>>>(c->u64, c->L64, c->in64, c->L64, nullptr, c->M, dst, g.nx, g.ny);
   else
     k_unpack<float><<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->L64, fm, c->M, dst, g.nx, g.ny);
@@ -801,7 +887,8 @@ extern "C" int pdfs_ctx_sweep(pdfs_ctx *c, int sn, const uint8_t *active, float 
   const int prec = c->o.precision == PDFS_PREC_FP32 ? 0 : 1;
   if (c->last_prec != prec) {  // start from the loaded input
     if (prec == 1) {
-      CK(cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st));
+      int r = ctx_fp64_start(c);
+      if (r) return r;
     } else {
       int r = ctx_narrow(c);
       if (r) return r;

@@ -51,7 +51,7 @@
 namespace pdfs {
 
 enum { MODE_MIN = 0, MODE_REPLACE = 1 };
-enum { ARITH_REF = 0, ARITH_FAST = 1, ARITH_MIXED = 2 };
+enum { ARITH_REF = 0, ARITH_FAST = 1, ARITH_MIXED = 2, ARITH_PAIR = 3 };
 enum { DEV_ERR_TIMEOUT = 1, DEV_ERR_SMEM_ALIGN = 2 };
 
 struct SweepArgs {
@@ -205,10 +205,13 @@ __device__ __forceinline__ T tmin(T a, T b) {  // the reference's min macro: a <
 
 // Minimum, "changed" test and running max of a variant: the mixed FP64
 // kernels do them on integer keys / bit patterns, off the FP64 pipe.
+// FP32-pair variants (ARITH_PAIR, FP64 slots holding pairs) work on the two floats.
 template <class T, int ARITH>
 __device__ __forceinline__ T vmin(T a, T b) {
   if constexpr (sizeof(T) == 8 && ARITH == ARITH_MIXED)
     return kmin(a, b);
+  else if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+    return pmin(a, b);
   else
     return tmin(a, b);
 }
@@ -216,6 +219,8 @@ template <class T, int ARITH>
 __device__ __forceinline__ bool vdiffers(T a, T b) {
   if constexpr (sizeof(T) == 8 && ARITH == ARITH_MIXED)
     return __double_as_longlong(a) != __double_as_longlong(b);
+  else if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+    return p_hi(a) != p_hi(b) || p_lo(a) != p_lo(b);
   else
     return a != b;
 }
@@ -223,8 +228,43 @@ template <class T, int ARITH>
 __device__ __forceinline__ T vmax_nonneg(T a, T b) {  // a, b >= 0
   if constexpr (sizeof(T) == 8 && ARITH == ARITH_MIXED)
     return __double_as_longlong(a) < __double_as_longlong(b) ? b : a;
+  else if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+    return p_hi(a) < p_hi(b) ? b : a;
   else
     return fmax(a, b);
+}
+
+// A node's change as a kernel accumulates it: relative for FP32, absolute
+// for FP64, absolute as the pair (|change|, 0) for FP32 pairs.
+template <class T, int ARITH>
+__device__ __forceinline__ T node_change(T cv, T nv, float hmin) {
+  if constexpr (sizeof(T) == 4)
+    return __fdividef(fabsf(cv - nv), fmaxf(nv, hmin));
+  else if constexpr (ARITH == ARITH_PAIR)
+    return p_make(fabsf(p_sub(cv, nv)), 0.0f);
+  else
+    return fabs(cv - nv);
+}
+template <class T, int ARITH>
+__device__ __forceinline__ float change_f(T d) {  // as a float (per-block change words)
+  if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+    return p_hi(d);
+  else
+    return (float)d;
+}
+template <class T, int ARITH>
+__device__ __forceinline__ bool change_pos(T d) {
+  if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+    return p_hi(d) > 0.0f;
+  else
+    return d > T(0);
+}
+template <class T, int ARITH>
+__device__ __forceinline__ unsigned long long change_u64(T d) {  // the FP64 phases' max-change word
+  if constexpr (ARITH == ARITH_PAIR)
+    return (unsigned long long)__double_as_longlong((double)p_hi(d));
+  else
+    return (unsigned long long)__double_as_longlong((double)d);
 }
 
 // The local solver of a kernel variant.  k64 / k32 are the compute warps'
@@ -265,6 +305,17 @@ PDFS_LUMX(MODE_MIN, false)
 PDFS_LUMX(MODE_REPLACE, true)
 PDFS_LUMX(MODE_REPLACE, false)
 #undef PDFS_LUMX
+#define PDFS_LUPR(MODE_, ISO_)                                                                       \
+  template <>                                                                                       \
+  __device__ __forceinline__ double local_update<double, MODE_, ARITH_PAIR, ISO_>(                  \
+      double m0, double m1, double m2, const GodConst64 &, const GodConst32 &k32) {                 \
+    return god_pair<ISO_>(m0, m1, m2, k32);                                                         \
+  }
+PDFS_LUPR(MODE_MIN, true)
+PDFS_LUPR(MODE_MIN, false)
+PDFS_LUPR(MODE_REPLACE, true)
+PDFS_LUPR(MODE_REPLACE, false)
+#undef PDFS_LUPR
 
 // Records a timeout and raises the abort flags (global and CTA).
 __device__ __forceinline__ void raise_timeout(const SweepArgs &a, int col, volatile int *s_abort) {

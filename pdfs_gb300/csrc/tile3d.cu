@@ -51,11 +51,17 @@ static cudaError_t dispatch_t3(int which, int arith, bool iso, const SweepArgs &
     if (which == 1) {
       if (arith == ARITH_REF) return launch_t3<double, BZ, MODE_MIN, ARITH_REF, false>(a, L, sms, st, g);
       if (arith == ARITH_FAST) return launch_t3<double, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
+      if (arith == ARITH_PAIR)
+        return iso ? launch_t3<double, BZ, MODE_MIN, ARITH_PAIR, true>(a, L, sms, st, g)
+                   : launch_t3<double, BZ, MODE_MIN, ARITH_PAIR, false>(a, L, sms, st, g);
       return iso ? launch_t3<double, BZ, MODE_MIN, ARITH_MIXED, true>(a, L, sms, st, g)
                  : launch_t3<double, BZ, MODE_MIN, ARITH_MIXED, false>(a, L, sms, st, g);
     }
     if (arith == ARITH_REF) return launch_t3<double, BZ, MODE_REPLACE, ARITH_REF, false>(a, L, sms, st, g);
     if (arith == ARITH_FAST) return launch_t3<double, BZ, MODE_REPLACE, ARITH_FAST, false>(a, L, sms, st, g);
+    if (arith == ARITH_PAIR)
+      return iso ? launch_t3<double, BZ, MODE_REPLACE, ARITH_PAIR, true>(a, L, sms, st, g)
+                 : launch_t3<double, BZ, MODE_REPLACE, ARITH_PAIR, false>(a, L, sms, st, g);
     return iso ? launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, true>(a, L, sms, st, g)
                : launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, false>(a, L, sms, st, g);
   }

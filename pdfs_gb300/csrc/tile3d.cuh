@@ -281,11 +281,7 @@ __global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ C
             if (vdiffers<T, ARITH>(nv, cv)) {
               box[o] = nv;
               u[gbase + (long long)gz * plane] = nv;
-              T d;
-              if (sizeof(T) == 4)
-                d = (T)__fdividef(fabsf((float)cv - (float)nv), fmaxf((float)nv, hmin));
-              else
-                d = (T)fabs((double)cv - (double)nv);
+              const T d = node_change<T, ARITH>(cv, nv, hmin);
               tmax = vmax_nonneg<T, ARITH>(tmax, d);
 #pragma unroll
               for (int q = 0; q < NZB; ++q)
@@ -315,9 +311,9 @@ __global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ C
         }
         // only nodes inside the grid change, so v > 0 names a block of the grid
         const int bz = bk * NZB + q;
-        if ((lane == 0 || lane == 8) && v > T(0) && bz < a.nbz) {
+        if ((lane == 0 || lane == 8) && change_pos<T, ARITH>(v) && bz < a.nbz) {
           const int bx = (x0 - 1 + gxl) >> 3, by = (y0 - 1 + gyl) >> 3;
-          atomicMax(blk_chg + ((long long)bz * a.nby + by) * a.nbx + bx, __float_as_uint((float)v));
+          atomicMax(blk_chg + ((long long)bz * a.nby + by) * a.nbx + bx, __float_as_uint(change_f<T, ARITH>(v)));
         }
       }
     }
@@ -331,11 +327,11 @@ __global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ C
     T v = tmax;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(0xffffffffu, v, off));
-    if (lane == 0 && v > T(0)) {
-      if (sizeof(T) == 4)
-        atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint((float)v));
+    if (lane == 0 && change_pos<T, ARITH>(v)) {
+      if constexpr (sizeof(T) == 4)
+        atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint(v));
       else
-        atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg), (unsigned long long)__double_as_longlong((double)v));
+        atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg), change_u64<T, ARITH>(v));
     }
   }
 }

@@ -59,11 +59,14 @@ def test_invalid_grid_rejected_before_device(grid):
 def test_invalid_options_rejected():
     g = L.Grid(4, 4, 4, 1.0, 1.0, 1.0)
     f = np.zeros(6 * 6 * 6, dtype=np.float64)
-    for k, v in [("precision", 7), ("arith", 3), ("freeze", -1), ("tol", -1.0), ("first_ordering", 9),
+    for k, v in [("precision", 7), ("arith", 4), ("freeze", -1), ("tol", -1.0), ("first_ordering", 9),
                  ("tile", 99)]:
         o = api.make_opts()
         setattr(o, k, v)
         assert L.load().pdfs_solve(C.byref(g), f.ctypes.data, None, C.byref(o), None) == L.PDFS_ERR_INVALID, k
+    # FP32 pairs run on the FP64 bricks (tile 5) only
+    o = api.make_opts(arith=L.ARITH_PAIR, tile=1 << 8)
+    assert L.load().pdfs_solve(C.byref(g), f.ctypes.data, None, C.byref(o), None) == L.PDFS_ERR_INVALID
     assert L.load().pdfs_sweep(C.byref(g), f.ctypes.data, None, 0, None, None) == L.PDFS_ERR_INVALID
 
 

@@ -177,3 +177,88 @@ def test_brick_bounded_wait_times_out_cleanly(monkeypatch):
     api.solve(a, sp, tol=0.0, tile=B64)
     O.solve(b, sp, tol=0.0, threads=8)
     assert same(a, b)
+
+
+# ---- FP32-pair arithmetic (FP64 bricks) --------------------------------------------------
+def rel_err(a, b, h):
+    return float(np.max(np.abs(inner(a) - inner(b)) / np.maximum(np.abs(inner(b)), h)))
+
+
+@pytest.mark.parametrize("iso", [True, False])
+def test_pair_polish_within_1e6(iso):
+    """FP32 bulk + FP32-pair polish against the FP64 oracle; frozen nodes and
+    the halo come back as the exact input."""
+    sz = 1.0 if iso else 0.5
+    w = W.random_spheres(90, 70, 60, 1.0, 1.0, sz, 8, 3.0, 14.0, seed=91)
+    sp = (w.dx, w.dy, w.dz)
+    a = w.field.copy()
+    st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
+                   arith=L.ARITH_PAIR, tol=1e-6 * min(sp), max_sweeps=200)
+    assert st["tile"] >> 8 == 5 and st["sweeps_fp64"] > 0
+    b = w.field.copy()
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    # tolerance: 1e-6 relative, as for the mixed arithmetic
+    assert rel_err(a, b, min(sp)) <= 1e-6
+    fz = w.frozen.astype(bool)
+    assert same(a[fz], w.field[fz])
+    halo = np.ones(a.shape, bool)
+    halo[1:-1, 1:-1, 1:-1] = False
+    assert same(a[halo], w.field[halo])
+
+
+def test_pair_agrees_with_mixed():
+    """Both keep an FP32 increment over a wide base; their fixed points agree
+    to a few 1e-8 relative."""
+    w = W.random_spheres(64, 64, 64, 1.0, 1.0, 1.0, 6, 3.0, 12.0, seed=92)
+    sp = (w.dx, w.dy, w.dz)
+    out = []
+    for ar in (L.ARITH_PAIR, L.ARITH_MIXED):
+        a = w.field.copy()
+        api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=ar,
+                  tol=1e-6, max_sweeps=200)
+        out.append(a)
+    assert rel_err(out[0], out[1], 1.0) <= 3e-7
+
+
+def test_pair_fp64_precision_solve():
+    """PREC_FP64 in pair arithmetic from the input (no FP32 phase)."""
+    w = W.random_spheres(72, 50, 40, 1.0, 1.0, 1.0, 5, 3.0, 12.0, seed=93)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP64, arith=L.ARITH_PAIR,
+              tol=1e-6, max_sweeps=200)
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    assert rel_err(a, b, 1.0) <= 1e-6
+
+
+@pytest.mark.parametrize("sn", [3, 8])
+def test_pair_masked_sweep_equals_frozen(grid, sn):
+    """A block-masked pair sweep equals the same sweep with the inactive
+    blocks' nodes frozen, bit for bit, and reports the same block changes."""
+    w = grid
+    act = patterned_mask(tuple(np.array(((w.nz + 7) // 8, (w.ny + 7) // 8, (w.nx + 7) // 8))),
+                         np.random.default_rng(700 + sn))
+    kw = dict(precision=L.PREC_FP64, arith=L.ARITH_PAIR)
+    with ctx_for(w, **kw) as c:
+        bc = np.zeros(act.shape, np.float32)
+        c.sweep(sn, act, bc)
+        got = np.empty_like(w.field)
+        c.store(got)
+    fz = (w.frozen | node_mask(act, w.field.shape)).astype(np.uint8)
+    with api.Context(w.nx, w.ny, w.nz, (w.dx, w.dy, w.dz), freeze=L.FREEZE_MASK, **kw) as c2:
+        c2.load(w.field, fz)
+        c2.sweep(sn)
+        exp = np.empty_like(w.field)
+        c2.store(exp)
+    assert same(got, exp)
+    assert not bc[act == 0].any()
+
+
+def test_pair_learned_scheduler_polish():
+    w = W.random_spheres(96, 80, 72, 1.0, 1.0, 1.0, 6, 3.0, 16.0, seed=5)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR,
+              tol=1e-6, max_sweeps=200, scheduler=L.SCHED_LEARNED)
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    assert rel_err(a, b, 1.0) <= 1e-6
