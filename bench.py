@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--mode", default="polish", choices=["polish", "fp32", "fp64", "fp64ref"])
     p.add_argument("--scheduler", default="none", choices=["none", "change", "learned"])
     p.add_argument("--tol", type=float, default=1e-5, help="FP64 polish tolerance (max change)")
-    p.add_argument("--polish-arith", default="mixed", choices=["mixed", "pair", "fast"],
+    p.add_argument("--polish-arith", default="pair", choices=["mixed", "pair", "fast"],
                    help="polish arithmetic: FP32 increments over an FP64 field (mixed) or an FP32-pair "
                         "field (pair), or all FP64 (fast)")
     p.add_argument("--no-sched-table", action="store_true", help="skip timing the three schedulers")
@@ -321,8 +321,9 @@ def run_batch(args, rank, world, pg, device):
 
 
 def run_configs(args, device):
-    """One JSON line per config (C1..C4): the FP32 + mixed-polish solve and
-    the FP32-only solve against the plain FP64 FSM on the same input -- max
+    """One JSON line per config (C1..C4): the FP32 + pair-polish and
+    FP32 + mixed-polish solves and the FP32-only solve against the plain FP64
+    FSM on the same input -- max
     and RMS relative error, sweeps and times.  C1 also runs the FP64
     reference arithmetic (bit-exact with the reference at tol 1e-12)."""
     from pdfs_gb300 import _lib as L
@@ -341,7 +342,8 @@ def run_configs(args, device):
         den = np.maximum(np.abs(ref[i]), h)
         out = {"config": name, "workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "spacing": list(sp),
                "plain_fp64": {"sweeps": ps["sweeps_fp64"], "time_s": t_plain}}
-        cases = [("fp32_polish_mixed", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_MIXED, tol=1e-5 * h)),
+        cases = [("fp32_polish_pair", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5 * h)),
+                 ("fp32_polish_mixed", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_MIXED, tol=1e-5 * h)),
                  ("fp32_only", dict(precision=L.PREC_FP32))]
         if name == "C1":
             cases.append(("fp64_reference_arith", dict(precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, tol=1e-12)))

@@ -38,10 +38,12 @@ struct MaskLayout {
 MaskLayout make_mask_layout(const pdfs_grid &g);
 
 // A sweep kernel variant: a column tile (tx x ty, c rows per compute warp,
-// bz = 0) or a brick (tx x ty x bz, tile3d.cuh).
+// bz = 0), a brick (tx x ty x bz, tile3d.cuh) or a pencil (tx x ty along z,
+// pencil.cuh; block-masked sweeps on bricks of depth bz).
 struct TileShape {
   int tx, ty, c;
   int bz = 0;
+  int pencil = 0;
 };
 // Tile ids (1-based) for FP32 and FP64 kernels.
 int tile_count32();
@@ -58,6 +60,11 @@ cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepAr
 // a.torder / a.ntx.. / a.epoch filled in.
 cudaError_t launch_sweep_bricks(int which, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
                                 cudaStream_t st, int *grid_used);
+// One unmasked sweep by the pencil kernel (pencil.cu): 16 x 16 pencils, the
+// column order / progress words of a 16 x 16 layout.
+cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
+                                 cudaStream_t st, int *grid_used);
+cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty);
 // Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
 std::vector<int> brick_order(int ntx, int nty, int ntz);
 cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by,

@@ -1,0 +1,319 @@
+// pencil.cuh -- the pencil sweep: a CTA marches a 16 x 16 pencil of the grid
+// through the whole z extent, one CTA barrier per level.
+//
+// The reference sweeps one hyperplane x+y+z = level of the whole grid per
+// kernel launch (single_gpu_cuda/src/phi3D_fsm.cu:161-185,
+// mpi_openacc/src/phi3D_fsm.c:92-117).  Any topological order of an
+// ordering's dependency DAG gives the same result (each node reads the new
+// values of its three upwind neighbours and the old values of its three
+// downwind ones).  This kernel's order:
+//   * compute thread (lx, ly) -- pencil-local coordinates in sweep order --
+//     updates node (lx, ly, lz = G - lx - ly) at level G; a named barrier of
+//     the 256 compute threads separates levels.  Every thread is busy on all
+//     but SK = 30 of the nz + 30 levels, where a brick (tile3d.cuh) idles its
+//     threads for 30 of every BZ + 30;
+//   * planes stream through a ring of D shared-memory slots (TMA,
+//     cp.async.bulk.tensor; one mbarrier per slot), as far ahead as the slot
+//     of the plane SK + 1 levels back allows;
+//   * a helper warp loads the planes, patches into them the upwind faces of
+//     the neighbouring pencils and publishes this pencil's progress (levels
+//     complete).  Thread (0, ly) at level G reads the upwind x pencil's node
+//     (15, ly, G - ly), which that pencil computed at its level G + 15: all
+//     sixteen x-face cells of level G are ready once the upwind pencil has
+//     published G + 16, and likewise the y face.  The faces are read from the
+//     field itself (L2) -- a node's value there is final once its pencil has
+//     passed it;
+//   * pencils are taken by ticket in wavefront order, so an upwind pencil is
+//     always running or done; every wait is bounded (SweepArgs::wait_cycles)
+//     and ends in DEV_ERR_TIMEOUT plus the abort flag, never in a hang.
+// Sweeps with a block mask or block-change output run on bricks instead.
+#pragma once
+#include "sweep.cuh"
+
+namespace pdfs {
+
+template <class T>
+struct PcGeo {
+  static constexpr int BX = 16, BY = 16;
+  static constexpr int V = 16 / (int)sizeof(T);
+  static constexpr int W = BX + 2 * V;     // slot row: x0-V .. x0+BX+V-1 (16-byte aligned start)
+  static constexpr int RY = BY + 2;        // slot rows: y0-1 .. y0+BY
+  static constexpr int SK = BX + BY - 2;   // thread (15, 15) trails thread (0, 0) by SK planes
+  static constexpr int LOOK = sizeof(T) == 4 ? 5 : 3;  // planes requested ahead of use
+  static constexpr int D = SK + 3 + LOOK;  // ring slots
+  static constexpr unsigned FIELD_BYTES = (unsigned)(W * RY * sizeof(T));
+  static constexpr unsigned MASK_OFF = (FIELD_BYTES + 127u) & ~127u;  // the plane's 16 frozen words
+  static constexpr unsigned SLOT_BYTES = MASK_OFF + 128u;
+  static constexpr int NC = BX * BY;       // compute threads
+  static constexpr int NT = NC + 32;       // and the helper warp
+  static constexpr int C = 8;              // levels the helper prepares per round, at most
+  static constexpr int CP = 4;             // replace-update: caps prefetched ahead (registers)
+  static constexpr size_t OFF_BAR = (size_t)D * SLOT_BYTES;
+  static constexpr size_t BYTES = OFF_BAR + (size_t)D * 8 + 16;
+  static_assert(SLOT_BYTES % 128 == 0, "TMA destinations stay 128-byte aligned");
+};
+
+__device__ __forceinline__ void compute_bar() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
+
+template <class T, int MODE, int ARITH, bool ISO>
+__global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
+                                                               const __grid_constant__ CUtensorMap tm_mask,
+                                                               const __grid_constant__ SweepArgs a) {
+  using G = PcGeo<T>;
+  constexpr int BX = G::BX, BY = G::BY, V = G::V, W = G::W, SK = G::SK, D = G::D, CP = G::CP;
+  constexpr int SE = (int)(G::SLOT_BYTES / sizeof(T));  // slot stride in elements
+  extern __shared__ __align__(1024) unsigned char sm[];
+  T *ring = reinterpret_cast<T *>(sm);
+  uint64_t *full = reinterpret_cast<uint64_t *>(sm + G::OFF_BAR);
+  __shared__ int s_ticket, s_stop, s_done, s_ready;
+  __shared__ volatile int s_abort;
+
+  if ((saddr(sm) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
+    if (threadIdx.x == 0) {
+      atomicCAS(a.err, 0, DEV_ERR_SMEM_ALIGN);
+      atomicExch(a.err + 1, 1);
+    }
+    return;
+  }
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool helper = warp == G::NC / 32;
+  const int ntick = a.ncx * a.ncy;
+  const int sxd = a.sx, syd = a.sy, szd = a.sz;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int NP = nz + 2, t_end = nz + SK;  // planes (sweep order, halo planes included), levels
+  const long long plane = a.plane, px = a.px;
+  const bool masked = a.fmask != nullptr;
+  T tmax = T(0);
+
+  if (tid == 0) s_abort = 0;
+  for (int npen = 0;; ++npen) {
+    if (tid == 0) {
+      const int tk = atomicAdd(a.ticket, 1);
+      s_ticket = tk;
+      if (*(volatile int *)(a.err + 1)) s_abort = 1;
+      s_stop = (tk >= ntick || s_abort) ? 1 : 0;
+      s_done = 0;
+      s_ready = 0;
+      for (int i = 0; i < D; ++i) {
+        if (npen) mbar_inval(full + i);
+        mbar_init(full + i, 1);
+      }
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (s_stop) break;
+    const int lc = a.order[s_ticket];
+    const int lcx = lc % a.ncx, lcy = lc / a.ncx;
+    const int cx = sxd > 0 ? lcx : a.ncx - 1 - lcx;
+    const int cy = syd > 0 ? lcy : a.ncy - 1 - lcy;
+    const int col = cy * a.ncx + cx;
+    const int upx = lcx > 0 ? col - sxd : -1;
+    const int upy = lcy > 0 ? col - syd * a.ncx : -1;
+    const int x0 = 1 + cx * BX, y0 = 1 + cy * BY;
+
+    if (helper) {
+      // ------------------------------------ helper warp ------------------------------------
+      int q_issue = 0, q_land = 0;  // planes requested / seen landed (plane q in slot q % D)
+      int g_ready = 0, pub = 0;     // levels prepared / progress published
+      const unsigned tx_bytes = G::FIELD_BYTES + (masked ? 64u : 0u);
+      const int xu = sxd > 0 ? x0 - 1 : x0 + BX, sxo = sxd > 0 ? V - 1 : V + BX;  // x face: grid x, slot x
+      const int yu = syd > 0 ? y0 - 1 : y0 + BY, syo = syd > 0 ? 0 : BY + 1;      // y face: grid y, slot row
+      long long t_last = cycles();
+      unsigned nap = 0;
+      bool failed = false;
+      for (;;) {
+        bool moved = false;
+        const int done = __shfl_sync(0xffffffffu, ld_acquire_cta_s(&s_done), 0);
+        if (done > pub) {  // the compute threads' node stores are visible before the progress word
+          __threadfence();
+          if (lane == 0 && col != a.poison_col) st_relaxed_gpu(a.prog + col, done);
+          pub = done;
+          moved = true;
+        }
+        if (lane == 0) {
+          // plane q reuses the slot of plane q - D, last read at level q - D + SK
+          while (q_issue < NP && (q_issue < D || done >= q_issue - D + SK + 1)) {
+            const int s = q_issue % D;
+            const int gz = szd > 0 ? q_issue : nz + 1 - q_issue;
+            unsigned char *dst = sm + (size_t)s * G::SLOT_BYTES;
+            mbar_arrive_tx(full + s, tx_bytes);
+            tma_load_3d(dst, &tm_u, cx * BX, y0 - 1, gz, full + s);
+            if (masked) tma_load_3d(dst + G::MASK_OFF, &tm_mask, cy * BY, cx >> 1, gz, full + s);
+            ++q_issue;
+            moved = true;
+          }
+          while (q_land < q_issue && mbar_try(full + q_land % D, (q_land / D) & 1)) ++q_land;
+        }
+        // lane 0's requests count as progress for the whole warp: every decision
+        // below (including the give-up) is warp-uniform
+        moved = __any_sync(0xffffffffu, moved);
+        q_issue = __shfl_sync(0xffffffffu, q_issue, 0);
+        q_land = __shfl_sync(0xffffffffu, q_land, 0);
+        if (g_ready < t_end) {
+          // level g needs planes up to min(g + 2, NP - 1) and upwind progress >= min(g + 16, t_end)
+          int ux = 0x3fffffff, uy = 0x3fffffff;
+          if (upx >= 0 && lane == 0) ux = ld_acquire_gpu(a.prog + upx);
+          if (upy >= 0 && lane == 1) uy = ld_acquire_gpu(a.prog + upy);
+          ux = __shfl_sync(0xffffffffu, ux, 0);
+          uy = __shfl_sync(0xffffffffu, uy, 1);
+          const int um = min(ux, uy);
+          int lim = um >= t_end ? t_end : um - 15;
+          lim = min(lim, q_land >= NP ? t_end : q_land - 2);
+          lim = min(lim, g_ready + G::C);
+          if (lim > g_ready) {
+            // faces of levels g_ready .. lim-1: lane < 16 -> x face row ly = lane,
+            // lane >= 16 -> y face column lx = lane - 16; loads first, then stores
+            T v[G::C];
+            int off[G::C];
+            const int k = lane & 15;
+            const bool xl = lane < 16;
+            const bool have = xl ? upx >= 0 : upy >= 0;
+            const int gk = xl ? (syd > 0 ? k : BY - 1 - k) : (sxd > 0 ? k : BX - 1 - k);
+            const bool inside = xl ? (y0 + gk <= ny) : (x0 + gk <= nx);
+#pragma unroll
+            for (int i = 0; i < G::C; ++i) {
+              off[i] = -1;
+              const int g = g_ready + i, lz = g - k;
+              if (have && inside && g < lim && lz >= 0 && lz < nz) {
+                const int gz = szd > 0 ? lz + 1 : nz - lz;
+                const long long gi = xl ? (long long)gz * plane + (long long)(y0 + gk) * px + xu + (V - 1)
+                                        : (long long)gz * plane + (long long)yu * px + x0 + gk + (V - 1);
+                v[i] = __ldcg(reinterpret_cast<const T *>(a.u) + gi);
+                const int s = (lz + 1) % D;
+                off[i] = s * SE + (xl ? (1 + gk) * W + sxo : syo * W + V + gk);
+              }
+            }
+#pragma unroll
+            for (int i = 0; i < G::C; ++i)
+              if (off[i] >= 0) ring[off[i]] = v[i];
+            __syncwarp();
+            if (lane == 0) st_release_cta_s(&s_ready, lim);
+            g_ready = lim;
+            moved = true;
+          }
+        }
+        if (pub >= t_end && q_land >= NP) break;  // every level done and published
+        if (moved) {
+          t_last = cycles();
+          nap = 0;
+        } else {
+          int stop = 0;  // lane 0 decides for the warp
+          if (lane == 0) {
+            if (s_abort || *(volatile int *)(a.err + 1)) {
+              stop = 1;
+            } else if (cycles() - t_last > a.wait_cycles) {
+              raise_timeout(a, col, &s_abort);
+              stop = 1;
+            }
+          }
+          if (__shfl_sync(0xffffffffu, stop, 0)) {
+            s_abort = 1;
+            failed = true;
+            break;
+          }
+          if (nap) __nanosleep(nap);
+          nap = min(nap + 32u, 128u);
+        }
+      }
+      if (failed && lane == 0) {  // let the copies in flight land before the CTA leaves
+        for (int q = q_land; q < q_issue; ++q) {
+          const long long t0 = cycles();
+          while (!mbar_try(full + q % D, (q / D) & 1) && cycles() - t0 < 4000000000ll) {
+          }
+        }
+      }
+    } else {
+      // ------------------------------------ compute threads ------------------------------------
+      const int lx = tid & (BX - 1), ly = tid / BX, lxy = lx + ly;  // sweep order
+      const int gx = sxd > 0 ? lx : BX - 1 - lx, gy = syd > 0 ? ly : BY - 1 - ly;
+      const bool vxy = (x0 + gx <= nx) && (y0 + gy <= ny);
+      const int orow = (1 + gy) * W + V + gx;  // my node within a slot
+      const int mbyte = (int)G::MASK_OFF + 4 * gy, mshift = 16 * (cx & 1) + gx;
+      const long long grow = (long long)(y0 + gy) * px + (x0 + gx) + (V - 1);
+      const float hmin = a.hmin;
+      const GodConst64 k64 = a.k64;
+      const GodConst32 k32 = a.k32;
+      T *__restrict__ u = reinterpret_cast<T *>(a.u);
+      const T *__restrict__ capg = reinterpret_cast<const T *>(a.cap);
+      auto gz_of = [&](int lz) { return szd > 0 ? lz + 1 : nz - lz; };
+      T capq[CP];
+      auto cap_at = [&](int lz) -> T {
+        if (MODE != MODE_REPLACE || !vxy || lz >= nz) return T(0);
+        return __ldg(capg + (long long)gz_of(lz) * plane + grow);
+      };
+#pragma unroll
+      for (int q = 0; q < CP; ++q) capq[q] = cap_at(q);
+      int sl = (1 - lxy) % D;  // slot of my node's plane (lz + 1) at level 0
+      if (sl < 0) sl += D;
+      for (int g = 0; g < t_end; ++g) {
+        if (tid == 0 && ld_acquire_cta_s(&s_ready) <= g) {
+          const long long t0 = cycles();
+          while (ld_acquire_cta_s(&s_ready) <= g) {
+            if (s_abort) {
+              s_stop = 1;
+              break;
+            }
+            if (cycles() - t0 > a.wait_cycles) {
+              raise_timeout(a, col, &s_abort);
+              s_stop = 1;
+              break;
+            }
+          }
+        }
+        compute_bar();
+        if (s_stop) break;
+        if (tid == 0) st_release_cta_s(&s_done, g);  // levels below g are complete
+        const int lz = g - lxy;
+        if ((unsigned)lz < (unsigned)nz) {
+          if (vxy) {
+            const int sp = sl == 0 ? D - 1 : sl - 1, sn = sl == D - 1 ? 0 : sl + 1;
+            T *cur = ring + sl * SE;
+            const T *prv = ring + sp * SE, *nxt = ring + sn * SE;
+            const T cv = cur[orow];
+            const T m0 = vmin<T, ARITH>(cur[orow - 1], cur[orow + 1]);
+            const T m1 = vmin<T, ARITH>(cur[orow - W], cur[orow + W]);
+            // grid orientation: min(u[z-1], u[z+1]); the sweep's previous plane is z-1 when sz > 0
+            const T m2 = szd > 0 ? vmin<T, ARITH>(prv[orow], nxt[orow]) : vmin<T, ARITH>(nxt[orow], prv[orow]);
+            bool act = true;
+            if (masked) {
+              const uint32_t w = *reinterpret_cast<const uint32_t *>(sm + (size_t)sl * G::SLOT_BYTES + mbyte);
+              act = !((w >> mshift) & 1u);
+            }
+            if (act) {
+              const T gv = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
+              const T nv = MODE == MODE_REPLACE ? vmin<T, ARITH>(capq[0], gv) : vmin<T, ARITH>(cv, gv);
+              if (vdiffers<T, ARITH>(nv, cv)) {
+                cur[orow] = nv;
+                u[(long long)gz_of(lz) * plane + grow] = nv;
+                tmax = vmax_nonneg<T, ARITH>(tmax, node_change<T, ARITH>(cv, nv, hmin));
+                fence_proxy_async();  // this store comes before a later TMA write into the slot
+              }
+            }
+          }
+          if (MODE == MODE_REPLACE) {
+#pragma unroll
+            for (int q = 0; q + 1 < CP; ++q) capq[q] = capq[q + 1];
+            capq[CP - 1] = cap_at(lz + CP);
+          }
+        }
+        sl = sl == D - 1 ? 0 : sl + 1;
+      }
+      compute_bar();
+      if (tid == 0 && !s_stop) st_release_cta_s(&s_done, t_end);
+    }
+    __syncthreads();
+    if (s_abort) break;
+  }
+  // the CTA's max change -> the grid's counter (one atomic per warp)
+  T v = tmax;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(0xffffffffu, v, off));
+  if (lane == 0 && change_pos<T, ARITH>(v)) {
+    if constexpr (sizeof(T) == 4)
+      atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint(v));
+    else
+      atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg), change_u64<T, ARITH>(v));
+  }
+}
+
+}  // namespace pdfs

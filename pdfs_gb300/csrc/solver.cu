@@ -276,9 +276,9 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4);
   // bricks (tile 5) for every arithmetic
   if (o->arith == PDFS_ARITH_PAIR) {
-    if (t64 != 0 && t64 != 5) return PDFS_ERR_INVALID;  // FP32 pairs: bricks only
+    if (t64 != 0 && t64 != 5 && t64 != 6) return PDFS_ERR_INVALID;  // FP32 pairs: bricks and pencils
   } else if (o->arith == PDFS_ARITH_MIXED) {
-    if (t64 != 0 && t64 != 1 && t64 != 4 && t64 != 5) return PDFS_ERR_INVALID;
+    if (t64 != 0 && t64 != 1 && t64 != 4 && t64 != 5 && t64 != 6) return PDFS_ERR_INVALID;
   } else {
     if (t64 == 4 && o->arith != PDFS_ARITH_FAST) return PDFS_ERR_INVALID;
     if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 == 3) return PDFS_ERR_INVALID;
@@ -615,7 +615,9 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
 
   const int tile = f32 ? c->t32 : c->t64;
   const TileShape ts = f32 ? tile32(tile) : tile64(tile);
-  if (ts.bz == 0) CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
+  // pencils sweep unmasked sweeps; a block mask or block-change output goes to bricks
+  const bool pencil = ts.pencil && !active && !blk_chg;
+  if (ts.bz == 0 || pencil) CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
   if (blk_chg) CK(cudaMemsetAsync(blk_chg, 0, (size_t)c->nblocks * 4, c->st));
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
@@ -625,7 +627,9 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
                                                        : ARITH_FAST;
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
-  if (ts.bz > 0) {
+  if (pencil) {
+    CK(launch_sweep_pencils(which, arith, iso, a, L, c->sms, c->st, &grid));
+  } else if (ts.bz > 0) {
     a.epoch = ++c->epoch;  // the flags of every earlier sweep are below it
     CK(launch_sweep_bricks(which, ts.bz, arith, iso, a, L, c->sms, c->st, &grid));
   } else {

@@ -11,10 +11,12 @@ namespace pdfs {
 // Tile variants.  Columns (sweep.cuh) are 32 nodes wide (one warp lane per
 // x); TY rows, R rows per compute warp: {tx, ty, rows per warp}.  Bricks
 // (tile3d.cuh) are 16 x 16 x BZ: {16, 16, 0, BZ}.
-static const TileShape kT32[] = {{32, 8, 2},  {32, 8, 4}, {32, 16, 4}, {32, 8, 1},      {32, 4, 2},
-                                 {32, 6, 1},  {32, 10, 1}, {16, 16, 0, 16}, {16, 16, 0, 32}};
+// Pencils (pencil.cuh) are 16 x 16 cross-sections marched along z: {16, 16,
+// 0, 16, 1}; their block-masked sweeps run on 16 x 16 x 16 bricks.
+static const TileShape kT32[] = {{32, 8, 2},  {32, 8, 4},  {32, 16, 4},     {32, 8, 1},      {32, 4, 2},
+                                 {32, 6, 1},  {32, 10, 1}, {16, 16, 0, 16}, {16, 16, 0, 32}, {16, 16, 0, 16, 1}};
 // tile 4 (32 x 6, one row per warp) exists for the fast and mixed arithmetic
-static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}, {32, 6, 1}, {16, 16, 0, 16}};
+static const TileShape kT64[] = {{32, 4, 1}, {32, 4, 2}, {32, 8, 2}, {32, 6, 1}, {16, 16, 0, 16}, {16, 16, 0, 16, 1}};
 
 int tile_count32() { return (int)(sizeof(kT32) / sizeof(kT32[0])); }
 int tile_count64() { return (int)(sizeof(kT64) / sizeof(kT64[0])); }
@@ -51,7 +53,7 @@ cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout
 
 // Frozen-mask map: 32-bit words, dims {fy, fw, nz+2}, box {MBOX, 1, 1} (the
 // column's TY rows rounded up to a 16-byte box).
-static cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty) {
+cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty) {
   auto fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
   cuuint64_t dims[3] = {(cuuint64_t)a.mask_fy, (cuuint64_t)a.mask_fw, (cuuint64_t)(a.nz + 2)};

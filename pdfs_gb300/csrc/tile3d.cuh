@@ -283,9 +283,11 @@ __global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ C
               u[gbase + (long long)gz * plane] = nv;
               const T d = node_change<T, ARITH>(cv, nv, hmin);
               tmax = vmax_nonneg<T, ARITH>(tmax, d);
+              if (blk_chg) {
 #pragma unroll
-              for (int q = 0; q < NZB; ++q)
-                if ((gz >> 3) == q) accb[q] = vmax_nonneg<T, ARITH>(accb[q], d);
+                for (int q = 0; q < NZB; ++q)
+                  if ((gz >> 3) == q) accb[q] = vmax_nonneg<T, ARITH>(accb[q], d);
+              }
             }
           }
         }
@@ -317,10 +319,13 @@ __global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ C
         }
       }
     }
-    // publish: every store of the brick is visible before the flag
-    __threadfence();
+    // publish: the barrier orders every thread's stores before thread 0's
+    // GPU-scope fence, which orders them before the flag
     __syncthreads();
-    if (tid == 0 && tile != a.poison_col) st_release_gpu(a.tflag + tile, epoch);
+    if (tid == 0) {
+      __threadfence();
+      if (tile != a.poison_col) st_release_gpu(a.tflag + tile, epoch);
+    }
   }
   // the CTA's max change -> the grid's counter (one atomic per warp)
   {

@@ -18,6 +18,8 @@ pytestmark = pytest.mark.gpu
 
 B64 = 5 << 8     # FP64 bricks, 16 x 16 x 16
 B32 = (8, 9)     # FP32 bricks, 16 x 16 x 16 and 16 x 16 x 32
+P64 = 6 << 8     # FP64 pencils, 16 x 16 along z (block-masked sweeps on bricks)
+P32 = 10         # FP32 pencils
 
 
 def same(a, b):
@@ -33,29 +35,92 @@ SHAPES = [(1, 1, 1), (2, 3, 5), (16, 16, 16), (17, 16, 15), (1, 40, 1), (70, 1, 
           (65, 31, 47), (48, 50, 35)]
 
 
+@pytest.mark.parametrize("tile", [B64, P64])
 @pytest.mark.parametrize("shape", SHAPES)
-def test_bricks_bit_exact_odd_shapes(shape):
+def test_bricks_bit_exact_odd_shapes(shape, tile):
     nx, ny, nz = shape
     f = W.random_field(nx, ny, nz, seed=nx * 5 + ny * 11 + nz, frac_known=0.1)
     for sp in [(1.0, 1.0, 1.0), (0.7, 1.3, 0.4)]:
         a, b = f.copy(), f.copy()
         s, _ = O.solve(b, sp, tol=0.0, threads=8)
-        st = api.solve(a, sp, tol=0.0, tile=B64)
+        st = api.solve(a, sp, tol=0.0, tile=tile)
         assert same(a, b)
         assert st["sweeps_fp64"] == s
-        assert st["tile"] >> 8 == 5
+        assert st["tile"] >> 8 == tile >> 8
 
 
+@pytest.mark.parametrize("tile", [B64, P64])
 @pytest.mark.parametrize("sn", range(1, 9))
-def test_brick_orderings_multisphere_frozen(sn):
+def test_brick_orderings_multisphere_frozen(sn, tile):
     """One sweep of each ordering on a frozen-mask multi-sphere grid whose
-    sizes are not brick multiples."""
+    sizes are not brick or pencil multiples."""
     w = W.random_spheres(75, 41, 38, 1.0, 1.0, 0.5, 6, 3.0, 12.0, seed=40 + sn)
     sp = (w.dx, w.dy, w.dz)
     a, b = w.field.copy(), w.field.copy()
-    api.sweep(a, sp, sn, frozen=w.frozen, freeze=L.FREEZE_MASK, tile=B64)
+    api.sweep(a, sp, sn, frozen=w.frozen, freeze=L.FREEZE_MASK, tile=tile)
     O.sweep(b, sp, sn, frozen=w.frozen)
     assert same(a, b)
+
+
+@pytest.mark.parametrize("tall", [False, True])
+def test_pencil_fp32_equals_column_fp32(tall):
+    """FP32 solves on pencils and on 32 x 8 columns agree bit for bit (a
+    tall grid recycles every ring slot many times)."""
+    nz = 300 if tall else 40
+    w = W.random_spheres(50, 37, nz, 1.0, 1.0, 1.0, 6, 3.0, 12.0, seed=17)
+    sp = (w.dx, w.dy, w.dz)
+    out = []
+    for t in (P32, 4):
+        a = w.field.copy()
+        st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32, tile=t)
+        out.append((a, st["sweeps_fp32"]))
+    assert same(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+
+
+@pytest.mark.parametrize("arith", [L.ARITH_MIXED, L.ARITH_PAIR])
+def test_pencil_polish_equals_bricks(arith):
+    """The polish on pencils and on bricks: the same topological order
+    class, so the same bits."""
+    w = W.random_spheres(70, 66, 90, 1.0, 1.0, 0.5, 8, 3.0, 14.0, seed=78)
+    sp = (w.dx, w.dy, w.dz)
+    out = []
+    for tile in (P32 | P64, 9 | B64):
+        a = w.field.copy()
+        api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=arith,
+                  tol=1e-6 * min(sp), max_sweeps=200, tile=tile)
+        out.append(a)
+    assert same(out[0], out[1])
+
+
+def test_pencil_bounded_wait_times_out_cleanly(monkeypatch):
+    w = W.random_spheres(64, 64, 48, 1.0, 1.0, 1.0, 4, 3.0, 10.0, seed=2)
+    sp = (w.dx, w.dy, w.dz)
+    monkeypatch.setenv("PDFS_TEST_POISON_COLUMN", "0")
+    a = w.field.copy()
+    with pytest.raises(api.PdfsError) as ei:
+        api.solve(a, sp, tol=0.0, wait_ms=200, tile=P64)
+    assert ei.value.status == L.PDFS_ERR_TIMEOUT
+    monkeypatch.delenv("PDFS_TEST_POISON_COLUMN")
+    a, b = w.field.copy(), w.field.copy()
+    api.solve(a, sp, tol=0.0, tile=P64)
+    O.solve(b, sp, tol=0.0, threads=8)
+    assert same(a, b)
+
+
+@pytest.mark.parametrize("sched", [L.SCHED_CHANGE, L.SCHED_LEARNED])
+def test_pencil_tiles_with_schedulers(sched):
+    """Scheduled solves on pencil tiles: full sweeps record block changes and
+    masked sweeps skip blocks, both on bricks; the fixed point is the plain one."""
+    w = W.random_spheres(96, 80, 72, 1.0, 1.0, 1.0, 6, 3.0, 16.0, seed=5)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, arith=L.ARITH_FAST, tol=0.0,
+                   scheduler=sched, tile=P64)
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    h = min(sp)
+    err = float(np.max(np.abs(inner(a) - inner(b)) / np.maximum(np.abs(inner(b)), h)))
+    assert err <= 1e-13, err
+    assert st["blocks_skipped"] > 0
 
 
 @pytest.fixture(scope="module", params=[37, 150])

@@ -36,8 +36,8 @@ def rel_err(a, b, h):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), h)))
 
 
-TILES64 = [t << 8 for t in (1, 2, 3, 5)]  # 5: 16 x 16 x 16 bricks
-TILES32 = [1, 2, 3, 4, 5, 6, 7, 8, 9]     # 8, 9: bricks 16 x 16 x 16 and 16 x 16 x 32
+TILES64 = [t << 8 for t in (1, 2, 3, 5, 6)]  # 5: 16 x 16 x 16 bricks, 6: 16 x 16 pencils
+TILES32 = [1, 2, 3, 4, 5, 6, 7, 8, 9, 10]    # 8, 9: bricks 16 x 16 x 16 and x 32; 10: pencils
 
 
 def test_godunov_known_answers_on_gpu():
