@@ -272,13 +272,14 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
     return PDFS_ERR_INVALID;
   const int t32 = o->tile & 0xff, t64 = (o->tile >> 8) & 0xff;
   if (t32 > tile_count32() || t64 > tile_count64()) return PDFS_ERR_INVALID;
-  // FP64 kernels: tiles 1 and 4 for the mixed arithmetic; 1-3 for the
+  // FP64 kernels: columns 1 and 4 for the mixed arithmetic; 1-3 for the
   // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4);
-  // bricks (tile 5) for every arithmetic
+  // bricks (5: 16 x 16 x 16, 7: 16 x 16 x 32) and pencils (6) for every
+  // arithmetic; FP32 pairs on bricks and pencils only
   if (o->arith == PDFS_ARITH_PAIR) {
-    if (t64 != 0 && t64 != 5 && t64 != 6) return PDFS_ERR_INVALID;  // FP32 pairs: bricks and pencils
+    if (t64 != 0 && t64 < 5) return PDFS_ERR_INVALID;  // FP32 pairs: bricks and pencils
   } else if (o->arith == PDFS_ARITH_MIXED) {
-    if (t64 != 0 && t64 != 1 && t64 != 4 && t64 != 5 && t64 != 6) return PDFS_ERR_INVALID;
+    if (t64 == 2 || t64 == 3) return PDFS_ERR_INVALID;
   } else {
     if (t64 == 4 && o->arith != PDFS_ARITH_FAST) return PDFS_ERR_INVALID;
     if (o->precision == PDFS_PREC_FP32_POLISH64 && t64 == 3) return PDFS_ERR_INVALID;

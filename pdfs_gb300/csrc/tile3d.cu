@@ -47,7 +47,7 @@ static cudaError_t dispatch_t3(int which, int arith, bool iso, const SweepArgs &
   if (which == 0)
     return iso ? launch_t3<float, BZ, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)
                : launch_t3<float, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
-  if constexpr (BZ == 16) {
+  {
     if (which == 1) {
       if (arith == ARITH_REF) return launch_t3<double, BZ, MODE_MIN, ARITH_REF, false>(a, L, sms, st, g);
       if (arith == ARITH_FAST) return launch_t3<double, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
@@ -65,7 +65,6 @@ static cudaError_t dispatch_t3(int which, int arith, bool iso, const SweepArgs &
     return iso ? launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, true>(a, L, sms, st, g)
                : launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, false>(a, L, sms, st, g);
   }
-  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_sweep_bricks(int which, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
