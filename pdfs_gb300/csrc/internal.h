@@ -56,10 +56,10 @@ TileShape tile64(int id);
 // (cap = upper bound field in the same layout).
 cudaError_t launch_sweep(int which, int tile, int arith, bool iso, const SweepArgs &a, const Layout &L,
                          const void *cap, int sms, cudaStream_t st, int *grid_used);
-// One sweep by the brick kernel (tile3d.cu): bricks of 16 x 16 x bz, a.tflag /
+// One sweep by the brick kernel (tile3d.cu): bricks of 16 x by x bz, a.tflag /
 // a.torder / a.ntx.. / a.epoch filled in.
-cudaError_t launch_sweep_bricks(int which, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
-                                cudaStream_t st, int *grid_used);
+cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L,
+                                int sms, cudaStream_t st, int *grid_used);
 // One unmasked sweep by the pencil kernel (pencil.cu): 16 x 16 pencils, the
 // column order / progress words of a 16 x 16 layout.
 cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,

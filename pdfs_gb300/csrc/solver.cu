@@ -632,7 +632,7 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
     CK(launch_sweep_pencils(which, arith, iso, a, L, c->sms, c->st, &grid));
   } else if (ts.bz > 0) {
     a.epoch = ++c->epoch;  // the flags of every earlier sweep are below it
-    CK(launch_sweep_bricks(which, ts.bz, arith, iso, a, L, c->sms, c->st, &grid));
+    CK(launch_sweep_bricks(which, ts.ty, ts.bz, arith, iso, a, L, c->sms, c->st, &grid));
   } else {
     CK(launch_sweep(which, tile, arith, iso, a, L, which == 2 ? (const void *)c->in64 : nullptr, c->sms, c->st,
                     &grid));

@@ -19,10 +19,10 @@ std::vector<int> brick_order(int ntx, int nty, int ntz) {
   return o;
 }
 
-template <class T, int BZ, int MODE, int ARITH, bool ISO>
+template <class T, int BY, int BZ, int MODE, int ARITH, bool ISO>
 static cudaError_t launch_t3(const SweepArgs &a, const Layout &L, int sms, cudaStream_t st, int *grid_used) {
-  using G = T3Geo<T, BZ>;
-  auto kern = t3_sweep_kernel<T, BZ, MODE, ARITH, ISO>;
+  using G = T3Geo<T, BY, BZ>;
+  auto kern = t3_sweep_kernel<T, BY, BZ, MODE, ARITH, ISO>;
   CUtensorMap m;
   cudaError_t e = encode_field_map(&m, a.u, sizeof(T), L, a.nz + 2, G::W, G::RY, G::RZ);
   if (e != cudaSuccess) return e;
@@ -41,37 +41,41 @@ static cudaError_t launch_t3(const SweepArgs &a, const Layout &L, int sms, cudaS
   return cudaGetLastError();
 }
 
-template <int BZ>
+template <int BY, int BZ>
 static cudaError_t dispatch_t3(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
                                cudaStream_t st, int *g) {
   if (which == 0)
-    return iso ? launch_t3<float, BZ, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)
-               : launch_t3<float, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
+    return iso ? launch_t3<float, BY, BZ, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)
+               : launch_t3<float, BY, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
   {
     if (which == 1) {
-      if (arith == ARITH_REF) return launch_t3<double, BZ, MODE_MIN, ARITH_REF, false>(a, L, sms, st, g);
-      if (arith == ARITH_FAST) return launch_t3<double, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
+      if (arith == ARITH_REF) return launch_t3<double, BY, BZ, MODE_MIN, ARITH_REF, false>(a, L, sms, st, g);
+      if (arith == ARITH_FAST) return launch_t3<double, BY, BZ, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
       if (arith == ARITH_PAIR)
-        return iso ? launch_t3<double, BZ, MODE_MIN, ARITH_PAIR, true>(a, L, sms, st, g)
-                   : launch_t3<double, BZ, MODE_MIN, ARITH_PAIR, false>(a, L, sms, st, g);
-      return iso ? launch_t3<double, BZ, MODE_MIN, ARITH_MIXED, true>(a, L, sms, st, g)
-                 : launch_t3<double, BZ, MODE_MIN, ARITH_MIXED, false>(a, L, sms, st, g);
+        return iso ? launch_t3<double, BY, BZ, MODE_MIN, ARITH_PAIR, true>(a, L, sms, st, g)
+                   : launch_t3<double, BY, BZ, MODE_MIN, ARITH_PAIR, false>(a, L, sms, st, g);
+      return iso ? launch_t3<double, BY, BZ, MODE_MIN, ARITH_MIXED, true>(a, L, sms, st, g)
+                 : launch_t3<double, BY, BZ, MODE_MIN, ARITH_MIXED, false>(a, L, sms, st, g);
     }
-    if (arith == ARITH_REF) return launch_t3<double, BZ, MODE_REPLACE, ARITH_REF, false>(a, L, sms, st, g);
-    if (arith == ARITH_FAST) return launch_t3<double, BZ, MODE_REPLACE, ARITH_FAST, false>(a, L, sms, st, g);
+    if (arith == ARITH_REF) return launch_t3<double, BY, BZ, MODE_REPLACE, ARITH_REF, false>(a, L, sms, st, g);
+    if (arith == ARITH_FAST) return launch_t3<double, BY, BZ, MODE_REPLACE, ARITH_FAST, false>(a, L, sms, st, g);
     if (arith == ARITH_PAIR)
-      return iso ? launch_t3<double, BZ, MODE_REPLACE, ARITH_PAIR, true>(a, L, sms, st, g)
-                 : launch_t3<double, BZ, MODE_REPLACE, ARITH_PAIR, false>(a, L, sms, st, g);
-    return iso ? launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, true>(a, L, sms, st, g)
-               : launch_t3<double, BZ, MODE_REPLACE, ARITH_MIXED, false>(a, L, sms, st, g);
+      return iso ? launch_t3<double, BY, BZ, MODE_REPLACE, ARITH_PAIR, true>(a, L, sms, st, g)
+                 : launch_t3<double, BY, BZ, MODE_REPLACE, ARITH_PAIR, false>(a, L, sms, st, g);
+    return iso ? launch_t3<double, BY, BZ, MODE_REPLACE, ARITH_MIXED, true>(a, L, sms, st, g)
+               : launch_t3<double, BY, BZ, MODE_REPLACE, ARITH_MIXED, false>(a, L, sms, st, g);
   }
 }
 
-cudaError_t launch_sweep_bricks(int which, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
-                                cudaStream_t st, int *g) {
-  if (!a.tflag || !a.torder || a.ntx < 1 || a.nty < 1 || a.ntz < 1) return cudaErrorInvalidValue;
-  if (bz == 16) return dispatch_t3<16>(which, arith, iso, a, L, sms, st, g);
-  if (bz == 32) return dispatch_t3<32>(which, arith, iso, a, L, sms, st, g);
+cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L,
+                                int sms, cudaStream_t st, int *g) {
+  if (!a.tflag || !a.torder || a.ntx < 1 || a.nty < 1 || a.ntz < 1 || L.ty != by) return cudaErrorInvalidValue;
+  if (by == 16 && bz == 16) return dispatch_t3<16, 16>(which, arith, iso, a, L, sms, st, g);
+  if (by == 16 && bz == 32) return dispatch_t3<16, 32>(which, arith, iso, a, L, sms, st, g);
+  if (by == 8 && bz == 32) return dispatch_t3<8, 32>(which, arith, iso, a, L, sms, st, g);
+  if (by == 8 && bz == 48 && which == 0)  // FP32 only
+    return iso ? launch_t3<float, 8, 48, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)
+               : launch_t3<float, 8, 48, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
   return cudaErrorInvalidValue;
 }
 

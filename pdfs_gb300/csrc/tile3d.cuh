@@ -1,4 +1,4 @@
-// tile3d.cuh -- the 3-D tile sweep: each CTA sweeps a 16 x 16 x BZ brick of
+// tile3d.cuh -- the 3-D tile sweep: each CTA sweeps a 16 x BY x BZ brick of
 // the grid held whole in shared memory, hyperplane by hyperplane.
 //
 // The reference sweeps one hyperplane x+y+z = level of the whole grid per
@@ -38,9 +38,9 @@
 
 namespace pdfs {
 
-template <class T, int BZ>
+template <class T, int BY_, int BZ>
 struct T3Geo {
-  static constexpr int BX = 16, BY = 16;
+  static constexpr int BX = 16, BY = BY_;
   static constexpr int V = 16 / (int)sizeof(T);
   static constexpr int W = BX + 2 * V;    // box row: x0-V .. x0+BX+V-1 (16-byte aligned start)
   static constexpr int RY = BY + 2;       // box rows: y0-1 .. y0+BY
@@ -54,7 +54,8 @@ struct T3Geo {
   static constexpr size_t OFF_MASK = ((size_t)BOX_BYTES + 127) & ~size_t(127);
   static constexpr size_t OFF_BAR = OFF_MASK + (size_t)BZ * BY * 4;
   static constexpr size_t BYTES = OFF_BAR + 16;
-  static_assert(BZ % 8 == 0, "bricks hold whole 8^3 blocks in z");
+  static_assert(BZ % 8 == 0 && BY % 8 == 0, "bricks hold whole 8^3 blocks");
+  static constexpr int NBX = BX / 8, NBY = BY / 8;  // 8^3 blocks per brick in x and y
   static_assert((W * sizeof(T)) % 16 == 0, "TMA rows are 16-byte multiples");
 };
 
@@ -62,10 +63,10 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
-template <class T, int BZ, int MODE, int ARITH, bool ISO>
-__global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
-                                                       const __grid_constant__ SweepArgs a) {
-  using G = T3Geo<T, BZ>;
+template <class T, int BY_, int BZ, int MODE, int ARITH, bool ISO>
+__global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
+                                                            const __grid_constant__ SweepArgs a) {
+  using G = T3Geo<T, BY_, BZ>;
   constexpr int BX = G::BX, BY = G::BY, V = G::V, W = G::W, PL = G::PL, NL = G::NL, NZB = G::NZB, CP = G::CP;
   extern __shared__ __align__(1024) unsigned char sm[];
   T *box = reinterpret_cast<T *>(sm);
@@ -127,8 +128,9 @@ __global__ void __launch_bounds__(256) t3_sweep_kernel(const __grid_constant__ C
     bool run = true;
     if (blk_active) {
       bool act = false;
-      if (tid < 4 * NZB) {
-        const int bx = 2 * bi + (tid & 1), by = 2 * bj + ((tid >> 1) & 1), bz = bk * NZB + (tid >> 2);
+      if (tid < G::NBX * G::NBY * NZB) {
+        const int bx = G::NBX * bi + tid % G::NBX, by = G::NBY * bj + (tid / G::NBX) % G::NBY;
+        const int bz = bk * NZB + tid / (G::NBX * G::NBY);
         if (bx < a.nbx && by < a.nby && bz < a.nbz)
           act = __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0;
       }

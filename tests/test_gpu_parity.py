@@ -36,8 +36,10 @@ def rel_err(a, b, h):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), h)))
 
 
-TILES64 = [t << 8 for t in (1, 2, 3, 5, 6, 7)]  # bricks 5: 16 x 16 x 16, 7: x 32; 6: pencils
-TILES32 = [1, 2, 3, 4, 5, 6, 7, 8, 9, 10]    # 8, 9: bricks 16 x 16 x 16 and x 32; 10: pencils
+# FP64 bricks 5: 16 x 16 x 16, 7: 16 x 16 x 32, 8: 16 x 8 x 32; 6: pencils
+TILES64 = [t << 8 for t in (1, 2, 3, 5, 6, 7, 8)]
+# FP32 bricks 8: 16 x 16 x 16, 9: 16 x 16 x 32, 11: 16 x 8 x 48; 10: pencils
+TILES32 = [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11]
 
 
 def test_godunov_known_answers_on_gpu():
