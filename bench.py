@@ -166,15 +166,21 @@ def peaks():
         return {}
 
 
-# sweep kernel variants by tile id: columns (TY, rows per warp) or bricks (BZ)
+# sweep kernel variants by tile id: columns (TY, rows per warp), bricks (BY, BZ), pencils
 COLUMNS32 = {1: (8, 2), 2: (8, 4), 3: (16, 4), 4: (8, 1), 5: (4, 2), 6: (6, 1), 7: (10, 1)}
 COLUMNS64 = {1: (4, 1), 2: (4, 2), 3: (8, 2), 4: (6, 1)}
-BRICKS32 = {8: 16, 9: 32}
-BRICKS64 = {5: 16}
+BRICKS32 = {8: (16, 16), 9: (16, 32), 11: (8, 48)}
+BRICKS64 = {5: (16, 16), 7: (16, 32), 8: (8, 32)}
+PENCILS32, PENCILS64 = (10,), (6,)
 
 
-def is_brick(kind, tile):
-    return (tile & 0xff) in BRICKS32 if kind == "fp32" else (tile >> 8) in BRICKS64
+def kernel_kind(kind, tile):
+    t = tile & 0xff if kind == "fp32" else tile >> 8
+    if t in (BRICKS32 if kind == "fp32" else BRICKS64):
+        return "brick"
+    if t in (PENCILS32 if kind == "fp32" else PENCILS64):
+        return "pencil"
+    return "column"
 
 
 def kernel_name(kind, tile, prec, arith):
@@ -184,10 +190,14 @@ def kernel_name(kind, tile, prec, arith):
     ar = "FAST" if kind == "fp32" else {L.ARITH_MIXED: "MIXED", L.ARITH_PAIR: "PAIR",
                                         L.ARITH_FAST: "FAST"}.get(arith, "REF")
     t = "float" if kind == "fp32" else "double"
-    if is_brick(kind, tile):
-        bz = BRICKS32[tile & 0xff] if kind == "fp32" else BRICKS64[tile >> 8]
-        return "t3_sweep_kernel<%s, %d, %s, %s>" % (t, bz, mode, ar)
-    ty = COLUMNS32.get(tile & 0xff, (0, 0)) if kind == "fp32" else COLUMNS64.get(tile >> 8, (0, 0))
+    tid = tile & 0xff if kind == "fp32" else tile >> 8
+    k = kernel_kind(kind, tile)
+    if k == "brick":
+        by, bz = (BRICKS32 if kind == "fp32" else BRICKS64)[tid]
+        return "t3_sweep_kernel<%s, %d, %d, %s, %s>" % (t, by, bz, mode, ar)
+    if k == "pencil":
+        return "pc_sweep_kernel<%s, %s, %s>" % (t, mode, ar)
+    ty = (COLUMNS32 if kind == "fp32" else COLUMNS64).get(tid, (0, 0))
     return "ws_sweep_kernel<%s, %d, %d, %s, %s>" % ((t,) + ty + (mode, ar))
 
 
@@ -202,8 +212,9 @@ def traffic_per_launch(kind, prec, nodes, tile):
     except (OSError, ValueError):
         return None
     key = "fp32" if kind == "fp32" else ("fp64_replace" if prec == L.PREC_FP32_POLISH64 else "fp64_min")
-    if is_brick(kind, tile):
-        key += "_brick"
+    k = kernel_kind(kind, tile)
+    if k != "column":
+        key += "_" + k
     e = t.get(key)
     return None if not e else float(e["dram_bytes_per_update"]) * nodes
 
