@@ -78,7 +78,10 @@ enum {
                              predicts will change                                         */
 };
 /* Whatever the scheduler, a solve only terminates after a sweep that visits
- * every block and changes nothing (FP32) or less than tol (FP64). */
+ * every block and changes nothing (FP32) or less than tol (FP64).  Under
+ * PDFS_PREC_FP32_POLISH64 the scheduler runs the FP32 phase, which may then
+ * end on a quiet scheduled sweep, and the polish visits every block: its
+ * full sweeps certify the fixed point. */
 
 typedef struct {
   int precision;         /* PDFS_PREC_*                                           */

@@ -719,10 +719,15 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   // replace-update).  tol bounds the phase's change metric.  With a
   // scheduler, the first round and every judging sweep visit all blocks;
   // the phase ends only at a full sweep whose change is <= tol.
+  // FP32 + polish: the polish's full sweeps certify the fixed point, so the
+  // FP32 phase may end on a quiet scheduled sweep (no judging sweep), and the
+  // polish -- one full cycle and a certifying sweep -- visits every block.
+  const bool polish = o.precision == PDFS_PREC_FP32_POLISH64;
   auto phase = [&](int which, double tol, int *count, double *ms, double *kms) -> int {
     c->kern_ms = 0.0;
     CK(cudaEventRecord(c->e0, c->st));
-    const bool sched = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0;
+    const bool sched = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0 && !(polish && which == 2);
+    const bool certify = !(polish && which == 0);  // must the phase end on a full sweep?
     const float thr = (float)tol;
     // per-block changes: ring slot cur = this sweep, (cur - k) mod kRing = k sweeps ago
     int cur = 0;
@@ -779,7 +784,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         st.voxel_updates += (long long)((double)nodes * (double)nact / (double)c->nblocks);
         st.blocks_skipped += c->nblocks - nact;
       }
-      if (o.fixed_sweeps == 0 && full && chg <= tol) break;
+      if (o.fixed_sweeps == 0 && (full || !certify) && chg <= tol) break;
       need_full = !full && chg <= tol;  // a quiet skipped sweep calls for a judging full sweep
       cur = (cur + 1) % kRing;          // this sweep's changes become history
     }

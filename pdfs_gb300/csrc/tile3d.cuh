@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
   T *box = reinterpret_cast<T *>(sm);
   uint32_t *smask = reinterpret_cast<uint32_t *>(sm + G::OFF_MASK);  // [BZ][BY] frozen words of the brick
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm + G::OFF_BAR);
-  __shared__ int s_next;
+  __shared__ int s_next, s_lo, s_hi;  // s_lo / s_hi: a masked brick's active planes (sweep order)
   __shared__ volatile int s_abort;
 
   if ((saddr(sm) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
@@ -112,6 +112,10 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
   unsigned par = 0;  // phase parity of the box barrier
   for (;;) {
     const int tk = s_next;
+    if (tid == 0) {
+      s_lo = BZ;
+      s_hi = -1;
+    }
     // a uniform decision (s_abort may change under the reads); the barrier
     // also orders every read of s_next before its next write
     if (__syncthreads_or(tk >= ntile || s_abort)) break;
@@ -124,17 +128,27 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     const int x0 = 1 + bi * BX, y0 = 1 + bj * BY, z0 = 1 + bk * BZ;
 
     // block mask: a brick none of whose 8^3 blocks is active keeps its values
-    // and publishes at once (its faces are the old values its neighbours need)
+    // and publishes at once (its faces are the old values its neighbours need);
+    // otherwise only the levels that reach its active planes run
     bool run = true;
+    int lev0 = 0, lev1 = NL;  // levels [lev0, lev1) of this brick
     if (blk_active) {
       bool act = false;
       if (tid < G::NBX * G::NBY * NZB) {
+        const int q = tid / (G::NBX * G::NBY);
         const int bx = G::NBX * bi + tid % G::NBX, by = G::NBY * bj + (tid / G::NBX) % G::NBY;
-        const int bz = bk * NZB + tid / (G::NBX * G::NBY);
+        const int bz = bk * NZB + q;
         if (bx < a.nbx && by < a.nby && bz < a.nbz)
           act = __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0;
+        if (act) {  // the block's planes 8q .. 8q+7 (grid order) in sweep order
+          const int lo = szd > 0 ? 8 * q : BZ - 8 * q - 8;
+          atomicMin(&s_lo, lo);
+          atomicMax(&s_hi, lo + 7);
+        }
       }
       run = __syncthreads_or(act) != 0;
+      lev0 = s_lo;                        // thread (0, 0) reaches the first active plane
+      lev1 = min(NL, s_hi + BX + BY - 1);  // thread (15, 15) leaves the last one
     }
     if (tid == 32) s_next = atomicAdd(a.ticket, 1);  // the next brick's ticket, fetched ahead
     if (!run) {
@@ -176,15 +190,16 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       }
     }
     const long long gbase = (long long)z0 * plane + (long long)(y0 + gyl) * px + (x0 + gxl) + (V - 1);
-    // replace-update caps of my first CP nodes (sweep order)
+    // replace-update caps of my first CP nodes (sweep order) from the first level run
     T capq[CP];
     auto cap_at = [&](int lz) -> T {
       const int gz = szd > 0 ? lz : BZ - 1 - lz;
       if (MODE != MODE_REPLACE || !vxy || lz >= BZ || gz >= zcnt) return T(0);
       return __ldg(capg + gbase + (long long)gz * plane);
     };
+    const int lz_first = max(0, lev0 - (lx + ly));
 #pragma unroll
-    for (int q = 0; q < CP; ++q) capq[q] = cap_at(q);
+    for (int q = 0; q < CP; ++q) capq[q] = cap_at(lz_first + q);
 
     // wait for the upwind bricks (lanes 0..2 of warp 0, one each)
     bool ok = true;
@@ -264,7 +279,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
 #pragma unroll
     for (int q = 0; q < NZB; ++q) accb[q] = T(0);
     const int lxy = lx + ly;
-    for (int L = 0; L < NL; ++L) {
+    for (int L = lev0; L < lev1; ++L) {
       const int lz = L - lxy;
       if ((unsigned)lz < (unsigned)BZ) {
         const int gz = szd > 0 ? lz : BZ - 1 - lz;
