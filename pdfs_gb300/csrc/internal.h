@@ -14,15 +14,19 @@ namespace pdfs {
 
 // Internal padded layout of one element type for one tile shape
 // (see sweep.cuh for the indexing rule).
+// xo is the x offset of the index: V - 1 for the column kernels (interior x =
+// 1 + tx*cx on a 16-byte boundary), 0 for bricks and pencils (their boxes
+// start at the halo node x0 - 1 = 16*cx, on a 16-byte boundary).
 struct Layout {
-  int tx = 0, ty = 0, V = 0, esize = 0;
+  int tx = 0, ty = 0, V = 0, esize = 0, xo = 0;
   int ncx = 0, ncy = 0;
   long long px = 0, ry = 0, plane = 0;
   size_t elems = 0;  // total elements including padding
-  __host__ __device__ long long index(int x, int y, int z) const { return (long long)z * plane + (long long)y * px + x + (V - 1); }
+  __host__ __device__ long long index(int x, int y, int z) const { return (long long)z * plane + (long long)y * px + x + xo; }
 };
 
-Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize);
+// xo < 0: the column kernels' offset V - 1
+Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize, int xo = -1);
 
 // Frozen bitmask layout, independent of the tile: node (x, y, z) is bit
 // (x-1)%32 of word z*fplane + ((x-1)/32)*fy + (y-1).  The rows of one 32-wide

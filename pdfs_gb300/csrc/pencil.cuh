@@ -35,8 +35,9 @@ namespace pdfs {
 template <class T>
 struct PcGeo {
   static constexpr int BX = 16, BY = 16;
-  static constexpr int V = 16 / (int)sizeof(T);
-  static constexpr int W = BX + 2 * V;     // slot row: x0-V .. x0+BX+V-1 (16-byte aligned start)
+  // slot row: x0-1 .. x0+BX rounded up to 16 bytes (the field's index has no x
+  // offset, so x0 - 1 = 16*cx starts the row on a 16-byte boundary)
+  static constexpr int W = (int)((((BX + 2) * sizeof(T)) + 15) / 16 * 16 / sizeof(T));
   static constexpr int RY = BY + 2;        // slot rows: y0-1 .. y0+BY
   static constexpr int SK = BX + BY - 2;   // thread (15, 15) trails thread (0, 0) by SK planes
   static constexpr int LOOK = sizeof(T) == 4 ? 5 : 3;  // planes requested ahead of use
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
                                                                const __grid_constant__ CUtensorMap tm_mask,
                                                                const __grid_constant__ SweepArgs a) {
   using G = PcGeo<T>;
-  constexpr int BX = G::BX, BY = G::BY, V = G::V, W = G::W, SK = G::SK, D = G::D, CP = G::CP;
+  constexpr int BX = G::BX, BY = G::BY, W = G::W, SK = G::SK, D = G::D, CP = G::CP;
   constexpr int SE = (int)(G::SLOT_BYTES / sizeof(T));  // slot stride in elements
   extern __shared__ __align__(1024) unsigned char sm[];
   T *ring = reinterpret_cast<T *>(sm);
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       int q_issue = 0, q_land = 0;  // planes requested / seen landed (plane q in slot q % D)
       int g_ready = 0, pub = 0;     // levels prepared / progress published
       const unsigned tx_bytes = G::FIELD_BYTES + (masked ? 64u : 0u);
-      const int xu = sxd > 0 ? x0 - 1 : x0 + BX, sxo = sxd > 0 ? V - 1 : V + BX;  // x face: grid x, slot x
+      const int xu = sxd > 0 ? x0 - 1 : x0 + BX, sxo = sxd > 0 ? 0 : BX + 1;  // x face: grid x, slot x
       const int yu = syd > 0 ? y0 - 1 : y0 + BY, syo = syd > 0 ? 0 : BY + 1;      // y face: grid y, slot row
       long long t_last = cycles();
       unsigned nap = 0;
@@ -176,11 +177,11 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
               const int g = g_ready + i, lz = g - k;
               if (have && inside && g < lim && lz >= 0 && lz < nz) {
                 const int gz = szd > 0 ? lz + 1 : nz - lz;
-                const long long gi = xl ? (long long)gz * plane + (long long)(y0 + gk) * px + xu + (V - 1)
-                                        : (long long)gz * plane + (long long)yu * px + x0 + gk + (V - 1);
+                const long long gi = xl ? (long long)gz * plane + (long long)(y0 + gk) * px + xu
+                                        : (long long)gz * plane + (long long)yu * px + x0 + gk;
                 v[i] = __ldcg(reinterpret_cast<const T *>(a.u) + gi);
                 const int s = (lz + 1) % D;
-                off[i] = s * SE + (xl ? (1 + gk) * W + sxo : syo * W + V + gk);
+                off[i] = s * SE + (xl ? (1 + gk) * W + sxo : syo * W + 1 + gk);
               }
             }
 #pragma unroll
@@ -227,9 +228,9 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       const int lx = tid & (BX - 1), ly = tid / BX, lxy = lx + ly;  // sweep order
       const int gx = sxd > 0 ? lx : BX - 1 - lx, gy = syd > 0 ? ly : BY - 1 - ly;
       const bool vxy = (x0 + gx <= nx) && (y0 + gy <= ny);
-      const int orow = (1 + gy) * W + V + gx;  // my node within a slot
+      const int orow = (1 + gy) * W + 1 + gx;  // my node within a slot
       const int mbyte = (int)G::MASK_OFF + 4 * gy, mshift = 16 * (cx & 1) + gx;
-      const long long grow = (long long)(y0 + gy) * px + (x0 + gx) + (V - 1);
+      const long long grow = (long long)(y0 + gy) * px + (x0 + gx);
       const float hmin = a.hmin;
       const GodConst64 k64 = a.k64;
       const GodConst32 k32 = a.k32;

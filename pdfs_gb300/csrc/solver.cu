@@ -18,12 +18,13 @@
 
 namespace pdfs {
 
-Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize) {
+Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize, int xo) {
   Layout L;
   L.tx = tx;
   L.ty = ty;
   L.esize = esize;
   L.V = 16 / esize;
+  L.xo = xo < 0 ? L.V - 1 : xo;
   L.ncx = (g.nx + tx - 1) / tx;
   L.ncy = (g.ny + ty - 1) / ty;
   const long long need = (long long)L.ncx * tx + 2 * L.V;
@@ -324,8 +325,9 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   c->dev = o.device;
   pick_tiles(c);
   const TileShape s32 = tile32(c->t32), s64 = tile64(c->t64);
-  c->L32 = make_layout(*g, s32.tx, s32.ty, 4);
-  c->L64 = make_layout(*g, s64.tx, s64.ty, 8);
+  // bricks and pencils (c == 0) index from the halo node; columns from the interior
+  c->L32 = make_layout(*g, s32.tx, s32.ty, 4, s32.c == 0 ? 0 : -1);
+  c->L64 = make_layout(*g, s64.tx, s64.ty, 8, s64.c == 0 ? 0 : -1);
   c->M = make_mask_layout(*g);
   int rc = PDFS_OK;
   auto fail = [&](cudaError_t e) {

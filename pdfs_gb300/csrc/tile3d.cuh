@@ -20,7 +20,7 @@
 //     brick holds a smaller ticket), so the wait always ends.
 //
 // A brick's old values do not depend on its upwind bricks, so its whole box
-// (the brick and a one-node halo, rounded out to 16-byte rows) is requested
+// (the brick and a one-node halo, rows rounded up to 16 bytes) is requested
 // by one TMA copy as soon as the ticket is taken; only the upwind halo faces
 // are read again, from L2, after the flags.  Updated nodes are stored to
 // global memory as they are computed (unchanged nodes are not written).
@@ -41,8 +41,9 @@ namespace pdfs {
 template <class T, int BY_, int BZ>
 struct T3Geo {
   static constexpr int BX = 16, BY = BY_;
-  static constexpr int V = 16 / (int)sizeof(T);
-  static constexpr int W = BX + 2 * V;    // box row: x0-V .. x0+BX+V-1 (16-byte aligned start)
+  // box row: x0-1 .. x0+BX, rounded up to 16 bytes; the field's index has no
+  // x offset, so x0 - 1 = 16*bi starts the row on a 16-byte boundary
+  static constexpr int W = (int)((((BX + 2) * sizeof(T)) + 15) / 16 * 16 / sizeof(T));
   static constexpr int RY = BY + 2;       // box rows: y0-1 .. y0+BY
   static constexpr int RZ = BZ + 2;       // box planes: z0-1 .. z0+BZ
   static constexpr int PL = RY * W;       // plane stride in shared memory
@@ -67,7 +68,7 @@ template <class T, int BY_, int BZ, int MODE, int ARITH, bool ISO>
 __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                             const __grid_constant__ SweepArgs a) {
   using G = T3Geo<T, BY_, BZ>;
-  constexpr int BX = G::BX, BY = G::BY, V = G::V, W = G::W, PL = G::PL, NL = G::NL, NZB = G::NZB, CP = G::CP;
+  constexpr int BX = G::BX, BY = G::BY, W = G::W, PL = G::PL, NL = G::NL, NZB = G::NZB, CP = G::CP;
   extern __shared__ __align__(1024) unsigned char sm[];
   T *box = reinterpret_cast<T *>(sm);
   uint32_t *smask = reinterpret_cast<uint32_t *>(sm + G::OFF_MASK);  // [BZ][BY] frozen words of the brick
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       continue;
     }
 
-    // the box: TMA from (x0 - V, y0 - 1, z0 - 1); out-of-range rows and planes read 0 (never used)
+    // the box: TMA from (x0 - 1, y0 - 1, z0 - 1); out-of-range rows and planes read 0 (never used)
     fence_proxy_async();  // this CTA's generic accesses to the box come before the copy's writes
     __syncthreads();
     if (tid == 0) {
@@ -189,7 +190,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
         if (bz < a.nbz && __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx)) actz |= 1u << q;
       }
     }
-    const long long gbase = (long long)z0 * plane + (long long)(y0 + gyl) * px + (x0 + gxl) + (V - 1);
+    const long long gbase = (long long)z0 * plane + (long long)(y0 + gyl) * px + (x0 + gxl);
     // replace-update caps of my first CP nodes (sweep order) from the first level run
     T capq[CP];
     auto cap_at = [&](int lz) -> T {
@@ -242,12 +243,12 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     // upwind halo faces: this sweep's values, written by the upwind bricks (L2)
     if (li > 0) {  // x face
       const int xu = sxd > 0 ? x0 - 1 : x0 + BX;
-      const int sxo = sxd > 0 ? V - 1 : V + BX;
+      const int sxo = sxd > 0 ? 0 : BX + 1;
       for (int q = tid; q < BZ * BY; q += G::NT) {
         const int p = q / BY, r = q % BY;
         if (p < zcnt && y0 + r <= ny)
           box[(1 + p) * PL + (1 + r) * W + sxo] =
-              __ldcg(u + (long long)(z0 + p) * plane + (long long)(y0 + r) * px + xu + (V - 1));
+              __ldcg(u + (long long)(z0 + p) * plane + (long long)(y0 + r) * px + xu);
       }
     }
     if (lj > 0) {  // y face
@@ -256,8 +257,8 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       for (int q = tid; q < BZ * BX; q += G::NT) {
         const int p = q / BX, xx = q % BX;
         if (p < zcnt && x0 + xx <= nx)
-          box[(1 + p) * PL + syo * W + V + xx] =
-              __ldcg(u + (long long)(z0 + p) * plane + (long long)yu * px + x0 + xx + (V - 1));
+          box[(1 + p) * PL + syo * W + 1 + xx] =
+              __ldcg(u + (long long)(z0 + p) * plane + (long long)yu * px + x0 + xx);
       }
     }
     if (lk > 0) {  // z face
@@ -266,14 +267,14 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       for (int q = tid; q < BY * BX; q += G::NT) {
         const int r = q / BX, xx = q % BX;
         if (y0 + r <= ny && x0 + xx <= nx)
-          box[szo * PL + (1 + r) * W + V + xx] =
-              __ldcg(u + (long long)zu * plane + (long long)(y0 + r) * px + x0 + xx + (V - 1));
+          box[szo * PL + (1 + r) * W + 1 + xx] =
+              __ldcg(u + (long long)zu * plane + (long long)(y0 + r) * px + x0 + xx);
       }
     }
     __syncthreads();
 
     // the levels: node (lx, ly, lz = L - lx - ly), sweep order
-    const int obase = (1 + gyl) * W + V + gxl + (szd > 0 ? PL : BZ * PL);  // lz = 0
+    const int obase = (1 + gyl) * W + 1 + gxl + (szd > 0 ? PL : BZ * PL);  // lz = 0
     const int dzo = szd > 0 ? PL : -PL;
     T accb[NZB];
 #pragma unroll
