@@ -15,9 +15,11 @@
 //   * planes stream through a ring of D shared-memory slots (TMA,
 //     cp.async.bulk.tensor; one mbarrier per slot), as far ahead as the slot
 //     of the plane SK + 1 levels back allows;
-//   * a helper warp loads the planes, patches into them the upwind faces of
-//     the neighbouring pencils and publishes this pencil's progress (levels
-//     complete).  Thread (0, ly) at level G reads the upwind x pencil's node
+//   * three helper warps overlap their latencies: a loader warp requests the
+//     planes and reports them landed, a publisher warp makes the pencil's
+//     stores visible (GPU-scope fence) and publishes its progress (levels
+//     complete), and a face warp patches into the landed planes the upwind
+//     faces of the neighbouring pencils.  Thread (0, ly) at level G reads the upwind x pencil's node
 //     (15, ly, G - ly), which that pencil computed at its level G + 15: all
 //     sixteen x-face cells of level G are ready once the upwind pencil has
 //     published G + 16, and likewise the y face.  The faces are read from the
@@ -46,8 +48,8 @@ struct PcGeo {
   static constexpr unsigned MASK_OFF = (FIELD_BYTES + 127u) & ~127u;  // the plane's 16 frozen words
   static constexpr unsigned SLOT_BYTES = MASK_OFF + 128u;
   static constexpr int NC = BX * BY;       // compute threads
-  static constexpr int NT = NC + 32;       // and the helper warp
-  static constexpr int C = 8;              // levels the helper prepares per round, at most
+  static constexpr int NT = NC + 96;       // and the loader, publisher and face warps
+  static constexpr int C = 8;              // levels the face warp prepares per round, at most
   static constexpr int CP = 4;             // replace-update: caps prefetched ahead (registers)
   static constexpr size_t OFF_BAR = (size_t)D * SLOT_BYTES;
   static constexpr size_t BYTES = OFF_BAR + (size_t)D * 8 + 16;
@@ -55,6 +57,28 @@ struct PcGeo {
 };
 
 __device__ __forceinline__ void compute_bar() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
+
+// One idle round of a helper warp: lane 0 decides, for the whole warp, to give
+// up on the abort flag or after wait_cycles without progress.
+__device__ __forceinline__ bool helper_idle(const SweepArgs &a, int col, volatile int *s_abort, long long t_last,
+                                            unsigned &nap) {
+  int stop = 0;
+  if ((threadIdx.x & 31) == 0) {
+    if (*s_abort || *(volatile int *)(a.err + 1)) {
+      stop = 1;
+    } else if (cycles() - t_last > a.wait_cycles) {
+      raise_timeout(a, col, s_abort);
+      stop = 1;
+    }
+  }
+  if (__shfl_sync(0xffffffffu, stop, 0)) {
+    *s_abort = 1;
+    return true;
+  }
+  if (nap) __nanosleep(nap);
+  nap = min(nap + 32u, 128u);
+  return false;
+}
 
 template <class T, int MODE, int ARITH, bool ISO>
 __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
@@ -66,7 +90,7 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
   extern __shared__ __align__(1024) unsigned char sm[];
   T *ring = reinterpret_cast<T *>(sm);
   uint64_t *full = reinterpret_cast<uint64_t *>(sm + G::OFF_BAR);
-  __shared__ int s_ticket, s_stop, s_done, s_ready;
+  __shared__ int s_ticket, s_stop, s_done, s_ready, s_landed;
   __shared__ volatile int s_abort;
 
   if ((saddr(sm) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
@@ -77,7 +101,6 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
     return;
   }
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool helper = warp == G::NC / 32;
   const int ntick = a.ncx * a.ncy;
   const int sxd = a.sx, syd = a.sy, szd = a.sz;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
@@ -95,6 +118,7 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       s_stop = (tk >= ntick || s_abort) ? 1 : 0;
       s_done = 0;
       s_ready = 0;
+      s_landed = 0;
       for (int i = 0; i < D; ++i) {
         if (npen) mbar_inval(full + i);
         mbar_init(full + i, 1);
@@ -112,26 +136,17 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
     const int upy = lcy > 0 ? col - syd * a.ncx : -1;
     const int x0 = 1 + cx * BX, y0 = 1 + cy * BY;
 
-    if (helper) {
-      // ------------------------------------ helper warp ------------------------------------
+    if (warp == G::NC / 32) {
+      // ------------------------------- loader warp (lane 0) -------------------------------
       int q_issue = 0, q_land = 0;  // planes requested / seen landed (plane q in slot q % D)
-      int g_ready = 0, pub = 0;     // levels prepared / progress published
       const unsigned tx_bytes = G::FIELD_BYTES + (masked ? 64u : 0u);
-      const int xu = sxd > 0 ? x0 - 1 : x0 + BX, sxo = sxd > 0 ? 0 : BX + 1;  // x face: grid x, slot x
-      const int yu = syd > 0 ? y0 - 1 : y0 + BY, syo = syd > 0 ? 0 : BY + 1;      // y face: grid y, slot row
       long long t_last = cycles();
       unsigned nap = 0;
       bool failed = false;
       for (;;) {
-        bool moved = false;
-        const int done = __shfl_sync(0xffffffffu, ld_acquire_cta_s(&s_done), 0);
-        if (done > pub) {  // the compute threads' node stores are visible before the progress word
-          __threadfence();
-          if (lane == 0 && col != a.poison_col) st_relaxed_gpu(a.prog + col, done);
-          pub = done;
-          moved = true;
-        }
+        int moved = 0;
         if (lane == 0) {
+          const int done = ld_acquire_cta_s(&s_done);
           // plane q reuses the slot of plane q - D, last read at level q - D + SK
           while (q_issue < NP && (q_issue < D || done >= q_issue - D + SK + 1)) {
             const int s = q_issue % D;
@@ -141,79 +156,25 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
             tma_load_3d(dst, &tm_u, cx * BX, y0 - 1, gz, full + s);
             if (masked) tma_load_3d(dst + G::MASK_OFF, &tm_mask, cy * BY, cx >> 1, gz, full + s);
             ++q_issue;
-            moved = true;
+            moved = 1;
           }
+          const int q0 = q_land;
           while (q_land < q_issue && mbar_try(full + q_land % D, (q_land / D) & 1)) ++q_land;
+          if (q_land > q0) {
+            st_release_cta_s(&s_landed, q_land);
+            moved = 1;
+          }
         }
-        // lane 0's requests count as progress for the whole warp: every decision
-        // below (including the give-up) is warp-uniform
-        moved = __any_sync(0xffffffffu, moved);
+        moved = __shfl_sync(0xffffffffu, moved, 0);  // lane 0 decides for the warp
         q_issue = __shfl_sync(0xffffffffu, q_issue, 0);
         q_land = __shfl_sync(0xffffffffu, q_land, 0);
-        if (g_ready < t_end) {
-          // level g needs planes up to min(g + 2, NP - 1) and upwind progress >= min(g + 16, t_end)
-          int ux = 0x3fffffff, uy = 0x3fffffff;
-          if (upx >= 0 && lane == 0) ux = ld_acquire_gpu(a.prog + upx);
-          if (upy >= 0 && lane == 1) uy = ld_acquire_gpu(a.prog + upy);
-          ux = __shfl_sync(0xffffffffu, ux, 0);
-          uy = __shfl_sync(0xffffffffu, uy, 1);
-          const int um = min(ux, uy);
-          int lim = um >= t_end ? t_end : um - 15;
-          lim = min(lim, q_land >= NP ? t_end : q_land - 2);
-          lim = min(lim, g_ready + G::C);
-          if (lim > g_ready) {
-            // faces of levels g_ready .. lim-1: lane < 16 -> x face row ly = lane,
-            // lane >= 16 -> y face column lx = lane - 16; loads first, then stores
-            T v[G::C];
-            int off[G::C];
-            const int k = lane & 15;
-            const bool xl = lane < 16;
-            const bool have = xl ? upx >= 0 : upy >= 0;
-            const int gk = xl ? (syd > 0 ? k : BY - 1 - k) : (sxd > 0 ? k : BX - 1 - k);
-            const bool inside = xl ? (y0 + gk <= ny) : (x0 + gk <= nx);
-#pragma unroll
-            for (int i = 0; i < G::C; ++i) {
-              off[i] = -1;
-              const int g = g_ready + i, lz = g - k;
-              if (have && inside && g < lim && lz >= 0 && lz < nz) {
-                const int gz = szd > 0 ? lz + 1 : nz - lz;
-                const long long gi = xl ? (long long)gz * plane + (long long)(y0 + gk) * px + xu
-                                        : (long long)gz * plane + (long long)yu * px + x0 + gk;
-                v[i] = __ldcg(reinterpret_cast<const T *>(a.u) + gi);
-                const int s = (lz + 1) % D;
-                off[i] = s * SE + (xl ? (1 + gk) * W + sxo : syo * W + 1 + gk);
-              }
-            }
-#pragma unroll
-            for (int i = 0; i < G::C; ++i)
-              if (off[i] >= 0) ring[off[i]] = v[i];
-            __syncwarp();
-            if (lane == 0) st_release_cta_s(&s_ready, lim);
-            g_ready = lim;
-            moved = true;
-          }
-        }
-        if (pub >= t_end && q_land >= NP) break;  // every level done and published
+        if (q_land >= NP) break;
         if (moved) {
           t_last = cycles();
           nap = 0;
-        } else {
-          int stop = 0;  // lane 0 decides for the warp
-          if (lane == 0) {
-            if (s_abort || *(volatile int *)(a.err + 1)) {
-              stop = 1;
-            } else if (cycles() - t_last > a.wait_cycles) {
-              raise_timeout(a, col, &s_abort);
-              stop = 1;
-            }
-          }
-          if (__shfl_sync(0xffffffffu, stop, 0)) {
-            s_abort = 1;
-            failed = true;
-            break;
-          }
-          if (nap) __nanosleep(nap);
-          nap = min(nap + 32u, 128u);
+        } else if (helper_idle(a, col, &s_abort, t_last, nap)) {
+          failed = true;
+          break;
         }
       }
       if (failed && lane == 0) {  // let the copies in flight land before the CTA leaves
@@ -221,6 +182,76 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
           const long long t0 = cycles();
           while (!mbar_try(full + q % D, (q / D) & 1) && cycles() - t0 < 4000000000ll) {
           }
+        }
+      }
+    } else if (warp == G::NC / 32 + 1) {
+      // ----------------------------------- publisher warp -----------------------------------
+      int pub = 0;
+      long long t_last = cycles();
+      unsigned nap = 0;
+      for (;;) {
+        const int done = __shfl_sync(0xffffffffu, ld_acquire_cta_s(&s_done), 0);
+        if (done > pub) {  // the compute threads' node stores are visible before the progress word
+          __threadfence();
+          if (lane == 0 && col != a.poison_col) st_relaxed_gpu(a.prog + col, done);
+          pub = done;
+          t_last = cycles();
+          nap = 0;
+        } else if (helper_idle(a, col, &s_abort, t_last, nap)) {
+          break;
+        }
+        if (pub >= t_end) break;
+      }
+    } else if (warp == G::NC / 32 + 2) {
+      // -------------------------------------- face warp --------------------------------------
+      // Level g needs planes up to min(g + 2, NP - 1) and upwind progress >= min(g + 16, t_end).
+      int g_ready = 0;
+      const int xu = sxd > 0 ? x0 - 1 : x0 + BX, sxo = sxd > 0 ? 0 : BX + 1;  // x face: grid x, slot x
+      const int yu = syd > 0 ? y0 - 1 : y0 + BY, syo = syd > 0 ? 0 : BY + 1;      // y face: grid y, slot row
+      const int k = lane & 15;
+      const bool xl = lane < 16;  // lane < 16: x face row ly = lane; else y face column lx = lane - 16
+      const bool have = xl ? upx >= 0 : upy >= 0;
+      const int gk = xl ? (syd > 0 ? k : BY - 1 - k) : (sxd > 0 ? k : BX - 1 - k);
+      const bool inside = xl ? (y0 + gk <= ny) : (x0 + gk <= nx);
+      long long t_last = cycles();
+      unsigned nap = 0;
+      while (g_ready < t_end) {
+        const int landed = __shfl_sync(0xffffffffu, ld_acquire_cta_s(&s_landed), 0);
+        int ux = 0x3fffffff, uy = 0x3fffffff;
+        if (upx >= 0 && lane == 0) ux = ld_acquire_gpu(a.prog + upx);
+        if (upy >= 0 && lane == 1) uy = ld_acquire_gpu(a.prog + upy);
+        ux = __shfl_sync(0xffffffffu, ux, 0);
+        uy = __shfl_sync(0xffffffffu, uy, 1);
+        const int um = min(ux, uy);
+        int lim = um >= t_end ? t_end : um - 15;
+        lim = min(lim, landed >= NP ? t_end : landed - 2);
+        lim = min(lim, g_ready + G::C);
+        if (lim > g_ready) {
+          T v[G::C];
+          int off[G::C];
+#pragma unroll
+          for (int i = 0; i < G::C; ++i) {  // loads first, then stores
+            off[i] = -1;
+            const int g = g_ready + i, lz = g - k;
+            if (have && inside && g < lim && lz >= 0 && lz < nz) {
+              const int gz = szd > 0 ? lz + 1 : nz - lz;
+              const long long gi = xl ? (long long)gz * plane + (long long)(y0 + gk) * px + xu
+                                      : (long long)gz * plane + (long long)yu * px + x0 + gk;
+              v[i] = __ldcg(reinterpret_cast<const T *>(a.u) + gi);
+              const int s = (lz + 1) % D;
+              off[i] = s * SE + (xl ? (1 + gk) * W + sxo : syo * W + 1 + gk);
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < G::C; ++i)
+            if (off[i] >= 0) ring[off[i]] = v[i];
+          __syncwarp();
+          if (lane == 0) st_release_cta_s(&s_ready, lim);
+          g_ready = lim;
+          t_last = cycles();
+          nap = 0;
+        } else if (helper_idle(a, col, &s_abort, t_last, nap)) {
+          break;
         }
       }
     } else {
