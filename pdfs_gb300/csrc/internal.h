@@ -142,7 +142,9 @@ struct pdfs_ctx {
   // brick tiles (tile3d.cuh): per-brick completion epochs, ticket orders, brick grids
   int *tflag = nullptr, *tord32 = nullptr, *tord64 = nullptr;
   int nt32[3] = {0, 0, 0}, nt64[3] = {0, 0, 0};
-  int epoch = 0;  // flag value of the last brick sweep
+  int epoch = 0;  // flag value of the last brick or pencil sweep
+  unsigned long long *pmail = nullptr;  // pencils: epoch-tagged face mailboxes
+  int prow = 0;                          // their diagonals per face
   void *mailbox = nullptr;  // x- and y-face mailboxes of every column
   size_t mailbox_bytes = 0;
   size_t progress_ints = 0;

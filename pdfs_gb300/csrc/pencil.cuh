@@ -15,16 +15,17 @@
 //   * planes stream through a ring of D shared-memory slots (TMA,
 //     cp.async.bulk.tensor; one mbarrier per slot), as far ahead as the slot
 //     of the plane SK + 1 levels back allows;
-//   * three helper warps overlap their latencies: a loader warp requests the
-//     planes and reports them landed, a publisher warp makes the pencil's
-//     stores visible (GPU-scope fence) and publishes its progress (levels
-//     complete), and a face warp patches into the landed planes the upwind
-//     faces of the neighbouring pencils.  Thread (0, ly) at level G reads the upwind x pencil's node
-//     (15, ly, G - ly), which that pencil computed at its level G + 15: all
-//     sixteen x-face cells of level G are ready once the upwind pencil has
-//     published G + 16, and likewise the y face.  The faces are read from the
-//     field itself (L2) -- a node's value there is final once its pencil has
-//     passed it;
+//   * faces cross pencils through mailboxes of epoch-tagged 64-bit words: the
+//     threads on a pencil's downwind x (y) face write each node's final value
+//     of the sweep, tagged with the sweep's epoch, to entry [lz + ly][ly]
+//     ([lz + lx][lx]).  A 64-bit store is single-copy atomic, so a reader that
+//     sees the tag sees the value: no GPU-scope fence and no progress counter.
+//     Thread (0, ly) at level G reads the upwind x pencil's node (15, ly,
+//     G - ly), entry [G][ly], which that pencil wrote at its level G + 15, so
+//     a pencil runs about 16 levels behind its neighbours;
+//   * a loader warp requests the planes and reports them landed, and a face
+//     warp polls the upwind mailboxes a few diagonals ahead and patches the
+//     tagged values into the landed planes;
 //   * pencils are taken by ticket in wavefront order, so an upwind pencil is
 //     always running or done; every wait is bounded (SweepArgs::wait_cycles)
 //     and ends in DEV_ERR_TIMEOUT plus the abort flag, never in a hang.
@@ -48,7 +49,8 @@ struct PcGeo {
   static constexpr unsigned MASK_OFF = (FIELD_BYTES + 127u) & ~127u;  // the plane's 16 frozen words
   static constexpr unsigned SLOT_BYTES = MASK_OFF + 128u;
   static constexpr int NC = BX * BY;       // compute threads
-  static constexpr int NT = NC + 96;       // and the loader, publisher and face warps
+  static constexpr int NT = NC + 64;       // and the loader and face warps
+  static constexpr int WV = (int)sizeof(T) / 4 > 1 ? 2 : 1;  // mailbox words per value (32 value bits each)
   static constexpr int C = 8;              // levels the face warp prepares per round, at most
   static constexpr int CP = 4;             // replace-update: caps prefetched ahead (registers)
   static constexpr size_t OFF_BAR = (size_t)D * SLOT_BYTES;
@@ -57,6 +59,39 @@ struct PcGeo {
 };
 
 __device__ __forceinline__ void compute_bar() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
+
+__device__ __forceinline__ void st_relaxed_gpu_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+// A value's 32-bit pieces, each tagged with the epoch in the upper word.
+template <class T>
+__device__ __forceinline__ void mail_put(unsigned long long *e, T v, int epoch) {
+  const unsigned long long tag = (unsigned long long)(unsigned)epoch << 32;
+  if constexpr (sizeof(T) == 4) {
+    st_relaxed_gpu_u64(e, tag | __float_as_uint(v));
+  } else {
+    st_relaxed_gpu_u64(e, tag | (unsigned)__double2loint(v));
+    st_relaxed_gpu_u64(e + 1, tag | (unsigned)__double2hiint(v));
+  }
+}
+template <class T>
+__device__ __forceinline__ bool mail_get(const unsigned long long *e, int epoch, T &v) {
+  const unsigned tag = (unsigned)epoch;
+  const unsigned long long w0 = ld_relaxed_gpu_u64(e);
+  if constexpr (sizeof(T) == 4) {
+    v = __uint_as_float((unsigned)w0);
+    return (unsigned)(w0 >> 32) == tag;
+  } else {
+    const unsigned long long w1 = ld_relaxed_gpu_u64(e + 1);
+    v = __hiloint2double((int)(unsigned)w1, (int)(unsigned)w0);
+    return (unsigned)(w0 >> 32) == tag && (unsigned)(w1 >> 32) == tag;
+  }
+}
 
 // One idle round of a helper warp: lane 0 decides, for the whole warp, to give
 // up on the abort flag or after wait_cycles without progress.
@@ -107,6 +142,7 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
   const int NP = nz + 2, t_end = nz + SK;  // planes (sweep order, halo planes included), levels
   const long long plane = a.plane, px = a.px;
   const bool masked = a.fmask != nullptr;
+  const int epoch = a.epoch;
   T tmax = T(0);
 
   if (tid == 0) s_abort = 0;
@@ -185,66 +221,45 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
         }
       }
     } else if (warp == G::NC / 32 + 1) {
-      // ----------------------------------- publisher warp -----------------------------------
-      int pub = 0;
-      long long t_last = cycles();
-      unsigned nap = 0;
-      for (;;) {
-        const int done = __shfl_sync(0xffffffffu, ld_acquire_cta_s(&s_done), 0);
-        if (done > pub) {  // the compute threads' node stores are visible before the progress word
-          __threadfence();
-          if (lane == 0 && col != a.poison_col) st_relaxed_gpu(a.prog + col, done);
-          pub = done;
-          t_last = cycles();
-          nap = 0;
-        } else if (helper_idle(a, col, &s_abort, t_last, nap)) {
-          break;
-        }
-        if (pub >= t_end) break;
-      }
-    } else if (warp == G::NC / 32 + 2) {
       // -------------------------------------- face warp --------------------------------------
-      // Level g needs planes up to min(g + 2, NP - 1) and upwind progress >= min(g + 16, t_end).
+      // Level g needs planes up to min(g + 2, NP - 1) and diagonal g of the
+      // upwind pencils' face mailboxes.
       int g_ready = 0;
-      const int xu = sxd > 0 ? x0 - 1 : x0 + BX, sxo = sxd > 0 ? 0 : BX + 1;  // x face: grid x, slot x
-      const int yu = syd > 0 ? y0 - 1 : y0 + BY, syo = syd > 0 ? 0 : BY + 1;      // y face: grid y, slot row
+      const int sxo = sxd > 0 ? 0 : BX + 1;  // x face: slot x
+      const int syo = syd > 0 ? 0 : BY + 1;  // y face: slot row
       const int k = lane & 15;
       const bool xl = lane < 16;  // lane < 16: x face row ly = lane; else y face column lx = lane - 16
-      const bool have = xl ? upx >= 0 : upy >= 0;
+      const int up = xl ? upx : upy;
       const int gk = xl ? (syd > 0 ? k : BY - 1 - k) : (sxd > 0 ? k : BX - 1 - k);
-      const bool inside = xl ? (y0 + gk <= ny) : (x0 + gk <= nx);
+      const bool need = up >= 0 && (xl ? (y0 + gk <= ny) : (x0 + gk <= nx));
+      const unsigned long long *box =
+          need ? a.pmail + (((size_t)up * 2 + (xl ? 0 : 1)) * a.prow * 16 + k) * G::WV : nullptr;
       long long t_last = cycles();
       unsigned nap = 0;
       while (g_ready < t_end) {
         const int landed = __shfl_sync(0xffffffffu, ld_acquire_cta_s(&s_landed), 0);
-        int ux = 0x3fffffff, uy = 0x3fffffff;
-        if (upx >= 0 && lane == 0) ux = ld_acquire_gpu(a.prog + upx);
-        if (upy >= 0 && lane == 1) uy = ld_acquire_gpu(a.prog + upy);
-        ux = __shfl_sync(0xffffffffu, ux, 0);
-        uy = __shfl_sync(0xffffffffu, uy, 1);
-        const int um = min(ux, uy);
-        int lim = um >= t_end ? t_end : um - 15;
-        lim = min(lim, landed >= NP ? t_end : landed - 2);
-        lim = min(lim, g_ready + G::C);
+        const int plim = landed >= NP ? t_end : landed - 2;
+        int lim = min(min(t_end, plim), g_ready + G::C);
+        T v[G::C];
+        unsigned okm = 0;  // bit i: level g_ready + i is ready for this lane
+#pragma unroll
+        for (int i = 0; i < G::C; ++i) {
+          const int g = g_ready + i, lz = g - k;
+          bool ok = true;
+          if (need && g < lim && lz >= 0 && lz < nz) ok = mail_get<T>(box + (size_t)g * 16 * G::WV, epoch, v[i]);
+          if (ok) okm |= 1u << i;
+        }
+        okm = __reduce_and_sync(0xffffffffu, okm);
+        lim = min(lim, g_ready + __ffs(~okm) - 1);  // the ready prefix
         if (lim > g_ready) {
-          T v[G::C];
-          int off[G::C];
 #pragma unroll
-          for (int i = 0; i < G::C; ++i) {  // loads first, then stores
-            off[i] = -1;
+          for (int i = 0; i < G::C; ++i) {
             const int g = g_ready + i, lz = g - k;
-            if (have && inside && g < lim && lz >= 0 && lz < nz) {
-              const int gz = szd > 0 ? lz + 1 : nz - lz;
-              const long long gi = xl ? (long long)gz * plane + (long long)(y0 + gk) * px + xu
-                                      : (long long)gz * plane + (long long)yu * px + x0 + gk;
-              v[i] = __ldcg(reinterpret_cast<const T *>(a.u) + gi);
-              const int s = (lz + 1) % D;
-              off[i] = s * SE + (xl ? (1 + gk) * W + sxo : syo * W + 1 + gk);
-            }
+            if (need && g < lim && lz >= 0 && lz < nz)
+              ring[((lz + 1) % D) * SE + (xl ? (1 + gk) * W + sxo : syo * W + 1 + gk)] = v[i];
           }
-#pragma unroll
-          for (int i = 0; i < G::C; ++i)
-            if (off[i] >= 0) ring[off[i]] = v[i];
+          __syncwarp();
+          fence_proxy_async();  // these halo stores come before a later TMA write into the slots
           __syncwarp();
           if (lane == 0) st_release_cta_s(&s_ready, lim);
           g_ready = lim;
@@ -262,6 +277,12 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       const int orow = (1 + gy) * W + 1 + gx;  // my node within a slot
       const int mbyte = (int)G::MASK_OFF + 4 * gy, mshift = 16 * (cx & 1) + gx;
       const long long grow = (long long)(y0 + gy) * px + (x0 + gx);
+      // downwind faces: my node's final value goes to a mailbox when a pencil is downwind
+      const bool poisoned = col == a.poison_col;
+      const bool mx = lx == BX - 1 && lcx < a.ncx - 1 && !poisoned;
+      const bool my = ly == BY - 1 && lcy < a.ncy - 1 && !poisoned;
+      unsigned long long *xmail = a.pmail + ((size_t)col * 2 + 0) * a.prow * 16 * G::WV;
+      unsigned long long *ymail = a.pmail + ((size_t)col * 2 + 1) * a.prow * 16 * G::WV;
       const float hmin = a.hmin;
       const GodConst64 k64 = a.k64;
       const GodConst32 k32 = a.k32;
@@ -311,16 +332,20 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
               const uint32_t w = *reinterpret_cast<const uint32_t *>(sm + (size_t)sl * G::SLOT_BYTES + mbyte);
               act = !((w >> mshift) & 1u);
             }
+            T fin = cv;  // the node's value at the end of the sweep
             if (act) {
               const T gv = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
               const T nv = MODE == MODE_REPLACE ? vmin<T, ARITH>(capq[0], gv) : vmin<T, ARITH>(cv, gv);
               if (vdiffers<T, ARITH>(nv, cv)) {
+                fin = nv;
                 cur[orow] = nv;
                 u[(long long)gz_of(lz) * plane + grow] = nv;
                 tmax = vmax_nonneg<T, ARITH>(tmax, node_change<T, ARITH>(cv, nv, hmin));
                 fence_proxy_async();  // this store comes before a later TMA write into the slot
               }
             }
+            if (mx) mail_put<T>(xmail + ((size_t)(lz + ly) * 16 + ly) * G::WV, fin, epoch);
+            if (my) mail_put<T>(ymail + ((size_t)(lz + lx) * 16 + lx) * G::WV, fin, epoch);
           }
           if (MODE == MODE_REPLACE) {
 #pragma unroll

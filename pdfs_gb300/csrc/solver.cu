@@ -406,6 +406,15 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
       if ((e = cudaMalloc(&c->tflag, nflags * 4)) != cudaSuccess) return fail(e);
       if ((e = cudaMemset(c->tflag, 0, nflags * 4)) != cudaSuccess) return fail(e);
     }
+    // pencils: two faces of prow diagonals x 16 entries x 2 words per pencil
+    // (tag 0 never matches: epochs start at 1)
+    if (s32.pencil || s64.pencil) {
+      const size_t ncol = (size_t)((g->nx + 15) / 16) * ((g->ny + 15) / 16);
+      c->prow = g->nz + 15;
+      const size_t words = ncol * 2 * (size_t)c->prow * 16 * 2;
+      if ((e = cudaMalloc(&c->pmail, words * 8)) != cudaSuccess) return fail(e);
+      if ((e = cudaMemset(c->pmail, 0, words * 8)) != cudaSuccess) return fail(e);
+    }
   }
   {
     std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
@@ -444,6 +453,7 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   cudaFree(c->order32);
   cudaFree(c->order64);
   cudaFree(c->tflag);
+  cudaFree(c->pmail);
   cudaFree(c->tord32);
   cudaFree(c->tord64);
   cudaFree(c->progress);
@@ -583,6 +593,8 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   a.nty = nt[1];
   a.ntz = nt[2];
   a.epoch = c->epoch;
+  a.pmail = c->pmail;
+  a.prow = c->prow;
   long long wait_ms = c->o.spin_limit > 0 ? c->o.spin_limit : 4000;
   if (getenv("PDFS_WAIT_MS")) wait_ms = atoll(getenv("PDFS_WAIT_MS"));
   a.wait_cycles = wait_ms * 1000000LL * 21 / 10;  // at most 2.07 GHz: never shorter than wait_ms
@@ -631,6 +643,7 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
   if (pencil) {
+    a.epoch = ++c->epoch;  // mailbox words of every earlier sweep carry a smaller tag
     CK(launch_sweep_pencils(which, arith, iso, a, L, c->sms, c->st, &grid));
   } else if (ts.bz > 0) {
     a.epoch = ++c->epoch;  // the flags of every earlier sweep are below it

@@ -88,6 +88,10 @@ struct SweepArgs {
   const int *torder;      // ticket -> local brick id in sweep order, wavefront order
   int ntx, nty, ntz;      // brick grid
   int epoch;              // this sweep's flag value (increases every launch)
+  // pencils (pencil.cuh): per pencil, its downwind x and y faces as epoch-tagged
+  // 64-bit words, [pencil][face][prow diagonals][16][words per value]
+  unsigned long long *pmail;
+  int prow;
 };
 
 // A batched sweep: tickets enumerate (grid, local column) pairs, each grid's
