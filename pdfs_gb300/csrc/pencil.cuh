@@ -43,7 +43,9 @@ struct PcGeo {
   static constexpr int W = (int)((((BX + 2) * sizeof(T)) + 15) / 16 * 16 / sizeof(T));
   static constexpr int RY = BY + 2;        // slot rows: y0-1 .. y0+BY
   static constexpr int SK = BX + BY - 2;   // thread (15, 15) trails thread (0, 0) by SK planes
-  static constexpr int LOOK = sizeof(T) == 4 ? 5 : 3;  // planes requested ahead of use
+  // planes requested ahead of use; FP32 publishes its done count every other level
+  static constexpr int LOOK = sizeof(T) == 4 ? 7 : 3;
+  static constexpr int PUB = sizeof(T) == 4 ? 1 : 0;
   static constexpr int D = SK + 3 + LOOK;  // ring slots
   static constexpr unsigned FIELD_BYTES = (unsigned)(W * RY * sizeof(T));
   static constexpr unsigned MASK_OFF = (FIELD_BYTES + 127u) & ~127u;  // the plane's 16 frozen words
@@ -298,24 +300,33 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       for (int q = 0; q < CP; ++q) capq[q] = cap_at(q);
       int sl = (1 - lxy) % D;  // slot of my node's plane (lz + 1) at level 0
       if (sl < 0) sl += D;
+      int ready = 0;  // thread 0: levels below it are prepared (re-read only when reached)
+      bool stop = false;
       for (int g = 0; g < t_end; ++g) {
-        if (tid == 0 && ld_acquire_cta_s(&s_ready) <= g) {
+        if (tid == 0 && ready <= g) {
+          ready = ld_acquire_cta_s(&s_ready);
           const long long t0 = cycles();
-          while (ld_acquire_cta_s(&s_ready) <= g) {
+          while (ready <= g) {
             if (s_abort) {
-              s_stop = 1;
+              stop = true;
               break;
             }
             if (cycles() - t0 > a.wait_cycles) {
               raise_timeout(a, col, &s_abort);
-              s_stop = 1;
+              stop = true;
               break;
             }
+            ready = ld_acquire_cta_s(&s_ready);
           }
         }
+        if (tid == 0 && stop) s_stop = 1;
         compute_bar();
-        if (s_stop) break;
-        if (tid == 0) st_release_cta_s(&s_done, g);  // levels below g are complete
+        if (s_stop) {
+          stop = true;
+          break;
+        }
+        // levels below g are complete (FP32: published every other level; its ring looks further ahead)
+        if (tid == 0 && (g & G::PUB) == 0) st_release_cta_s(&s_done, g);
         const int lz = g - lxy;
         if ((unsigned)lz < (unsigned)nz) {
           if (vxy) {
@@ -356,7 +367,7 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
         sl = sl == D - 1 ? 0 : sl + 1;
       }
       compute_bar();
-      if (tid == 0 && !s_stop) st_release_cta_s(&s_done, t_end);
+      if (tid == 0 && !stop) st_release_cta_s(&s_done, t_end);
     }
     __syncthreads();
     if (s_abort) break;

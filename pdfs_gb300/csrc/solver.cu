@@ -290,15 +290,16 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
 }
 
 // Default tile choice (pdfs_autotune may override through opts.tile).
-// FP32: 16 x 16 x 32 bricks (tile 9: 4.2 ms per 768^3 sweep against 7.9 ms
-// for the best column tile, 32 x 8 with one row per compute warp).
+// FP32: 16 x 16 pencils (tile 10: 3.6 ms per 768^3 sweep, against 3.9 ms for
+// 16 x 16 x 32 bricks and 7.9 ms for the best column tile); their masked
+// sweeps run on 16 x 16 x 32 bricks.
 // FP64: bricks (tile 5) for the mixed arithmetic (14.4 ms per 768^3 polish
 // sweep against 15.9 ms for 32 x 6 columns) and for FP32 pairs (bricks
 // only); the reference and fast arithmetic are bound by the FP64 pipe and
 // run 2.3x faster on 32 x 4 columns (16 against 36 ms per 384^3 sweep).
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
-  c->t32 = t32 ? t32 : 9;
+  c->t32 = t32 ? t32 : 10;
   c->t64 = t64 ? t64 : ((c->o.arith == PDFS_ARITH_MIXED || c->o.arith == PDFS_ARITH_PAIR) ? 5 : 1);
 }
 

@@ -12,10 +12,10 @@ namespace pdfs {
 // x); TY rows, R rows per compute warp: {tx, ty, rows per warp}.  Bricks
 // (tile3d.cuh) are 16 x 16 x BZ: {16, 16, 0, BZ}.
 // Bricks may also be 16 x 8 x BZ.  Pencils (pencil.cuh) are 16 x 16
-// cross-sections marched along z: {16, 16, 0, 16, 1}; their block-masked
-// sweeps run on 16 x 16 x 16 bricks.
+// cross-sections marched along z: {16, 16, 0, BZ, 1}; their block-masked
+// sweeps run on 16 x 16 x BZ bricks.
 static const TileShape kT32[] = {{32, 8, 2},  {32, 8, 4},  {32, 16, 4},     {32, 8, 1},      {32, 4, 2},
-                                 {32, 6, 1},  {32, 10, 1}, {16, 16, 0, 16}, {16, 16, 0, 32}, {16, 16, 0, 16, 1},
+                                 {32, 6, 1},  {32, 10, 1}, {16, 16, 0, 16}, {16, 16, 0, 32}, {16, 16, 0, 32, 1},
                                  {16, 8, 0, 48}};
 // tile 4 (32 x 6, one row per warp) exists for the fast and mixed arithmetic
 static const TileShape kT64[] = {{32, 4, 1},      {32, 4, 2},         {32, 8, 2},     {32, 6, 1},
