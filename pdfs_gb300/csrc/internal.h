@@ -134,6 +134,8 @@ struct pdfs_ctx {
   double *in64 = nullptr;   // exact input, internal FP64 layout (also the polish cap)
   double *u64 = nullptr;    // FP64 working field (FP32 pairs under PDFS_ARITH_PAIR)
   double *cap2 = nullptr;   // the polish cap as FP32 pairs (PDFS_ARITH_PAIR)
+  double *bcap64 = nullptr; // polish: per 8^3 block, the smallest cap of its updated nodes
+  float *bcap32 = nullptr;  // the same rounded down to float
   float *u32 = nullptr;     // FP32 working field
   uint32_t *fmask = nullptr;
   void *stage = nullptr;    // reference-layout staging buffer for host transfers

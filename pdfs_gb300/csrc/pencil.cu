@@ -35,7 +35,8 @@ static cudaError_t launch_pc(const SweepArgs &a, const Layout &L, int sms, cudaS
 
 cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
                                  cudaStream_t st, int *g) {
-  if (L.tx != 16 || L.ty != 16 || L.xo != 0 || a.blk_active || a.blk_chg || !a.pmail || a.prow < a.nz + 15)
+  if (L.tx != 16 || L.ty != 16 || L.xo != 0 || a.blk_active || a.blk_chg || !a.pmail || a.prow < a.nz + 15 ||
+      (which == 2 && (!a.bcap64 || !a.bcap32)))
     return cudaErrorInvalidValue;
   if (which == 0)
     return iso ? launch_pc<float, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)

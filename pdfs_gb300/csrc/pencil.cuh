@@ -54,7 +54,6 @@ struct PcGeo {
   static constexpr int NT = NC + 64;       // and the loader and face warps
   static constexpr int WV = (int)sizeof(T) / 4 > 1 ? 2 : 1;  // mailbox words per value (32 value bits each)
   static constexpr int C = 8;              // levels the face warp prepares per round, at most
-  static constexpr int CP = 4;             // replace-update: caps prefetched ahead (registers)
   static constexpr size_t OFF_BAR = (size_t)D * SLOT_BYTES;
   static constexpr size_t BYTES = OFF_BAR + (size_t)D * 8 + 16;
   static_assert(SLOT_BYTES % 128 == 0, "TMA destinations stay 128-byte aligned");
@@ -122,7 +121,7 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
                                                                const __grid_constant__ CUtensorMap tm_mask,
                                                                const __grid_constant__ SweepArgs a) {
   using G = PcGeo<T>;
-  constexpr int BX = G::BX, BY = G::BY, W = G::W, SK = G::SK, D = G::D, CP = G::CP;
+  constexpr int BX = G::BX, BY = G::BY, W = G::W, SK = G::SK, D = G::D;
   constexpr int SE = (int)(G::SLOT_BYTES / sizeof(T));  // slot stride in elements
   extern __shared__ __align__(1024) unsigned char sm[];
   T *ring = reinterpret_cast<T *>(sm);
@@ -291,13 +290,21 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       T *__restrict__ u = reinterpret_cast<T *>(a.u);
       const T *__restrict__ capg = reinterpret_cast<const T *>(a.cap);
       auto gz_of = [&](int lz) { return szd > 0 ? lz + 1 : nz - lz; };
-      T capq[CP];
-      auto cap_at = [&](int lz) -> T {
-        if (MODE != MODE_REPLACE || !vxy || lz >= nz) return T(0);
-        return __ldg(capg + (long long)gz_of(lz) * plane + grow);
+      // replace-update: the cap bound of my node's 8^3 block, and of the next
+      // block in sweep order (loaded one block ahead)
+      using CB = CapBound<T, ARITH>;
+      typename CB::type bcur = 0, bnxt = 0;
+      int bzc = 0;
+      const long long bxy = (long long)((y0 - 1 + gy) >> 3) * a.nbx + ((x0 - 1 + gx) >> 3);
+      const int dbz = szd > 0 ? 1 : -1;
+      auto bnd_at = [&](int bz) -> typename CB::type {
+        return (bz >= 0 && bz < a.nbz) ? CB::load(a, (long long)bz * a.nby * a.nbx + bxy) : typename CB::type(0);
       };
-#pragma unroll
-      for (int q = 0; q < CP; ++q) capq[q] = cap_at(q);
+      if (MODE == MODE_REPLACE && vxy) {
+        bzc = (gz_of(0) - 1) >> 3;
+        bcur = bnd_at(bzc);
+        bnxt = bnd_at(bzc + dbz);
+      }
       int sl = (1 - lxy) % D;  // slot of my node's plane (lz + 1) at level 0
       if (sl < 0) sl += D;
       int ready = 0;  // thread 0: levels below it are prepared (re-read only when reached)
@@ -343,10 +350,24 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
               const uint32_t w = *reinterpret_cast<const uint32_t *>(sm + (size_t)sl * G::SLOT_BYTES + mbyte);
               act = !((w >> mshift) & 1u);
             }
+            if constexpr (MODE == MODE_REPLACE) {
+              // my nodes are consecutive in sweep order: the block moves one step at a time
+              const int bz = (gz_of(lz) - 1) >> 3;
+              if (bz != bzc) {
+                bzc = bz;
+                bcur = bnxt;
+                bnxt = bnd_at(bz + dbz);
+              }
+            }
             T fin = cv;  // the node's value at the end of the sweep
             if (act) {
               const T gv = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
-              const T nv = MODE == MODE_REPLACE ? vmin<T, ARITH>(capq[0], gv) : vmin<T, ARITH>(cv, gv);
+              T nv;
+              if constexpr (MODE == MODE_REPLACE) {
+                nv = CB::below(gv, bcur) ? gv : vmin<T, ARITH>(__ldg(capg + (long long)gz_of(lz) * plane + grow), gv);
+              } else {
+                nv = vmin<T, ARITH>(cv, gv);
+              }
               if (vdiffers<T, ARITH>(nv, cv)) {
                 fin = nv;
                 cur[orow] = nv;
@@ -357,11 +378,6 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
             }
             if (mx) mail_put<T>(xmail + ((size_t)(lz + ly) * 16 + ly) * G::WV, fin, epoch);
             if (my) mail_put<T>(ymail + ((size_t)(lz + lx) * 16 + lx) * G::WV, fin, epoch);
-          }
-          if (MODE == MODE_REPLACE) {
-#pragma unroll
-            for (int q = 0; q + 1 < CP; ++q) capq[q] = capq[q + 1];
-            capq[CP - 1] = cap_at(lz + CP);
           }
         }
         sl = sl == D - 1 ? 0 : sl + 1;

@@ -157,6 +157,33 @@ __global__ void k_unpack_pair(const double *__restrict__ src, Layout L, const do
   }
 }
 
+// Per 8^3 block: the smallest input value (the replace-update's cap) of the
+// nodes the sweeps update (+inf if every node is frozen), and the same rounded
+// down to float.  One warp per block, one lane per (x, y) pair of a row.
+__global__ void k_block_capmin(const double *__restrict__ in64, Layout L, const uint32_t *__restrict__ fmask,
+                               MaskLayout M, int nx, int ny, int nz, int nbx, int nby, int nbz,
+                               double *__restrict__ b64, float *__restrict__ b32) {
+  const long long nb = (long long)nbx * nby * nbz;
+  const int lane = threadIdx.x & 31;
+  for (long long b = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; b < nb;
+       b += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long long)nbx * nby));
+    double m = INFINITY;
+    for (int i = lane; i < 512; i += 32) {
+      const int x = 1 + bx * 8 + (i & 7), y = 1 + by * 8 + ((i >> 3) & 7), z = 1 + bz * 8 + (i >> 6);
+      if (x > nx || y > ny || z > nz) continue;
+      if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
+      m = fmin(m, in64[L.index(x, y, z)]);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if (lane == 0) {
+      b64[b] = m;
+      b32[b] = __double2float_rd(m);
+    }
+  }
+}
+
 // uint8 mask in the reference layout -> frozen bitmask (interior nodes only)
 __global__ void k_pack_mask(const uint8_t *__restrict__ m, uint32_t *__restrict__ bits, MaskLayout M, int nx,
                             int ny) {
@@ -347,6 +374,12 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if (o.arith == PDFS_ARITH_PAIR && o.precision == PDFS_PREC_FP32_POLISH64 &&
       (e = cudaMalloc(&c->cap2, c->L64.elems * 8)) != cudaSuccess)
     return fail(e);
+  // polish: the per-block cap bounds
+  if (o.precision == PDFS_PREC_FP32_POLISH64) {
+    const size_t nb = (size_t)((g->nx + 7) / 8) * ((g->ny + 7) / 8) * ((g->nz + 7) / 8);
+    if ((e = cudaMalloc(&c->bcap64, nb * 8)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&c->bcap32, nb * 4)) != cudaSuccess) return fail(e);
+  }
   if (need32 && (e = cudaMalloc(&c->u32, c->L32.elems * 4)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&c->fmask, c->M.words * 4)) != cudaSuccess) return fail(e);
   {
@@ -448,6 +481,8 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   cudaFree(c->in64);
   cudaFree(c->u64);
   cudaFree(c->cap2);
+  cudaFree(c->bcap64);
+  cudaFree(c->bcap32);
   cudaFree(c->u32);
   cudaFree(c->fmask);
   cudaFree(c->stage);
@@ -534,6 +569,11 @@ static int load_impl(pdfs_ctx *c, const double *field, const uint8_t *frozen, do
     k_to_pair<<<4 * c->sms, 256, 0, c->st>>>(c->in64, c->cap2, c->L64.elems);
     CK(cudaGetLastError());
   }
+  if (c->bcap64) {
+    k_block_capmin<<<8 * c->sms, 256, 0, c->st>>>(c->in64, c->L64, use_mask ? c->fmask : nullptr, c->M, g.nx, g.ny,
+                                                   g.nz, c->nbx, c->nby, c->nbz, c->bcap64, c->bcap32);
+    CK(cudaGetLastError());
+  }
   CK(cudaEventRecord(c->e1, c->st));
   CK(cudaStreamSynchronize(c->st));
   if (ms_h2d) *ms_h2d = ms_between(c->e0, c->e1);
@@ -583,6 +623,8 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   a.blk_active = active;
   a.blk_chg = blk_chg;
   a.cap = which == 2 ? (c->cap2 ? (const void *)c->cap2 : (const void *)c->in64) : nullptr;
+  a.bcap64 = which == 2 ? c->bcap64 : nullptr;
+  a.bcap32 = which == 2 ? c->bcap32 : nullptr;
   a.nbx = c->nbx;
   a.nby = c->nby;
   a.nbz = c->nbz;

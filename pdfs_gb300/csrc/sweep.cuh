@@ -45,6 +45,7 @@
 #include <cuda.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "godunov.cuh"
 
@@ -92,6 +93,11 @@ struct SweepArgs {
   // 64-bit words, [pencil][face][prow diagonals][16][words per value]
   unsigned long long *pmail;
   int prow;
+  // replace-update on bricks and pencils: per 8^3 block, the smallest cap of
+  // its updated nodes (+inf if none), exact and rounded down to float.  A new
+  // value below it is below every cap of the block, so the cap is not read.
+  const double *bcap64;
+  const float *bcap32;
 };
 
 // A batched sweep: tickets enumerate (grid, local column) pairs, each grid's
@@ -237,6 +243,28 @@ __device__ __forceinline__ T vmax_nonneg(T a, T b) {  // a, b >= 0
   else
     return fmax(a, b);
 }
+
+// The cap bound of a block in the form a variant compares with: float for
+// FP32 pairs (rounded down), double otherwise.
+template <class T, int ARITH>
+struct CapBound {
+  using type = typename std::conditional<sizeof(T) == 8 && ARITH == ARITH_PAIR, float, double>::type;
+  __device__ __forceinline__ static type load(const SweepArgs &a, long long b) {
+    if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+      return __ldg(a.bcap32 + b);
+    else
+      return __ldg(a.bcap64 + b);
+  }
+  // v < bound, so min(cap, v) == v for every cap of the block
+  __device__ __forceinline__ static bool below(T v, type bnd) {
+    if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+      return p_hi(v) < bnd;  // hi < the rounded-down bound: hi + lo is below the exact one
+    else if constexpr (sizeof(T) == 8 && ARITH == ARITH_MIXED)
+      return dkey(v) < dkey(bnd);
+    else
+      return (double)v < bnd;
+  }
+};
 
 // A node's change as a kernel accumulates it: relative for FP32, absolute
 // for FP64, absolute as the pair (|change|, 0) for FP32 pairs.

@@ -69,7 +69,8 @@ static cudaError_t dispatch_t3(int which, int arith, bool iso, const SweepArgs &
 
 cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L,
                                 int sms, cudaStream_t st, int *g) {
-  if (!a.tflag || !a.torder || a.ntx < 1 || a.nty < 1 || a.ntz < 1 || L.ty != by || L.tx != 16 || L.xo != 0)
+  if (!a.tflag || !a.torder || a.ntx < 1 || a.nty < 1 || a.ntz < 1 || L.ty != by || L.tx != 16 || L.xo != 0 ||
+      (which == 2 && (!a.bcap64 || !a.bcap32)))
     return cudaErrorInvalidValue;
   if (by == 16 && bz == 16) return dispatch_t3<16, 16>(which, arith, iso, a, L, sms, st, g);
   if (by == 16 && bz == 32) return dispatch_t3<16, 32>(which, arith, iso, a, L, sms, st, g);

@@ -50,7 +50,6 @@ struct T3Geo {
   static constexpr int NL = BX + BY + BZ - 2;  // levels of one brick
   static constexpr int NT = BX * BY;      // one thread per (x, y) of the brick
   static constexpr int NZB = BZ / 8;      // 8^3 scheduler blocks per brick column
-  static constexpr int CP = 4;            // replace-update: caps prefetched ahead (registers)
   static constexpr unsigned BOX_BYTES = (unsigned)(W * RY * RZ * sizeof(T));
   static constexpr size_t OFF_MASK = ((size_t)BOX_BYTES + 127) & ~size_t(127);
   static constexpr size_t OFF_BAR = OFF_MASK + (size_t)BZ * BY * 4;
@@ -68,7 +67,7 @@ template <class T, int BY_, int BZ, int MODE, int ARITH, bool ISO>
 __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                             const __grid_constant__ SweepArgs a) {
   using G = T3Geo<T, BY_, BZ>;
-  constexpr int BX = G::BX, BY = G::BY, W = G::W, PL = G::PL, NL = G::NL, NZB = G::NZB, CP = G::CP;
+  constexpr int BX = G::BX, BY = G::BY, W = G::W, PL = G::PL, NL = G::NL, NZB = G::NZB;
   extern __shared__ __align__(1024) unsigned char sm[];
   T *box = reinterpret_cast<T *>(sm);
   uint32_t *smask = reinterpret_cast<uint32_t *>(sm + G::OFF_MASK);  // [BZ][BY] frozen words of the brick
@@ -191,16 +190,15 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       }
     }
     const long long gbase = (long long)z0 * plane + (long long)(y0 + gyl) * px + (x0 + gxl);
-    // replace-update caps of my first CP nodes (sweep order) from the first level run
-    T capq[CP];
-    auto cap_at = [&](int lz) -> T {
-      const int gz = szd > 0 ? lz : BZ - 1 - lz;
-      if (MODE != MODE_REPLACE || !vxy || lz >= BZ || gz >= zcnt) return T(0);
-      return __ldg(capg + gbase + (long long)gz * plane);
-    };
-    const int lz_first = max(0, lev0 - (lx + ly));
+    // replace-update: the cap bounds of my column's 8^3 blocks in this brick
+    using CB = CapBound<T, ARITH>;
+    typename CB::type bnd[NZB];
 #pragma unroll
-    for (int q = 0; q < CP; ++q) capq[q] = cap_at(lz_first + q);
+    for (int q = 0; q < NZB; ++q) {
+      bnd[q] = 0;
+      if (MODE == MODE_REPLACE && vxy && bk * NZB + q < a.nbz)
+        bnd[q] = CB::load(a, ((long long)(bk * NZB + q) * a.nby + ((y0 - 1 + gyl) >> 3)) * a.nbx + ((x0 - 1 + gxl) >> 3));
+    }
 
     // wait for the upwind bricks (lanes 0..2 of warp 0, one each)
     bool ok = true;
@@ -295,7 +293,16 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
           if (masked && act) act = !((smask[gz * BY + gyl] >> mshift) & 1u);
           if (act) {
             const T g = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
-            const T nv = MODE == MODE_REPLACE ? vmin<T, ARITH>(capq[0], g) : vmin<T, ARITH>(cv, g);
+            T nv;
+            if constexpr (MODE == MODE_REPLACE) {
+              typename CB::type b = bnd[0];
+#pragma unroll
+              for (int q = 1; q < NZB; ++q)
+                if ((gz >> 3) == q) b = bnd[q];
+              nv = CB::below(g, b) ? g : vmin<T, ARITH>(__ldg(capg + gbase + (long long)gz * plane), g);
+            } else {
+              nv = vmin<T, ARITH>(cv, g);
+            }
             if (vdiffers<T, ARITH>(nv, cv)) {
               box[o] = nv;
               u[gbase + (long long)gz * plane] = nv;
@@ -309,11 +316,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
             }
           }
         }
-        if (MODE == MODE_REPLACE) {
-#pragma unroll
-          for (int q = 0; q + 1 < CP; ++q) capq[q] = capq[q + 1];
-          capq[CP - 1] = cap_at(lz + CP);
-        }
+
       }
       __syncthreads();
     }

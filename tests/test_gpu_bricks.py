@@ -327,3 +327,33 @@ def test_pair_learned_scheduler_polish():
               tol=1e-6, max_sweeps=200, scheduler=L.SCHED_LEARNED)
     O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
     assert rel_err(a, b, 1.0) <= 1e-6
+
+
+@pytest.mark.parametrize("arith", [L.ARITH_MIXED, L.ARITH_PAIR])
+def test_polish_binding_caps(arith):
+    """Replace-update where the caps bind: 3 % of the updated nodes start from
+    small finite values.  Bricks and pencils read a cap only when the new value
+    is not below its block's smallest cap; the result must not depend on it
+    (bricks, pencils and, for the mixed arithmetic, columns give the same bits)."""
+    w = W.random_spheres(70, 60, 50, 1.0, 1.0, 1.0, 6, 3.0, 12.0, seed=81)
+    f = w.field.copy()
+    rng = np.random.default_rng(3)
+    free = (w.frozen == 0)
+    free[0, :, :] = free[-1, :, :] = False
+    free[:, 0, :] = free[:, -1, :] = False
+    free[:, :, 0] = free[:, :, -1] = False
+    pick = free & (rng.random(f.shape) < 0.03)
+    f[pick] = rng.uniform(0.0, 6.0, int(pick.sum()))
+    sp = (w.dx, w.dy, w.dz)
+    tiles = [9 | B64, P32 | P64] + ([4 | (4 << 8)] if arith == L.ARITH_MIXED else [])
+    out = []
+    for tile in tiles:
+        a = f.copy()
+        api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=arith,
+                  tol=1e-6, max_sweeps=200, tile=tile)
+        out.append(a)
+    for o in out[1:]:
+        assert same(out[0], o)
+    b = f.copy()
+    O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
+    assert rel_err(out[0], b, 1.0) <= 1e-6
