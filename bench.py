@@ -479,7 +479,10 @@ def main():
         per_launch = w.interior * (8 + mask_b)
         dur = k32 / max(s32, 1)
     else:
-        per_launch = w.interior * (16 + 8 + mask_b) if prec == L.PREC_FP32_POLISH64 else w.interior * (16 + mask_b)
+        # 2 * sizeof(T) per voxel-update plus the frozen-mask bit; the polish's cap
+        # reads are not algorithmic bytes (bricks and pencils skip them where a
+        # block's smallest cap is above the new value)
+        per_launch = w.interior * (16 + mask_b)
         dur = k64 / max(s64, 1)
     achieved = per_launch / (dur / 1e3) / 1e9 if dur > 0 else 0.0
     kname = kernel_name(dominant, st["tile"], prec, arith)
