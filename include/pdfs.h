@@ -58,8 +58,9 @@ enum {
   PDFS_ARITH_PAIR = 3,      /* as MIXED, with the field, minima and update held as FP32
                                pairs hi + lo (48 significant bits, Knuth/Dekker error-free
                                sums) instead of FP64: no FP64 instruction in the sweeps.
-                               FP64 bricks only (tile 5, the default); frozen nodes and
-                               the halo come back as the exact FP64 input.  Same tol rule */
+                               FP64 bricks and pencils only (tiles 5-8; 6 is the
+                               default); frozen nodes and the halo come back as the
+                               exact FP64 input.  Same tol rule                          */
 };
 
 /* Which nodes are updated. */

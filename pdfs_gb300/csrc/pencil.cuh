@@ -44,7 +44,7 @@ struct PcGeo {
   static constexpr int RY = BY + 2;        // slot rows: y0-1 .. y0+BY
   static constexpr int SK = BX + BY - 2;   // thread (15, 15) trails thread (0, 0) by SK planes
   // planes requested ahead of use; FP32 publishes its done count every other level
-  static constexpr int LOOK = sizeof(T) == 4 ? 7 : 3;
+  static constexpr int LOOK = sizeof(T) == 4 ? 11 : 7;
   static constexpr int PUB = sizeof(T) == 4 ? 1 : 0;
   static constexpr int D = SK + 3 + LOOK;  // ring slots
   static constexpr unsigned FIELD_BYTES = (unsigned)(W * RY * sizeof(T));

@@ -320,14 +320,14 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
 // FP32: 16 x 16 pencils (tile 10: 3.6 ms per 768^3 sweep, against 3.9 ms for
 // 16 x 16 x 32 bricks and 7.9 ms for the best column tile); their masked
 // sweeps run on 16 x 16 x 32 bricks.
-// FP64: bricks (tile 5) for the mixed arithmetic (14.4 ms per 768^3 polish
-// sweep against 15.9 ms for 32 x 6 columns) and for FP32 pairs (bricks
-// only); the reference and fast arithmetic are bound by the FP64 pipe and
-// run 2.3x faster on 32 x 4 columns (16 against 36 ms per 384^3 sweep).
+// FP64: pencils (tile 6) for every arithmetic: 6.9 ms per 768^3 pair polish
+// sweep, against 8.1 ms for 16 x 16 x 16 bricks and 15.9 ms for mixed 32 x 6
+// columns; 51 ms per plain fast-arithmetic sweep against 55 ms for 32 x 4
+// columns (the reference arithmetic is even: both are FP64-pipe-bound).
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
   c->t32 = t32 ? t32 : 10;
-  c->t64 = t64 ? t64 : ((c->o.arith == PDFS_ARITH_MIXED || c->o.arith == PDFS_ARITH_PAIR) ? 5 : 1);
+  c->t64 = t64 ? t64 : 6;
 }
 
 extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_ctx **out) {
