@@ -239,6 +239,12 @@ __device__ __forceinline__ bool p_lt(double a, double b) {
   const float ah = p_hi(a), bh = p_hi(b);
   return ah < bh || (ah == bh && p_lo(a) < p_lo(b));
 }
+// the pair nearest a double (infinite, or beyond the float range: (hi, 0))
+__device__ __forceinline__ double p_from_double(double d) {
+  const float hi = (float)d;
+  if (!(fabsf(hi) < INFINITY)) return p_make(hi, 0.0f);
+  return p_make(hi, (float)(d - (double)hi));
+}
 // the reference's min(a, b) = a < b ? a : b, on pairs
 __device__ __forceinline__ double pmin(double a, double b) { return p_lt(a, b) ? a : b; }
 // a - b rounded to float (a, b not both infinite)

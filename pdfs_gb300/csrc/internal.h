@@ -133,7 +133,6 @@ struct pdfs_ctx {
   pdfs::MaskLayout M;
   double *in64 = nullptr;   // exact input, internal FP64 layout (also the polish cap)
   double *u64 = nullptr;    // FP64 working field (FP32 pairs under PDFS_ARITH_PAIR)
-  double *cap2 = nullptr;   // the polish cap as FP32 pairs (PDFS_ARITH_PAIR)
   double *bcap64 = nullptr; // polish: per 8^3 block, the smallest cap of its updated nodes
   float *bcap32 = nullptr;  // the same rounded down to float
   float *u32 = nullptr;     // FP32 working field
@@ -163,6 +162,10 @@ struct pdfs_ctx {
   bool loaded = false, has_mask = false;
   int last_prec = -1;      // which working field holds the last result
   cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr, q0 = nullptr, q1 = nullptr;
+  // load / store pipeline: slab copies on st, layout kernels on st2
+  cudaStream_t st2 = nullptr;
+  static constexpr int kSlabs = 32;
+  cudaEvent_t slab_ev[kSlabs + 1] = {};
   double kern_ms = 0.0;  // accumulated sweep-kernel time since the last reset
   int launches = 0;      // kernels launched since the last reset
 };

@@ -364,7 +364,8 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
               const T gv = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
               T nv;
               if constexpr (MODE == MODE_REPLACE) {
-                nv = CB::below(gv, bcur) ? gv : vmin<T, ARITH>(__ldg(capg + (long long)gz_of(lz) * plane + grow), gv);
+                nv = CB::below(gv, bcur) ? gv
+                                         : vmin<T, ARITH>(cap_value<T, ARITH>(capg + (long long)gz_of(lz) * plane + grow), gv);
               } else {
                 nv = vmin<T, ARITH>(cv, gv);
               }

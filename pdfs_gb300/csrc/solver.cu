@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstddef>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "internal.h"
@@ -53,8 +54,8 @@ __global__ void k_fill(T *p, size_t n, T v) {
 
 // reference layout (double) -> internal layout of T
 template <class T>
-__global__ void k_pack(const double *__restrict__ ref, T *__restrict__ dst, int nx, int ny, Layout L) {
-  const int y = blockIdx.x, z = blockIdx.y;
+__global__ void k_pack(const double *__restrict__ ref, T *__restrict__ dst, int nx, int ny, Layout L, int z0) {
+  const int y = blockIdx.x, z = blockIdx.y + z0;
   const double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
   T *out = dst + L.index(0, y, z);
   for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) out[x] = (T)row[x];
@@ -64,8 +65,9 @@ __global__ void k_pack(const double *__restrict__ ref, T *__restrict__ dst, int 
 // (mask bit set) take the exact FP64 input instead of the rounded value.
 template <class T>
 __global__ void k_unpack(const T *__restrict__ src, Layout L, const double *__restrict__ in64, Layout L64,
-                         const uint32_t *__restrict__ fmask, MaskLayout M, double *__restrict__ ref, int nx, int ny) {
-  const int y = blockIdx.x, z = blockIdx.y;
+                         const uint32_t *__restrict__ fmask, MaskLayout M, double *__restrict__ ref, int nx, int ny,
+                         int z0) {
+  const int y = blockIdx.x, z = blockIdx.y + z0;
   double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
   const T *s = src + L.index(0, y, z);
   for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
@@ -105,15 +107,10 @@ __global__ void k_widen(const float *__restrict__ u32, Layout L32, const double 
   }
 }
 
-// FP32 pairs (godunov.cuh): the pair nearest a double, and its value
-__device__ __forceinline__ double to_pair(double d) {
-  const float hi = (float)d;
-  if (!(fabsf(hi) < INFINITY)) return p_make(hi, 0.0f);  // infinite, or beyond the float range
-  return p_make(hi, (float)(d - (double)hi));
-}
+__device__ __forceinline__ double to_pair(double d) { return p_from_double(d); }
 
-// every element of an FP64 buffer -> the pair nearest it (the polish cap; the
-// start of an FP64-precision solve in pair arithmetic)
+// every element of an FP64 buffer -> the pair nearest it (the start of an
+// FP64-precision solve in pair arithmetic)
 __global__ void k_to_pair(const double *__restrict__ src, double *__restrict__ dst, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     dst[i] = to_pair(src[i]);
@@ -141,8 +138,8 @@ __global__ void k_widen_pair(const float *__restrict__ u32, Layout L32, const do
 // updated nodes; frozen nodes and the halo take the exact FP64 input
 __global__ void k_unpack_pair(const double *__restrict__ src, Layout L, const double *__restrict__ in64,
                               const uint32_t *__restrict__ fmask, MaskLayout M, double *__restrict__ ref, int nx,
-                              int ny, int nz) {
-  const int y = blockIdx.x, z = blockIdx.y;
+                              int ny, int nz, int z0) {
+  const int y = blockIdx.x, z = blockIdx.y + z0;
   double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
   for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
     const long long i = L.index(x, y, z);
@@ -159,24 +156,34 @@ __global__ void k_unpack_pair(const double *__restrict__ src, Layout L, const do
 
 // Per 8^3 block: the smallest input value (the replace-update's cap) of the
 // nodes the sweeps update (+inf if every node is frozen), and the same rounded
-// down to float.  One warp per block, one lane per (x, y) pair of a row.
+// down to float.  One warp per block, blocks b0 .. b1-1: lane (x, y) = (lane %
+// 8, lane / 8) of a 8 x 4 quarter plane loads its 16 nodes before reducing.
 __global__ void k_block_capmin(const double *__restrict__ in64, Layout L, const uint32_t *__restrict__ fmask,
-                               MaskLayout M, int nx, int ny, int nz, int nbx, int nby, int nbz,
+                               MaskLayout M, int nx, int ny, int nz, int nbx, int nby, long long b0, long long b1,
                                double *__restrict__ b64, float *__restrict__ b32) {
-  const long long nb = (long long)nbx * nby * nbz;
   const int lane = threadIdx.x & 31;
-  for (long long b = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; b < nb;
+  for (long long b = b0 + ((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); b < b1;
        b += ((long long)gridDim.x * blockDim.x) >> 5) {
     const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long long)nbx * nby));
-    double m = INFINITY;
-    for (int i = lane; i < 512; i += 32) {
-      const int x = 1 + bx * 8 + (i & 7), y = 1 + by * 8 + ((i >> 3) & 7), z = 1 + bz * 8 + (i >> 6);
-      if (x > nx || y > ny || z > nz) continue;
-      if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
-      m = fmin(m, in64[L.index(x, y, z)]);
-    }
+    const int x = 1 + bx * 8 + (lane & 7);
+    double v[16];
+    bool use[16];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, off));
+    for (int k = 0; k < 16; ++k) {
+      const int y = 1 + by * 8 + (lane >> 3) + 4 * (k & 1), z = 1 + bz * 8 + (k >> 1);
+      use[k] = x <= nx && y <= ny && z <= nz;
+      v[k] = use[k] ? in64[L.index(x, y, z)] : INFINITY;
+      if (use[k] && fmask) use[k] = !((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u);
+    }
+    double m = INFINITY;
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      if (use[k] && dkey(v[k]) < dkey(m)) m = v[k];  // integer keys: off the FP64 pipe
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double o = __shfl_xor_sync(0xffffffffu, m, off);
+      m = dkey(o) < dkey(m) ? o : m;
+    }
     if (lane == 0) {
       b64[b] = m;
       b32[b] = __double2float_rd(m);
@@ -286,6 +293,40 @@ extern "C" const char *pdfs_status_string(int s) {
 
 extern "C" const char *pdfs_version(void) { return "pdfs-gb300 0.1 (sm_103a)"; }
 
+// Context buffers come from the device's stream-ordered memory pool, which
+// keeps up to a quarter of the device's memory for the next context: a
+// repeated solve does not pay the allocation of its multi-GB buffers again.
+// An allocation that finds the device full trims the pool and retries.
+static void keep_pool(int dev) {
+  static bool done[64] = {false};
+  if (dev < 0 || dev >= 64 || done[dev]) return;
+  done[dev] = true;
+  cudaMemPool_t pool;
+  size_t fr = 0, tot = 0;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess || cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  cuuint64_t thr = (cuuint64_t)tot / 4;
+  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  cudaGetLastError();
+}
+template <class P>
+static cudaError_t ctx_malloc(pdfs_ctx *c, P **p, size_t bytes) {
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(p), bytes, c->st);
+  if (e != cudaErrorMemoryAllocation) return e;
+  // out of memory: hand what the pool keeps back to the device and try once more
+  cudaGetLastError();
+  cudaMemPool_t pool;
+  if (cudaStreamSynchronize(c->st) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, c->dev) != cudaSuccess)
+    return e;
+  cudaMemPoolTrimTo(pool, 0);
+  return cudaMallocAsync(reinterpret_cast<void **>(p), bytes, c->st);
+}
+static void ctx_free(pdfs_ctx *c, void *p) {
+  if (p) cudaFreeAsync(p, c->st);
+}
+
 static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   if (!g || !o) return PDFS_ERR_INVALID;
   if (g->nx < 1 || g->ny < 1 || g->nz < 1) return PDFS_ERR_INVALID;
@@ -346,6 +387,7 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
     return PDFS_ERR_NO_DEVICE;
   }
   if (o.device < 0 || o.device >= ndev) return PDFS_ERR_INVALID;
+  const auto t_start = std::chrono::steady_clock::now();
   CK(cudaSetDevice(o.device));
   pdfs_ctx *c = new pdfs_ctx();
   c->g = *g;
@@ -363,25 +405,28 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
     pdfs_ctx_destroy(c);
     return rc;
   };
+  std::vector<std::pair<const char *, std::chrono::steady_clock::time_point>> marks;
+  auto mark = [&](const char *what) {
+    if (verbose(o)) marks.emplace_back(what, std::chrono::steady_clock::now());
+  };
   cudaError_t e;
   if ((e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->dev)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  keep_pool(c->dev);
+  mark("stream");
   const bool need32 = o.precision != PDFS_PREC_FP64;
   const bool need64 = o.precision != PDFS_PREC_FP32 || true;  // FP64 input always resident
-  if (need64 && (e = cudaMalloc(&c->in64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
-  if ((o.precision != PDFS_PREC_FP32) && (e = cudaMalloc(&c->u64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
-  // FP32-pair polish: the cap (the input) as pairs
-  if (o.arith == PDFS_ARITH_PAIR && o.precision == PDFS_PREC_FP32_POLISH64 &&
-      (e = cudaMalloc(&c->cap2, c->L64.elems * 8)) != cudaSuccess)
-    return fail(e);
+  if (need64 && (e = ctx_malloc(c, &c->in64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
+  if ((o.precision != PDFS_PREC_FP32) && (e = ctx_malloc(c, &c->u64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
   // polish: the per-block cap bounds
   if (o.precision == PDFS_PREC_FP32_POLISH64) {
     const size_t nb = (size_t)((g->nx + 7) / 8) * ((g->ny + 7) / 8) * ((g->nz + 7) / 8);
-    if ((e = cudaMalloc(&c->bcap64, nb * 8)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc(&c->bcap32, nb * 4)) != cudaSuccess) return fail(e);
+    if ((e = ctx_malloc(c, &c->bcap64, nb * 8)) != cudaSuccess) return fail(e);
+    if ((e = ctx_malloc(c, &c->bcap32, nb * 4)) != cudaSuccess) return fail(e);
   }
-  if (need32 && (e = cudaMalloc(&c->u32, c->L32.elems * 4)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&c->fmask, c->M.words * 4)) != cudaSuccess) return fail(e);
+  if (need32 && (e = ctx_malloc(c, &c->u32, c->L32.elems * 4)) != cudaSuccess) return fail(e);
+  if ((e = ctx_malloc(c, &c->fmask, c->M.words * 4)) != cudaSuccess) return fail(e);
+  mark("fields");
   {
     // per-row progress words and face mailboxes, sized for the larger of the two layouts
     const int nb = mailbox_chunks(g->nz) * kMailboxChunk;
@@ -393,19 +438,21 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
       mb = std::max(mb, ncol * (size_t)nb * (size_t)(L.tx + L.ty) * (size_t)L.esize);
     }
     c->progress_ints = prog;
-    if ((e = cudaMalloc(&c->progress, prog * 4)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc(&c->mailbox, mb)) != cudaSuccess) return fail(e);
+    if ((e = ctx_malloc(c, &c->progress, prog * 4)) != cudaSuccess) return fail(e);
+    if ((e = ctx_malloc(c, &c->mailbox, mb)) != cudaSuccess) return fail(e);
     c->mailbox_bytes = mb;
   }
-  if ((e = cudaMalloc(&c->ticket, 16)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&c->dstat, sizeof(DevStatus))) != cudaSuccess) return fail(e);
+  mark("mailboxes");
+  if ((e = ctx_malloc(c, &c->ticket, 16)) != cudaSuccess) return fail(e);
+  if ((e = ctx_malloc(c, &c->dstat, sizeof(DevStatus))) != cudaSuccess) return fail(e);
   if ((e = cudaHostAlloc(&c->hstat, sizeof(DevStatus), cudaHostAllocDefault)) != cudaSuccess) return fail(e);
+  mark("status");
   c->nbx = (g->nx + 7) / 8;
   c->nby = (g->ny + 7) / 8;
   c->nbz = (g->nz + 7) / 8;
   c->nblocks = (long long)c->nbx * c->nby * c->nbz;
-  if ((e = cudaMalloc(&c->bchg, (size_t)c->nblocks * kRing * 4)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&c->bact, (size_t)c->nblocks)) != cudaSuccess) return fail(e);
+  if ((e = ctx_malloc(c, &c->bchg, (size_t)c->nblocks * kRing * 4)) != cudaSuccess) return fail(e);
+  if ((e = ctx_malloc(c, &c->bact, (size_t)c->nblocks)) != cudaSuccess) return fail(e);
   if (o.scheduler == PDFS_SCHED_LEARNED) {
     const float *blob = o.mlp_weights ? o.mlp_weights : default_mlp_blob();
     std::vector<uint16_t> wb(PDFS_MLP_PARAMS);
@@ -415,11 +462,12 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
       wb[i] = (uint16_t)(u >> 16);
     }
     c->mlp_thr = blob[PDFS_MLP_PARAMS];
-    if ((e = cudaMalloc(&c->mlp_w, PDFS_MLP_PARAMS * 2)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc(&c->bmin, (size_t)c->nblocks * 4)) != cudaSuccess) return fail(e);
-    if ((e = cudaMemcpy(c->mlp_w, wb.data(), PDFS_MLP_PARAMS * 2, cudaMemcpyHostToDevice)) != cudaSuccess)
+    if ((e = ctx_malloc(c, &c->mlp_w, PDFS_MLP_PARAMS * 2)) != cudaSuccess) return fail(e);
+    if ((e = ctx_malloc(c, &c->bmin, (size_t)c->nblocks * 4)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpyAsync(c->mlp_w, wb.data(), PDFS_MLP_PARAMS * 2, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
       return fail(e);
   }
+  mark("blocks");
   {
     // brick tiles: ticket orders and the completion flags (epoch 0 = never)
     size_t nflags = 0;
@@ -432,32 +480,38 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
       nt[2] = (g->nz + ts.bz - 1) / ts.bz;
       std::vector<int> bo = brick_order(nt[0], nt[1], nt[2]);
       int **dst = k ? &c->tord64 : &c->tord32;
-      if ((e = cudaMalloc(dst, bo.size() * 4)) != cudaSuccess) return fail(e);
-      if ((e = cudaMemcpy(*dst, bo.data(), bo.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+      if ((e = ctx_malloc(c, dst, bo.size() * 4)) != cudaSuccess) return fail(e);
+      if ((e = cudaMemcpyAsync(*dst, bo.data(), bo.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+        return fail(e);
       nflags = std::max(nflags, bo.size());
     }
     if (nflags) {
-      if ((e = cudaMalloc(&c->tflag, nflags * 4)) != cudaSuccess) return fail(e);
-      if ((e = cudaMemset(c->tflag, 0, nflags * 4)) != cudaSuccess) return fail(e);
+      if ((e = ctx_malloc(c, &c->tflag, nflags * 4)) != cudaSuccess) return fail(e);
+      if ((e = cudaMemsetAsync(c->tflag, 0, nflags * 4, c->st)) != cudaSuccess) return fail(e);
     }
+    mark("brick orders");
     // pencils: two faces of prow diagonals x 16 entries x 2 words per pencil
     // (tag 0 never matches: epochs start at 1)
     if (s32.pencil || s64.pencil) {
       const size_t ncol = (size_t)((g->nx + 15) / 16) * ((g->ny + 15) / 16);
       c->prow = g->nz + 15;
       const size_t words = ncol * 2 * (size_t)c->prow * 16 * 2;
-      if ((e = cudaMalloc(&c->pmail, words * 8)) != cudaSuccess) return fail(e);
-      if ((e = cudaMemset(c->pmail, 0, words * 8)) != cudaSuccess) return fail(e);
+      if ((e = ctx_malloc(c, &c->pmail, words * 8)) != cudaSuccess) return fail(e);
+      if ((e = cudaMemsetAsync(c->pmail, 0, words * 8, c->st)) != cudaSuccess) return fail(e);
     }
   }
+  mark("pencil mail");
   {
     std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
                      w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
-    if ((e = cudaMalloc(&c->order32, w32.size() * 4)) != cudaSuccess) return fail(e);
-    if ((e = cudaMalloc(&c->order64, w64.size() * 4)) != cudaSuccess) return fail(e);
-    if ((e = cudaMemcpy(c->order32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
-    if ((e = cudaMemcpy(c->order64, w64.data(), w64.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+    if ((e = ctx_malloc(c, &c->order32, w32.size() * 4)) != cudaSuccess) return fail(e);
+    if ((e = ctx_malloc(c, &c->order64, w64.size() * 4)) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpyAsync(c->order32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+      return fail(e);
+    if ((e = cudaMemcpyAsync(c->order64, w64.data(), w64.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+      return fail(e);
   }
+  const auto t_alloc = std::chrono::steady_clock::now();
   // padding outside the halo-padded grid is never written by the sweeps; fill it with +inf once
   if (c->in64) k_fill<double><<<2 * c->sms, 256, 0, c->st>>>(c->in64, c->L64.elems, INFINITY);
   if (c->u64) k_fill<double><<<2 * c->sms, 256, 0, c->st>>>(c->u64, c->L64.elems, INFINITY);
@@ -469,7 +523,21 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((e = cudaEventCreate(&c->k1)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->q0)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->q1)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  for (cudaEvent_t &ev : c->slab_ev)
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) return fail(e);
+  if (verbose(o)) {
+    const auto t_end = std::chrono::steady_clock::now();
+    auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+    fprintf(stderr, "pdfs: create %.1f ms (", ms(t_start, t_end));
+    auto t = t_start;
+    for (auto &m : marks) {
+      fprintf(stderr, "%s %.1f, ", m.first, ms(t, m.second));
+      t = m.second;
+    }
+    fprintf(stderr, "columns %.1f, fills %.1f)\n", ms(t, t_alloc), ms(t_alloc, t_end));
+  }
   *out = c;
   return PDFS_OK;
 }
@@ -477,29 +545,13 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
 extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->dev);
+  void *bufs[] = {(void *)c->in64, (void *)c->u64, (void *)c->bcap64, (void *)c->bcap32, (void *)c->u32,
+                  (void *)c->fmask, (void *)c->stage, (void *)c->order32, (void *)c->order64, (void *)c->tflag,
+                  (void *)c->pmail, (void *)c->tord32, (void *)c->tord64, (void *)c->progress, (void *)c->mailbox,
+                  (void *)c->ticket, (void *)c->dstat, (void *)c->bchg, (void *)c->bact, (void *)c->bmin,
+                  (void *)c->mlp_w};
+  for (void *p : bufs) ctx_free(c, p);
   if (c->st) cudaStreamSynchronize(c->st);
-  cudaFree(c->in64);
-  cudaFree(c->u64);
-  cudaFree(c->cap2);
-  cudaFree(c->bcap64);
-  cudaFree(c->bcap32);
-  cudaFree(c->u32);
-  cudaFree(c->fmask);
-  cudaFree(c->stage);
-  cudaFree(c->order32);
-  cudaFree(c->order64);
-  cudaFree(c->tflag);
-  cudaFree(c->pmail);
-  cudaFree(c->tord32);
-  cudaFree(c->tord64);
-  cudaFree(c->progress);
-  cudaFree(c->mailbox);
-  cudaFree(c->ticket);
-  cudaFree(c->dstat);
-  cudaFree(c->bchg);
-  cudaFree(c->bact);
-  cudaFree(c->bmin);
-  cudaFree(c->mlp_w);
   if (c->hstat) cudaFreeHost(c->hstat);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
@@ -507,6 +559,9 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   if (c->k1) cudaEventDestroy(c->k1);
   if (c->q0) cudaEventDestroy(c->q0);
   if (c->q1) cudaEventDestroy(c->q1);
+  for (cudaEvent_t ev : c->slab_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->st2) cudaStreamDestroy(c->st2);
   if (c->st) cudaStreamDestroy(c->st);
   cudaGetLastError();
   delete c;
@@ -514,15 +569,22 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
 
 static size_t ref_nodes(const pdfs_grid &g) { return (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2); }
 
+// The stage holds a field in the reference layout and, after it, a mask.
 static int ensure_stage(pdfs_ctx *c) {
-  const size_t b = ref_nodes(c->g) * 8;
+  const size_t b = ref_nodes(c->g) * 9;
   if (c->stage_bytes >= b) return PDFS_OK;
-  cudaFree(c->stage);
+  ctx_free(c, c->stage);
   c->stage = nullptr;
   c->stage_bytes = 0;
-  CK(cudaMalloc(&c->stage, b));
+  CK(ctx_malloc(c, &c->stage, b));
   c->stage_bytes = b;
   return PDFS_OK;
+}
+
+// Planes per slab of the load / store pipelines: at most kSlabs slabs.
+static int slab_planes(const pdfs_grid &g) {
+  const int planes = g.nz + 2;
+  return std::max(16, (planes + pdfs_ctx::kSlabs - 1) / pdfs_ctx::kSlabs);
 }
 
 static double ms_between(cudaEvent_t a, cudaEvent_t b) {
@@ -531,52 +593,75 @@ static double ms_between(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
+// Host -> device.  The mask goes first (the cap bounds need it), then the
+// field in z-slabs on c->st; c->st2 packs each slab as it lands and takes the
+// cap bounds of the 8^3 blocks whose planes are all packed, so that only the
+// last slab's kernels trail the copies.
 static int load_impl(pdfs_ctx *c, const double *field, const uint8_t *frozen, double *ms_h2d) {
   if (!c || !field) return PDFS_ERR_INVALID;
   CK(cudaSetDevice(c->dev));
   const pdfs_grid &g = c->g;
   const size_t n = ref_nodes(g);
-  const double *src = field;
+  const size_t plane = (size_t)(g.nx + 2) * (g.ny + 2);
   const bool dev_field = is_device_ptr(field);
   const bool use_mask = c->o.freeze == PDFS_FREEZE_MASK && frozen;
   const bool dev_mask = use_mask && is_device_ptr(frozen);
+  const auto t_start = std::chrono::steady_clock::now();
   int s;
   if (!dev_field || (use_mask && !dev_mask)) {
     if ((s = ensure_stage(c))) return s;
   }
+  const auto t_stage = std::chrono::steady_clock::now();
   CK(cudaEventRecord(c->e0, c->st));
-  if (!dev_field) {
-    CK(cudaMemcpyAsync(c->stage, field, n * 8, cudaMemcpyHostToDevice, c->st));
-    src = (const double *)c->stage;
-  }
-  dim3 grid(g.ny + 2, g.nz + 2);
-  k_pack<double><<<grid, 128, 0, c->st>>>(src, c->in64, g.nx, g.ny, c->L64);
-  CK(cudaGetLastError());
-  CK(cudaMemsetAsync(c->fmask, 0, c->M.words * 4, c->st));
+  CK(cudaStreamWaitEvent(c->st2, c->e0, 0));
+  CK(cudaMemsetAsync(c->fmask, 0, c->M.words * 4, c->st2));
   if (use_mask) {
     const uint8_t *m = frozen;
     if (!dev_mask) {
-      // the stage is re-used for the mask bytes; the stream orders the copy
-      // after k_pack has read the field out of it
-      CK(cudaMemcpyAsync(c->stage, frozen, n, cudaMemcpyHostToDevice, c->st));
-      m = (const uint8_t *)c->stage;
+      m = (const uint8_t *)c->stage + n * 8;
+      CK(cudaMemcpyAsync((void *)m, frozen, n, cudaMemcpyHostToDevice, c->st));
+      CK(cudaEventRecord(c->slab_ev[pdfs_ctx::kSlabs], c->st));
+      CK(cudaStreamWaitEvent(c->st2, c->slab_ev[pdfs_ctx::kSlabs], 0));
     }
     dim3 mg(g.ny, g.nz);
-    k_pack_mask<<<mg, 64, 0, c->st>>>(m, c->fmask, c->M, g.nx, g.ny);
+    k_pack_mask<<<mg, 64, 0, c->st2>>>(m, c->fmask, c->M, g.nx, g.ny);
     CK(cudaGetLastError());
   }
-  if (c->cap2) {
-    k_to_pair<<<4 * c->sms, 256, 0, c->st>>>(c->in64, c->cap2, c->L64.elems);
+  const double *src = dev_field ? field : (const double *)c->stage;
+  const int planes = g.nz + 2, per = dev_field ? planes : slab_planes(g);
+  const long long blocks_per_z = (long long)c->nbx * c->nby;
+  int bz_done = 0;
+  for (int z0 = 0, k = 0; z0 < planes; z0 += per, ++k) {
+    const int z1 = std::min(planes, z0 + per);
+    if (!dev_field) {
+      CK(cudaMemcpyAsync((char *)c->stage + z0 * plane * 8, field + z0 * plane, (size_t)(z1 - z0) * plane * 8,
+                         cudaMemcpyHostToDevice, c->st));
+      CK(cudaEventRecord(c->slab_ev[k], c->st));
+      CK(cudaStreamWaitEvent(c->st2, c->slab_ev[k], 0));
+    }
+    dim3 grid(g.ny + 2, z1 - z0);
+    k_pack<double><<<grid, 128, 0, c->st2>>>(src, c->in64, g.nx, g.ny, c->L64, z0);
     CK(cudaGetLastError());
+    if (c->bcap64) {
+      // block bz holds planes 8 bz + 1 .. min(8 bz + 8, nz): complete once plane z1 - 1 is packed
+      const int bz_ready = z1 >= g.nz + 1 ? c->nbz : std::min(c->nbz, (z1 - 1) / 8);
+      if (bz_ready > bz_done) {
+        k_block_capmin<<<8 * c->sms, 256, 0, c->st2>>>(c->in64, c->L64, use_mask ? c->fmask : nullptr, c->M, g.nx,
+                                                        g.ny, g.nz, c->nbx, c->nby, bz_done * blocks_per_z,
+                                                        bz_ready * blocks_per_z, c->bcap64, c->bcap32);
+        CK(cudaGetLastError());
+        bz_done = bz_ready;
+      }
+    }
   }
-  if (c->bcap64) {
-    k_block_capmin<<<8 * c->sms, 256, 0, c->st>>>(c->in64, c->L64, use_mask ? c->fmask : nullptr, c->M, g.nx, g.ny,
-                                                   g.nz, c->nbx, c->nby, c->nbz, c->bcap64, c->bcap32);
-    CK(cudaGetLastError());
-  }
-  CK(cudaEventRecord(c->e1, c->st));
+  CK(cudaEventRecord(c->e1, c->st2));
+  CK(cudaStreamWaitEvent(c->st, c->e1, 0));
   CK(cudaStreamSynchronize(c->st));
   if (ms_h2d) *ms_h2d = ms_between(c->e0, c->e1);
+  if (verbose(c->o))
+    fprintf(stderr, "pdfs: load %.1f ms (stage allocation %.1f, copies and layout kernels %.1f)\n",
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count(),
+            std::chrono::duration<double, std::milli>(t_stage - t_start).count(), ms_between(c->e0, c->e1));
   c->has_mask = use_mask;
   c->loaded = true;
   c->last_prec = -1;
@@ -622,7 +707,7 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   a.maxchg = &c->dstat->chg;
   a.blk_active = active;
   a.blk_chg = blk_chg;
-  a.cap = which == 2 ? (c->cap2 ? (const void *)c->cap2 : (const void *)c->in64) : nullptr;
+  a.cap = which == 2 ? (const void *)c->in64 : nullptr;  // FP64; pair kernels convert the rare cap they read
   a.bcap64 = which == 2 ? c->bcap64 : nullptr;
   a.bcap32 = which == 2 ? c->bcap32 : nullptr;
   a.nbx = c->nbx;
@@ -881,10 +966,13 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   return r;
 }
 
+// Device -> host: c->st converts the result to the reference layout slab by
+// slab, c->st2 copies each converted slab out.
 static int store_impl(pdfs_ctx *c, double *field, double *ms_d2h) {
   if (!c || !field || c->last_prec < 0) return PDFS_ERR_INVALID;
   CK(cudaSetDevice(c->dev));
   const pdfs_grid &g = c->g;
+  const size_t plane = (size_t)(g.nx + 2) * (g.ny + 2);
   const bool dev = is_device_ptr(field);
   double *dst = field;
   int s;
@@ -893,16 +981,29 @@ static int store_impl(pdfs_ctx *c, double *field, double *ms_d2h) {
     dst = (double *)c->stage;
   }
   CK(cudaEventRecord(c->e0, c->st));
-  dim3 grid(g.ny + 2, g.nz + 2);
   const uint32_t *fm = c->has_mask ? c->fmask : nullptr;
-  if (c->last_prec == 1 && c->o.arith == PDFS_ARITH_PAIR)
-    k_unpack_pair<<<grid, 128, 0, c->st>>>(c->u64, c->L64, c->in64, fm, c->M, dst, g.nx, g.ny, g.nz);
-  else if (c->last_prec == 1)
-    k_unpack<double><<<grid, 128, 0, c->st>>>(c->u64, c->L64, c->in64, c->L64, nullptr, c->M, dst, g.nx, g.ny);
-  else
-    k_unpack<float><<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->L64, fm, c->M, dst, g.nx, g.ny);
-  CK(cudaGetLastError());
-  if (!dev) CK(cudaMemcpyAsync(field, c->stage, ref_nodes(g) * 8, cudaMemcpyDeviceToHost, c->st));
+  const int planes = g.nz + 2, per = dev ? planes : slab_planes(g);
+  for (int z0 = 0, k = 0; z0 < planes; z0 += per, ++k) {
+    const int z1 = std::min(planes, z0 + per);
+    dim3 grid(g.ny + 2, z1 - z0);
+    if (c->last_prec == 1 && c->o.arith == PDFS_ARITH_PAIR)
+      k_unpack_pair<<<grid, 128, 0, c->st>>>(c->u64, c->L64, c->in64, fm, c->M, dst, g.nx, g.ny, g.nz, z0);
+    else if (c->last_prec == 1)
+      k_unpack<double><<<grid, 128, 0, c->st>>>(c->u64, c->L64, c->in64, c->L64, nullptr, c->M, dst, g.nx, g.ny, z0);
+    else
+      k_unpack<float><<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->L64, fm, c->M, dst, g.nx, g.ny, z0);
+    CK(cudaGetLastError());
+    if (!dev) {
+      CK(cudaEventRecord(c->slab_ev[k], c->st));
+      CK(cudaStreamWaitEvent(c->st2, c->slab_ev[k], 0));
+      CK(cudaMemcpyAsync(field + z0 * plane, (char *)c->stage + z0 * plane * 8, (size_t)(z1 - z0) * plane * 8,
+                         cudaMemcpyDeviceToHost, c->st2));
+    }
+  }
+  if (!dev) {
+    CK(cudaEventRecord(c->slab_ev[pdfs_ctx::kSlabs], c->st2));
+    CK(cudaStreamWaitEvent(c->st, c->slab_ev[pdfs_ctx::kSlabs], 0));
+  }
   CK(cudaEventRecord(c->e1, c->st));
   CK(cudaStreamSynchronize(c->st));
   if (ms_d2h) *ms_d2h = ms_between(c->e0, c->e1);

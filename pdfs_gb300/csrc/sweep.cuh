@@ -266,6 +266,15 @@ struct CapBound {
   }
 };
 
+// A node's cap (the input, FP64) in the variant's representation.
+template <class T, int ARITH>
+__device__ __forceinline__ T cap_value(const T *p) {
+  if constexpr (sizeof(T) == 8 && ARITH == ARITH_PAIR)
+    return p_from_double(__ldg(p));
+  else
+    return __ldg(p);
+}
+
 // A node's change as a kernel accumulates it: relative for FP32, absolute
 // for FP64, absolute as the pair (|change|, 0) for FP32 pairs.
 template <class T, int ARITH>

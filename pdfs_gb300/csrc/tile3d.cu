@@ -7,15 +7,21 @@
 namespace pdfs {
 
 std::vector<int> brick_order(int ntx, int nty, int ntz) {
-  std::vector<int> o((size_t)ntx * nty * ntz);
-  for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
-  // a brick waits for one brick a level below in each axis: ordering by level
-  // lists all three first, which is all the deadlock argument needs
-  std::stable_sort(o.begin(), o.end(), [&](int a, int b) {
-    const int la = a % ntx + (a / ntx) % nty + a / (ntx * nty);
-    const int lb = b % ntx + (b / ntx) % nty + b / (ntx * nty);
-    return la < lb;
-  });
+  // a brick waits for one brick a level below in each axis: listing bricks by
+  // level (x + y + z), in index order within a level, lists all three first,
+  // which is all the deadlock argument needs.  A counting sort by level.
+  const size_t n = (size_t)ntx * nty * ntz;
+  const int levels = ntx + nty + ntz - 2;
+  std::vector<size_t> start((size_t)levels + 1, 0);
+  for (int z = 0; z < ntz; ++z)
+    for (int y = 0; y < nty; ++y)
+      for (int x = 0; x < ntx; ++x) ++start[x + y + z + 1];
+  for (int l = 0; l < levels; ++l) start[l + 1] += start[l];
+  std::vector<int> o(n);
+  int i = 0;
+  for (int z = 0; z < ntz; ++z)
+    for (int y = 0; y < nty; ++y)
+      for (int x = 0; x < ntx; ++x) o[start[x + y + z]++] = i++;
   return o;
 }
 

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
 #pragma unroll
               for (int q = 1; q < NZB; ++q)
                 if ((gz >> 3) == q) b = bnd[q];
-              nv = CB::below(g, b) ? g : vmin<T, ARITH>(__ldg(capg + gbase + (long long)gz * plane), g);
+              nv = CB::below(g, b) ? g : vmin<T, ARITH>(cap_value<T, ARITH>(capg + gbase + (long long)gz * plane), g);
             } else {
               nv = vmin<T, ARITH>(cv, g);
             }
