@@ -408,7 +408,7 @@ extern "C" int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o_in, int *til
   else
     for (int t = 1; t <= (o.precision == PDFS_PREC_FP32_POLISH64 ? 2 : 3); ++t) c64.push_back(t);
   if (o.arith == PDFS_ARITH_FAST) c64.push_back(4);
-  for (int t : {5, 6, 7, 8, 9}) c64.push_back(t);  // bricks and pencils: every arithmetic
+  for (int t : {5, 6, 7, 8}) c64.push_back(t);  // bricks and pencils: every arithmetic
   for (int t : c64) {
     double ms = 0;
     if (time_tile(PDFS_PREC_FP64, t, &ms) == PDFS_OK && ms < b) {

@@ -47,7 +47,7 @@ MaskLayout make_mask_layout(const pdfs_grid &g);
 struct TileShape {
   int tx, ty, c;
   int bz = 0;
-  int pencil = 0;  // pencils: compute nodes per thread and level (1 or 2); 0 = not a pencil tile
+  int pencil = 0;
 };
 // Tile ids (1-based) for FP32 and FP64 kernels.
 int tile_count32();
@@ -66,8 +66,8 @@ cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, 
                                 int sms, cudaStream_t st, int *grid_used);
 // One unmasked sweep by the pencil kernel (pencil.cu): 16 x 16 pencils, the
 // column order / progress words of a 16 x 16 layout.
-cudaError_t launch_sweep_pencils(int which, int arith, bool iso, int npt, const SweepArgs &a, const Layout &L,
-                                 int sms, cudaStream_t st, int *grid_used);
+cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
+                                 cudaStream_t st, int *grid_used);
 cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty);
 // Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
 std::vector<int> brick_order(int ntx, int nty, int ntz);

@@ -6,10 +6,10 @@
 
 namespace pdfs {
 
-template <class T, int MODE, int ARITH, bool ISO, int NPT>
+template <class T, int MODE, int ARITH, bool ISO>
 static cudaError_t launch_pc(const SweepArgs &a, const Layout &L, int sms, cudaStream_t st, int *grid_used) {
-  using G = PcGeo<T, NPT>;
-  auto kern = pc_sweep_kernel<T, MODE, ARITH, ISO, NPT>;
+  using G = PcGeo<T>;
+  auto kern = pc_sweep_kernel<T, MODE, ARITH, ISO>;
   CUtensorMap m[2];
   cudaError_t e = encode_field_map(&m[0], a.u, sizeof(T), L, a.nz + 2, G::W, G::RY, 1);
   if (e != cudaSuccess) return e;
@@ -33,46 +33,37 @@ static cudaError_t launch_pc(const SweepArgs &a, const Layout &L, int sms, cudaS
   return cudaGetLastError();
 }
 
-template <int NPT>
-static cudaError_t dispatch_pc(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
-                               cudaStream_t st, int *g) {
-  if (which == 0)
-    return iso ? launch_pc<float, MODE_MIN, ARITH_FAST, true, NPT>(a, L, sms, st, g)
-               : launch_pc<float, MODE_MIN, ARITH_FAST, false, NPT>(a, L, sms, st, g);
-  const bool rep = which == 2;
-  switch (arith) {
-    case ARITH_REF:
-      return rep ? launch_pc<double, MODE_REPLACE, ARITH_REF, false, NPT>(a, L, sms, st, g)
-                 : launch_pc<double, MODE_MIN, ARITH_REF, false, NPT>(a, L, sms, st, g);
-    case ARITH_FAST:
-      return rep ? launch_pc<double, MODE_REPLACE, ARITH_FAST, false, NPT>(a, L, sms, st, g)
-                 : launch_pc<double, MODE_MIN, ARITH_FAST, false, NPT>(a, L, sms, st, g);
-    case ARITH_MIXED:
-      if (iso)
-        return rep ? launch_pc<double, MODE_REPLACE, ARITH_MIXED, true, NPT>(a, L, sms, st, g)
-                   : launch_pc<double, MODE_MIN, ARITH_MIXED, true, NPT>(a, L, sms, st, g);
-      return rep ? launch_pc<double, MODE_REPLACE, ARITH_MIXED, false, NPT>(a, L, sms, st, g)
-                 : launch_pc<double, MODE_MIN, ARITH_MIXED, false, NPT>(a, L, sms, st, g);
-    case ARITH_PAIR:
-      if (iso)
-        return rep ? launch_pc<double, MODE_REPLACE, ARITH_PAIR, true, NPT>(a, L, sms, st, g)
-                   : launch_pc<double, MODE_MIN, ARITH_PAIR, true, NPT>(a, L, sms, st, g);
-      return rep ? launch_pc<double, MODE_REPLACE, ARITH_PAIR, false, NPT>(a, L, sms, st, g)
-                 : launch_pc<double, MODE_MIN, ARITH_PAIR, false, NPT>(a, L, sms, st, g);
-    default:
-      return cudaErrorInvalidValue;
-  }
-}
-
-// npt: nodes per compute thread and level (1: 256 compute threads, 2: 128)
-cudaError_t launch_sweep_pencils(int which, int arith, bool iso, int npt, const SweepArgs &a, const Layout &L,
-                                 int sms, cudaStream_t st, int *g) {
+cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
+                                 cudaStream_t st, int *g) {
   if (L.tx != 16 || L.ty != 16 || L.xo != 0 || a.blk_active || a.blk_chg || !a.pmail || a.prow < a.nz + 15 ||
       (which == 2 && (!a.bcap64 || !a.bcap32)))
     return cudaErrorInvalidValue;
-  if (npt == 1) return dispatch_pc<1>(which, arith, iso, a, L, sms, st, g);
-  if (npt == 2) return dispatch_pc<2>(which, arith, iso, a, L, sms, st, g);
-  return cudaErrorInvalidValue;
+  if (which == 0)
+    return iso ? launch_pc<float, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)
+               : launch_pc<float, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
+  const bool rep = which == 2;
+  switch (arith) {
+    case ARITH_REF:
+      return rep ? launch_pc<double, MODE_REPLACE, ARITH_REF, false>(a, L, sms, st, g)
+                 : launch_pc<double, MODE_MIN, ARITH_REF, false>(a, L, sms, st, g);
+    case ARITH_FAST:
+      return rep ? launch_pc<double, MODE_REPLACE, ARITH_FAST, false>(a, L, sms, st, g)
+                 : launch_pc<double, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
+    case ARITH_MIXED:
+      if (iso)
+        return rep ? launch_pc<double, MODE_REPLACE, ARITH_MIXED, true>(a, L, sms, st, g)
+                   : launch_pc<double, MODE_MIN, ARITH_MIXED, true>(a, L, sms, st, g);
+      return rep ? launch_pc<double, MODE_REPLACE, ARITH_MIXED, false>(a, L, sms, st, g)
+                 : launch_pc<double, MODE_MIN, ARITH_MIXED, false>(a, L, sms, st, g);
+    case ARITH_PAIR:
+      if (iso)
+        return rep ? launch_pc<double, MODE_REPLACE, ARITH_PAIR, true>(a, L, sms, st, g)
+                   : launch_pc<double, MODE_MIN, ARITH_PAIR, true>(a, L, sms, st, g);
+      return rep ? launch_pc<double, MODE_REPLACE, ARITH_PAIR, false>(a, L, sms, st, g)
+                 : launch_pc<double, MODE_MIN, ARITH_PAIR, false>(a, L, sms, st, g);
+    default:
+      return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace pdfs

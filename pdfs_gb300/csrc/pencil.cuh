@@ -9,8 +9,7 @@
 // downwind ones).  This kernel's order:
 //   * compute thread (lx, ly) -- pencil-local coordinates in sweep order --
 //     updates node (lx, ly, lz = G - lx - ly) at level G; a named barrier of
-//     the 256 compute threads separates levels.  (With NPT = 2, 128 threads
-//     each update the two nodes (lx, ly) and (lx, ly + 8) of a level.)  Every thread is busy on all
+//     the 256 compute threads separates levels.  Every thread is busy on all
 //     but SK = 30 of the nz + 30 levels, where a brick (tile3d.cuh) idles its
 //     threads for 30 of every BZ + 30;
 //   * planes stream through a ring of D shared-memory slots (TMA,
@@ -36,10 +35,9 @@
 
 namespace pdfs {
 
-template <class T, int NPT = 1>
+template <class T>
 struct PcGeo {
   static constexpr int BX = 16, BY = 16;
-  static_assert(NPT == 1 || NPT == 2, "one or two nodes per compute thread");
   // slot row: x0-1 .. x0+BX rounded up to 16 bytes (the field's index has no x
   // offset, so x0 - 1 = 16*cx starts the row on a 16-byte boundary)
   static constexpr int W = (int)((((BX + 2) * sizeof(T)) + 15) / 16 * 16 / sizeof(T));
@@ -52,7 +50,7 @@ struct PcGeo {
   static constexpr unsigned FIELD_BYTES = (unsigned)(W * RY * sizeof(T));
   static constexpr unsigned MASK_OFF = (FIELD_BYTES + 127u) & ~127u;  // the plane's 16 frozen words
   static constexpr unsigned SLOT_BYTES = MASK_OFF + 128u;
-  static constexpr int NC = BX * BY / NPT; // compute threads: NPT nodes of a level each
+  static constexpr int NC = BX * BY;       // compute threads
   static constexpr int NT = NC + 64;       // and the loader and face warps
   static constexpr int WV = (int)sizeof(T) / 4 > 1 ? 2 : 1;  // mailbox words per value (32 value bits each)
   static constexpr int C = 8;              // levels the face warp prepares per round, at most
@@ -61,8 +59,7 @@ struct PcGeo {
   static_assert(SLOT_BYTES % 128 == 0, "TMA destinations stay 128-byte aligned");
 };
 
-template <int NC>
-__device__ __forceinline__ void compute_bar() { asm volatile("bar.sync 1, %0;\n" ::"n"(NC) : "memory"); }
+__device__ __forceinline__ void compute_bar() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
 
 __device__ __forceinline__ void st_relaxed_gpu_u64(unsigned long long *p, unsigned long long v) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
@@ -119,14 +116,11 @@ __device__ __forceinline__ bool helper_idle(const SweepArgs &a, int col, volatil
   return false;
 }
 
-// No minimum-blocks bound: ptxas then keeps the pair polish at 64 registers,
-// and 7.0 ms per 768^3 sweep beats the 7.2 ms of the 96-register build that a
-// two-CTA bound allows.
-template <class T, int MODE, int ARITH, bool ISO, int NPT = 1>
-__global__ void __launch_bounds__(PcGeo<T, NPT>::NT)
-    pc_sweep_kernel(const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_mask,
-                    const __grid_constant__ SweepArgs a) {
-  using G = PcGeo<T, NPT>;
+template <class T, int MODE, int ARITH, bool ISO>
+__global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
+                                                               const __grid_constant__ CUtensorMap tm_mask,
+                                                               const __grid_constant__ SweepArgs a) {
+  using G = PcGeo<T>;
   constexpr int BX = G::BX, BY = G::BY, W = G::W, SK = G::SK, D = G::D;
   constexpr int SE = (int)(G::SLOT_BYTES / sizeof(T));  // slot stride in elements
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -278,12 +272,16 @@ __global__ void __launch_bounds__(PcGeo<T, NPT>::NT)
       }
     } else {
       // ------------------------------------ compute threads ------------------------------------
-      // thread (lx, lb) updates the nodes (lx, lb + j BY / NPT), j < NPT, of every level (sweep order)
-      constexpr int RB = BY / NPT;
-      const int lx = tid & (BX - 1), lb = tid / BX;
-      const int gx = sxd > 0 ? lx : BX - 1 - lx;
-      const int mshift = 16 * (cx & 1) + gx;
+      const int lx = tid & (BX - 1), ly = tid / BX, lxy = lx + ly;  // sweep order
+      const int gx = sxd > 0 ? lx : BX - 1 - lx, gy = syd > 0 ? ly : BY - 1 - ly;
+      const bool vxy = (x0 + gx <= nx) && (y0 + gy <= ny);
+      const int orow = (1 + gy) * W + 1 + gx;  // my node within a slot
+      const int mbyte = (int)G::MASK_OFF + 4 * gy, mshift = 16 * (cx & 1) + gx;
+      const long long grow = (long long)(y0 + gy) * px + (x0 + gx);
+      // downwind faces: my node's final value goes to a mailbox when a pencil is downwind
       const bool poisoned = col == a.poison_col;
+      const bool mx = lx == BX - 1 && lcx < a.ncx - 1 && !poisoned;
+      const bool my = ly == BY - 1 && lcy < a.ncy - 1 && !poisoned;
       unsigned long long *xmail = a.pmail + ((size_t)col * 2 + 0) * a.prow * 16 * G::WV;
       unsigned long long *ymail = a.pmail + ((size_t)col * 2 + 1) * a.prow * 16 * G::WV;
       const float hmin = a.hmin;
@@ -292,40 +290,23 @@ __global__ void __launch_bounds__(PcGeo<T, NPT>::NT)
       T *__restrict__ u = reinterpret_cast<T *>(a.u);
       const T *__restrict__ capg = reinterpret_cast<const T *>(a.cap);
       auto gz_of = [&](int lz) { return szd > 0 ? lz + 1 : nz - lz; };
+      // replace-update: the cap bound of my node's 8^3 block, and of the next
+      // block in sweep order (loaded one block ahead)
       using CB = CapBound<T, ARITH>;
+      typename CB::type bcur = 0, bnxt = 0;
+      int bzc = 0;
+      const long long bxy = (long long)((y0 - 1 + gy) >> 3) * a.nbx + ((x0 - 1 + gx) >> 3);
       const int dbz = szd > 0 ? 1 : -1;
-      auto bnd_at = [&](int bz, long long bxy) -> typename CB::type {
+      auto bnd_at = [&](int bz) -> typename CB::type {
         return (bz >= 0 && bz < a.nbz) ? CB::load(a, (long long)bz * a.nby * a.nbx + bxy) : typename CB::type(0);
       };
-      int ly[NPT], lxy[NPT], orow[NPT], mbyte[NPT], sl[NPT], bzc[NPT];
-      bool vxy[NPT], mx[NPT], my[NPT];
-      long long grow[NPT], bxy[NPT];
-      // replace-update: the cap bound of each node's 8^3 block, and of the
-      // next block in sweep order (loaded one block ahead)
-      typename CB::type bcur[NPT], bnxt[NPT];
-#pragma unroll
-      for (int j = 0; j < NPT; ++j) {
-        ly[j] = lb + j * RB;
-        lxy[j] = lx + ly[j];
-        const int gy = syd > 0 ? ly[j] : BY - 1 - ly[j];
-        vxy[j] = (x0 + gx <= nx) && (y0 + gy <= ny);
-        orow[j] = (1 + gy) * W + 1 + gx;  // the node within a slot
-        mbyte[j] = (int)G::MASK_OFF + 4 * gy;
-        grow[j] = (long long)(y0 + gy) * px + (x0 + gx);
-        // downwind faces: the node's final value goes to a mailbox when a pencil is downwind
-        mx[j] = lx == BX - 1 && lcx < a.ncx - 1 && !poisoned;
-        my[j] = ly[j] == BY - 1 && lcy < a.ncy - 1 && !poisoned;
-        bxy[j] = (long long)((y0 - 1 + gy) >> 3) * a.nbx + ((x0 - 1 + gx) >> 3);
-        bzc[j] = 0;
-        bcur[j] = bnxt[j] = 0;
-        if (MODE == MODE_REPLACE && vxy[j]) {
-          bzc[j] = (gz_of(0) - 1) >> 3;
-          bcur[j] = bnd_at(bzc[j], bxy[j]);
-          bnxt[j] = bnd_at(bzc[j] + dbz, bxy[j]);
-        }
-        sl[j] = (1 - lxy[j]) % D;  // slot of the node's plane (lz + 1) at level 0
-        if (sl[j] < 0) sl[j] += D;
+      if (MODE == MODE_REPLACE && vxy) {
+        bzc = (gz_of(0) - 1) >> 3;
+        bcur = bnd_at(bzc);
+        bnxt = bnd_at(bzc + dbz);
       }
+      int sl = (1 - lxy) % D;  // slot of my node's plane (lz + 1) at level 0
+      if (sl < 0) sl += D;
       int ready = 0;  // thread 0: levels below it are prepared (re-read only when reached)
       bool stop = false;
       for (int g = 0; g < t_end; ++g) {
@@ -346,72 +327,63 @@ __global__ void __launch_bounds__(PcGeo<T, NPT>::NT)
           }
         }
         if (tid == 0 && stop) s_stop = 1;
-        compute_bar<G::NC>();
+        compute_bar();
         if (s_stop) {
           stop = true;
           break;
         }
         // levels below g are complete (FP32: published every other level; its ring looks further ahead)
         if (tid == 0 && (g & G::PUB) == 0) st_release_cta_s(&s_done, g);
-        // The nodes of one level neither read nor write one another, so every
-        // node's update is evaluated first (in-bounds slot reads, whatever the
-        // node's range) and committed after.
-        T cv[NPT], gv[NPT];
-#pragma unroll
-        for (int j = 0; j < NPT; ++j) {
-          const int sp = sl[j] == 0 ? D - 1 : sl[j] - 1, sn = sl[j] == D - 1 ? 0 : sl[j] + 1;
-          const T *cur = ring + sl[j] * SE, *prv = ring + sp * SE, *nxt = ring + sn * SE;
-          const int o = orow[j];
-          cv[j] = cur[o];
-          const T m0 = vmin<T, ARITH>(cur[o - 1], cur[o + 1]);
-          const T m1 = vmin<T, ARITH>(cur[o - W], cur[o + W]);
-          // grid orientation: min(u[z-1], u[z+1]); the sweep's previous plane is z-1 when sz > 0
-          const T m2 = szd > 0 ? vmin<T, ARITH>(prv[o], nxt[o]) : vmin<T, ARITH>(nxt[o], prv[o]);
-          gv[j] = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
-        }
-#pragma unroll
-        for (int j = 0; j < NPT; ++j) {
-          const int lz = g - lxy[j];
-          if ((unsigned)lz < (unsigned)nz && vxy[j]) {
+        const int lz = g - lxy;
+        if ((unsigned)lz < (unsigned)nz) {
+          if (vxy) {
+            const int sp = sl == 0 ? D - 1 : sl - 1, sn = sl == D - 1 ? 0 : sl + 1;
+            T *cur = ring + sl * SE;
+            const T *prv = ring + sp * SE, *nxt = ring + sn * SE;
+            const T cv = cur[orow];
+            const T m0 = vmin<T, ARITH>(cur[orow - 1], cur[orow + 1]);
+            const T m1 = vmin<T, ARITH>(cur[orow - W], cur[orow + W]);
+            // grid orientation: min(u[z-1], u[z+1]); the sweep's previous plane is z-1 when sz > 0
+            const T m2 = szd > 0 ? vmin<T, ARITH>(prv[orow], nxt[orow]) : vmin<T, ARITH>(nxt[orow], prv[orow]);
             bool act = true;
             if (masked) {
-              const uint32_t w = *reinterpret_cast<const uint32_t *>(sm + (size_t)sl[j] * G::SLOT_BYTES + mbyte[j]);
+              const uint32_t w = *reinterpret_cast<const uint32_t *>(sm + (size_t)sl * G::SLOT_BYTES + mbyte);
               act = !((w >> mshift) & 1u);
             }
             if constexpr (MODE == MODE_REPLACE) {
-              // a node's planes are consecutive in sweep order: the block moves one step at a time
+              // my nodes are consecutive in sweep order: the block moves one step at a time
               const int bz = (gz_of(lz) - 1) >> 3;
-              if (bz != bzc[j]) {
-                bzc[j] = bz;
-                bcur[j] = bnxt[j];
-                bnxt[j] = bnd_at(bz + dbz, bxy[j]);
+              if (bz != bzc) {
+                bzc = bz;
+                bcur = bnxt;
+                bnxt = bnd_at(bz + dbz);
               }
             }
-            T fin = cv[j];  // the node's value at the end of the sweep
+            T fin = cv;  // the node's value at the end of the sweep
             if (act) {
+              const T gv = local_update<T, MODE, ARITH, ISO>(m0, m1, m2, k64, k32);
               T nv;
               if constexpr (MODE == MODE_REPLACE) {
-                nv = CB::below(gv[j], bcur[j])
-                         ? gv[j]
-                         : vmin<T, ARITH>(cap_value<T, ARITH>(capg + (long long)gz_of(lz) * plane + grow[j]), gv[j]);
+                nv = CB::below(gv, bcur) ? gv
+                                         : vmin<T, ARITH>(cap_value<T, ARITH>(capg + (long long)gz_of(lz) * plane + grow), gv);
               } else {
-                nv = vmin<T, ARITH>(cv[j], gv[j]);
+                nv = vmin<T, ARITH>(cv, gv);
               }
-              if (vdiffers<T, ARITH>(nv, cv[j])) {
+              if (vdiffers<T, ARITH>(nv, cv)) {
                 fin = nv;
-                ring[sl[j] * SE + orow[j]] = nv;
-                u[(long long)gz_of(lz) * plane + grow[j]] = nv;
-                tmax = vmax_nonneg<T, ARITH>(tmax, node_change<T, ARITH>(cv[j], nv, hmin));
+                cur[orow] = nv;
+                u[(long long)gz_of(lz) * plane + grow] = nv;
+                tmax = vmax_nonneg<T, ARITH>(tmax, node_change<T, ARITH>(cv, nv, hmin));
                 fence_proxy_async();  // this store comes before a later TMA write into the slot
               }
             }
-            if (mx[j]) mail_put<T>(xmail + ((size_t)(lz + ly[j]) * 16 + ly[j]) * G::WV, fin, epoch);
-            if (my[j]) mail_put<T>(ymail + ((size_t)(lz + lx) * 16 + lx) * G::WV, fin, epoch);
+            if (mx) mail_put<T>(xmail + ((size_t)(lz + ly) * 16 + ly) * G::WV, fin, epoch);
+            if (my) mail_put<T>(ymail + ((size_t)(lz + lx) * 16 + lx) * G::WV, fin, epoch);
           }
-          sl[j] = sl[j] == D - 1 ? 0 : sl[j] + 1;
         }
+        sl = sl == D - 1 ? 0 : sl + 1;
       }
-      compute_bar<G::NC>();
+      compute_bar();
       if (tid == 0 && !stop) st_release_cta_s(&s_done, t_end);
     }
     __syncthreads();

@@ -772,7 +772,7 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   CK(cudaEventRecord(c->k0, c->st));
   if (pencil) {
     a.epoch = ++c->epoch;  // mailbox words of every earlier sweep carry a smaller tag
-    CK(launch_sweep_pencils(which, arith, iso, ts.pencil, a, L, c->sms, c->st, &grid));
+    CK(launch_sweep_pencils(which, arith, iso, a, L, c->sms, c->st, &grid));
   } else if (ts.bz > 0) {
     a.epoch = ++c->epoch;  // the flags of every earlier sweep are below it
     CK(launch_sweep_bricks(which, ts.ty, ts.bz, arith, iso, a, L, c->sms, c->st, &grid));

@@ -16,11 +16,10 @@ namespace pdfs {
 // sweeps run on 16 x 16 x BZ bricks.
 static const TileShape kT32[] = {{32, 8, 2},  {32, 8, 4},  {32, 16, 4},     {32, 8, 1},      {32, 4, 2},
                                  {32, 6, 1},  {32, 10, 1}, {16, 16, 0, 16}, {16, 16, 0, 32}, {16, 16, 0, 32, 1},
-                                 {16, 8, 0, 48},  {16, 16, 0, 32, 2}};
+                                 {16, 8, 0, 48}};
 // tile 4 (32 x 6, one row per warp) exists for the fast and mixed arithmetic
 static const TileShape kT64[] = {{32, 4, 1},      {32, 4, 2},         {32, 8, 2},     {32, 6, 1},
-                                 {16, 16, 0, 16}, {16, 16, 0, 16, 1}, {16, 16, 0, 32}, {16, 8, 0, 32},
-                                 {16, 16, 0, 16, 2}};
+                                 {16, 16, 0, 16}, {16, 16, 0, 16, 1}, {16, 16, 0, 32}, {16, 8, 0, 32}};
 
 int tile_count32() { return (int)(sizeof(kT32) / sizeof(kT32[0])); }
 int tile_count64() { return (int)(sizeof(kT64) / sizeof(kT64[0])); }

@@ -67,7 +67,7 @@ def test_autotune_returns_valid_tiles():
     t = api.autotune(96, 80, 64, (1.0, 1.0, 1.0), precision=L.PREC_FP32_POLISH64)
     # FP32: columns 1-7, bricks 8, 9, 11, pencils 10; FP64 polish, reference
     # arithmetic: columns 1-2, bricks 5, 7, 8, pencils 6
-    assert 1 <= (t & 0xFF) <= 12 and (t >> 8) in (1, 2, 5, 6, 7, 8, 9)
+    assert 1 <= (t & 0xFF) <= 11 and (t >> 8) in (1, 2, 5, 6, 7, 8)
     w = W.random_spheres(96, 80, 64, 1.0, 1.0, 1.0, 5, 3.0, 10.0, seed=2)
     a = w.field.copy()
     api.solve(a, (1.0, 1.0, 1.0), frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
