@@ -523,9 +523,6 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((e = cudaEventCreate(&c->k1)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->q0)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->q1)) != cudaSuccess) return fail(e);
-  if ((e = cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
-  for (cudaEvent_t &ev : c->slab_ev)
-    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) return fail(e);
   if (verbose(o)) {
     const auto t_end = std::chrono::steady_clock::now();
@@ -581,10 +578,21 @@ static int ensure_stage(pdfs_ctx *c) {
   return PDFS_OK;
 }
 
-// Planes per slab of the load / store pipelines: at most kSlabs slabs.
+// Planes per slab of the load / store pipelines: at most kSlabs slabs, and
+// one slab (no pipeline) for fields under 256 MB, where the layout kernels
+// that a pipeline would hide take a few tens of microseconds.
 static int slab_planes(const pdfs_grid &g) {
   const int planes = g.nz + 2;
+  if (ref_nodes(g) * 8 < (256u << 20)) return planes;
   return std::max(16, (planes + pdfs_ctx::kSlabs - 1) / pdfs_ctx::kSlabs);
+}
+
+// The pipeline's second stream and slab events, made on first use.
+static int ensure_pipeline(pdfs_ctx *c) {
+  if (c->st2) return PDFS_OK;
+  CK(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
+  for (cudaEvent_t &ev : c->slab_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  return PDFS_OK;
 }
 
 static double ms_between(cudaEvent_t a, cudaEvent_t b) {
@@ -611,24 +619,31 @@ static int load_impl(pdfs_ctx *c, const double *field, const uint8_t *frozen, do
   if (!dev_field || (use_mask && !dev_mask)) {
     if ((s = ensure_stage(c))) return s;
   }
+  const double *src = dev_field ? field : (const double *)c->stage;
+  const int planes = g.nz + 2, per = dev_field ? planes : slab_planes(g);
+  const bool pipe = per < planes;  // else every step runs on c->st
+  if (pipe && (s = ensure_pipeline(c))) return s;
+  cudaStream_t ks = pipe ? c->st2 : c->st;  // the layout kernels' stream
+  auto handoff = [&](cudaEvent_t ev) -> cudaError_t {  // ks waits for the copies issued so far
+    if (!pipe) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(ev, c->st);
+    return e != cudaSuccess ? e : cudaStreamWaitEvent(ks, ev, 0);
+  };
   const auto t_stage = std::chrono::steady_clock::now();
   CK(cudaEventRecord(c->e0, c->st));
-  CK(cudaStreamWaitEvent(c->st2, c->e0, 0));
-  CK(cudaMemsetAsync(c->fmask, 0, c->M.words * 4, c->st2));
+  if (pipe) CK(cudaStreamWaitEvent(ks, c->e0, 0));
+  CK(cudaMemsetAsync(c->fmask, 0, c->M.words * 4, ks));
   if (use_mask) {
     const uint8_t *m = frozen;
     if (!dev_mask) {
       m = (const uint8_t *)c->stage + n * 8;
       CK(cudaMemcpyAsync((void *)m, frozen, n, cudaMemcpyHostToDevice, c->st));
-      CK(cudaEventRecord(c->slab_ev[pdfs_ctx::kSlabs], c->st));
-      CK(cudaStreamWaitEvent(c->st2, c->slab_ev[pdfs_ctx::kSlabs], 0));
+      CK(handoff(c->slab_ev[pdfs_ctx::kSlabs]));
     }
     dim3 mg(g.ny, g.nz);
-    k_pack_mask<<<mg, 64, 0, c->st2>>>(m, c->fmask, c->M, g.nx, g.ny);
+    k_pack_mask<<<mg, 64, 0, ks>>>(m, c->fmask, c->M, g.nx, g.ny);
     CK(cudaGetLastError());
   }
-  const double *src = dev_field ? field : (const double *)c->stage;
-  const int planes = g.nz + 2, per = dev_field ? planes : slab_planes(g);
   const long long blocks_per_z = (long long)c->nbx * c->nby;
   int bz_done = 0;
   for (int z0 = 0, k = 0; z0 < planes; z0 += per, ++k) {
@@ -636,17 +651,16 @@ static int load_impl(pdfs_ctx *c, const double *field, const uint8_t *frozen, do
     if (!dev_field) {
       CK(cudaMemcpyAsync((char *)c->stage + z0 * plane * 8, field + z0 * plane, (size_t)(z1 - z0) * plane * 8,
                          cudaMemcpyHostToDevice, c->st));
-      CK(cudaEventRecord(c->slab_ev[k], c->st));
-      CK(cudaStreamWaitEvent(c->st2, c->slab_ev[k], 0));
+      CK(handoff(c->slab_ev[k]));
     }
     dim3 grid(g.ny + 2, z1 - z0);
-    k_pack<double><<<grid, 128, 0, c->st2>>>(src, c->in64, g.nx, g.ny, c->L64, z0);
+    k_pack<double><<<grid, 128, 0, ks>>>(src, c->in64, g.nx, g.ny, c->L64, z0);
     CK(cudaGetLastError());
     if (c->bcap64) {
       // block bz holds planes 8 bz + 1 .. min(8 bz + 8, nz): complete once plane z1 - 1 is packed
       const int bz_ready = z1 >= g.nz + 1 ? c->nbz : std::min(c->nbz, (z1 - 1) / 8);
       if (bz_ready > bz_done) {
-        k_block_capmin<<<8 * c->sms, 256, 0, c->st2>>>(c->in64, c->L64, use_mask ? c->fmask : nullptr, c->M, g.nx,
+        k_block_capmin<<<8 * c->sms, 256, 0, ks>>>(c->in64, c->L64, use_mask ? c->fmask : nullptr, c->M, g.nx,
                                                         g.ny, g.nz, c->nbx, c->nby, bz_done * blocks_per_z,
                                                         bz_ready * blocks_per_z, c->bcap64, c->bcap32);
         CK(cudaGetLastError());
@@ -654,8 +668,8 @@ static int load_impl(pdfs_ctx *c, const double *field, const uint8_t *frozen, do
       }
     }
   }
-  CK(cudaEventRecord(c->e1, c->st2));
-  CK(cudaStreamWaitEvent(c->st, c->e1, 0));
+  CK(cudaEventRecord(c->e1, ks));
+  if (pipe) CK(cudaStreamWaitEvent(c->st, c->e1, 0));
   CK(cudaStreamSynchronize(c->st));
   if (ms_h2d) *ms_h2d = ms_between(c->e0, c->e1);
   if (verbose(c->o))
@@ -980,9 +994,12 @@ static int store_impl(pdfs_ctx *c, double *field, double *ms_d2h) {
     if ((s = ensure_stage(c))) return s;
     dst = (double *)c->stage;
   }
+  const int planes = g.nz + 2, per = dev ? planes : slab_planes(g);
+  const bool pipe = per < planes;  // else the copy runs on c->st
+  if (pipe && (s = ensure_pipeline(c))) return s;
+  cudaStream_t cs = pipe ? c->st2 : c->st;  // the copies' stream
   CK(cudaEventRecord(c->e0, c->st));
   const uint32_t *fm = c->has_mask ? c->fmask : nullptr;
-  const int planes = g.nz + 2, per = dev ? planes : slab_planes(g);
   for (int z0 = 0, k = 0; z0 < planes; z0 += per, ++k) {
     const int z1 = std::min(planes, z0 + per);
     dim3 grid(g.ny + 2, z1 - z0);
@@ -994,14 +1011,16 @@ static int store_impl(pdfs_ctx *c, double *field, double *ms_d2h) {
       k_unpack<float><<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->L64, fm, c->M, dst, g.nx, g.ny, z0);
     CK(cudaGetLastError());
     if (!dev) {
-      CK(cudaEventRecord(c->slab_ev[k], c->st));
-      CK(cudaStreamWaitEvent(c->st2, c->slab_ev[k], 0));
+      if (pipe) {
+        CK(cudaEventRecord(c->slab_ev[k], c->st));
+        CK(cudaStreamWaitEvent(cs, c->slab_ev[k], 0));
+      }
       CK(cudaMemcpyAsync(field + z0 * plane, (char *)c->stage + z0 * plane * 8, (size_t)(z1 - z0) * plane * 8,
-                         cudaMemcpyDeviceToHost, c->st2));
+                         cudaMemcpyDeviceToHost, cs));
     }
   }
-  if (!dev) {
-    CK(cudaEventRecord(c->slab_ev[pdfs_ctx::kSlabs], c->st2));
+  if (pipe) {
+    CK(cudaEventRecord(c->slab_ev[pdfs_ctx::kSlabs], cs));
     CK(cudaStreamWaitEvent(c->st, c->slab_ev[pdfs_ctx::kSlabs], 0));
   }
   CK(cudaEventRecord(c->e1, c->st));
