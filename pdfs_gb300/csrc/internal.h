@@ -137,6 +137,8 @@ struct pdfs_ctx {
   float *bcap32 = nullptr;  // the same rounded down to float
   float *u32 = nullptr;     // FP32 working field
   uint32_t *fmask = nullptr;
+  void *arena = nullptr;    // every device buffer below but the stage, as one allocation
+  size_t arena_bytes = 0;
   void *stage = nullptr;    // reference-layout staging buffer for host transfers
   size_t stage_bytes = 0;
   int *order32 = nullptr, *order64 = nullptr, *progress = nullptr, *ticket = nullptr;

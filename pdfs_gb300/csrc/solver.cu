@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstddef>
 #include <cstring>
+#include <mutex>
 #include <utility>
 #include <vector>
 
@@ -293,38 +294,110 @@ extern "C" const char *pdfs_status_string(int s) {
 
 extern "C" const char *pdfs_version(void) { return "pdfs-gb300 0.1 (sm_103a)"; }
 
-// Context buffers come from the device's stream-ordered memory pool, which
-// keeps up to a quarter of the device's memory for the next context: a
-// repeated solve does not pay the allocation of its multi-GB buffers again.
-// An allocation that finds the device full trims the pool and retries.
-static void keep_pool(int dev) {
-  static bool done[64] = {false};
-  if (dev < 0 || dev >= 64 || done[dev]) return;
-  done[dev] = true;
-  cudaMemPool_t pool;
-  size_t fr = 0, tot = 0;
-  if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess || cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
-    cudaGetLastError();
-    return;
+// Context blocks (the arena of a context's buffers, the transfer stage) are
+// kept in a per-process cache when a context is destroyed, up to a quarter of
+// the device's memory, and handed to the next context that needs a block of
+// about that size: a repeated solve pays neither cudaMalloc nor cudaFree (which
+// synchronises the device; 10 ms for the 15 GB of a 768^3 solve) again.  Every
+// block is idle when cached: destroy and the stage's reallocation synchronise
+// the context's streams first.  An allocation that finds the device full
+// empties the cache and retries.
+namespace {
+struct CachedBlock {
+  int dev;
+  void *p;
+  size_t bytes;
+};
+struct BlockCache {
+  std::mutex m;
+  std::vector<CachedBlock> blocks;
+  size_t held[64] = {};
+};
+BlockCache &block_cache() {
+  static BlockCache *bc = new BlockCache();  // never destroyed: the driver frees device memory at exit
+  return *bc;
+}
+size_t cache_cap(int dev) {
+  static size_t cap[64] = {};
+  if (dev < 0 || dev >= 64) return 0;
+  if (!cap[dev]) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    cap[dev] = tot / 4;
   }
-  cuuint64_t thr = (cuuint64_t)tot / 4;
-  cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-  cudaGetLastError();
+  return cap[dev];
 }
+void cache_release(int dev) {
+  std::vector<void *> drop;
+  {
+    BlockCache &bc = block_cache();
+    std::lock_guard<std::mutex> lk(bc.m);
+    for (size_t i = 0; i < bc.blocks.size();) {
+      if (bc.blocks[i].dev == dev) {
+        drop.push_back(bc.blocks[i].p);
+        bc.held[dev] -= bc.blocks[i].bytes;
+        bc.blocks[i] = bc.blocks.back();
+        bc.blocks.pop_back();
+      } else {
+        ++i;
+      }
+    }
+  }
+  for (void *p : drop) cudaFree(p);
+}
+}  // namespace
+
+// A block of at least `bytes` (a cached one of at most 1/8 more, else new).
 template <class P>
-static cudaError_t ctx_malloc(pdfs_ctx *c, P **p, size_t bytes) {
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(p), bytes, c->st);
-  if (e != cudaErrorMemoryAllocation) return e;
-  // out of memory: hand what the pool keeps back to the device and try once more
-  cudaGetLastError();
-  cudaMemPool_t pool;
-  if (cudaStreamSynchronize(c->st) != cudaSuccess || cudaDeviceGetDefaultMemPool(&pool, c->dev) != cudaSuccess)
-    return e;
-  cudaMemPoolTrimTo(pool, 0);
-  return cudaMallocAsync(reinterpret_cast<void **>(p), bytes, c->st);
+static cudaError_t ctx_malloc(pdfs_ctx *c, P **out, size_t bytes) {
+  const int dev = c->dev;
+  if (dev >= 0 && dev < 64) {
+    BlockCache &bc = block_cache();
+    std::lock_guard<std::mutex> lk(bc.m);
+    int best = -1;
+    for (size_t i = 0; i < bc.blocks.size(); ++i) {
+      const CachedBlock &b = bc.blocks[i];
+      if (b.dev == dev && b.bytes >= bytes && b.bytes - bytes <= bytes / 8 &&
+          (best < 0 || b.bytes < bc.blocks[best].bytes))
+        best = (int)i;
+    }
+    if (best >= 0) {
+      *out = reinterpret_cast<P *>(bc.blocks[best].p);
+      bc.held[dev] -= bc.blocks[best].bytes;
+      bc.blocks[best] = bc.blocks.back();
+      bc.blocks.pop_back();
+      return cudaSuccess;
+    }
+  }
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e == cudaErrorMemoryAllocation) {  // give the cached blocks back and try once more
+    cudaGetLastError();
+    cache_release(dev);
+    e = cudaMalloc(&p, bytes);
+  }
+  *out = reinterpret_cast<P *>(p);
+  return e;
 }
-static void ctx_free(pdfs_ctx *c, void *p) {
-  if (p) cudaFreeAsync(p, c->st);
+// Returns an idle block of `bytes` to the cache (or to the device when the
+// cache is full).
+static void ctx_free(pdfs_ctx *c, void *p, size_t bytes) {
+  if (!p) return;
+  const int dev = c->dev;
+  if (dev >= 0 && dev < 64) {
+    const size_t cap = cache_cap(dev);
+    BlockCache &bc = block_cache();
+    std::lock_guard<std::mutex> lk(bc.m);
+    if (bc.held[dev] + bytes <= cap) {
+      bc.blocks.push_back({dev, p, bytes});
+      bc.held[dev] += bytes;
+      return;
+    }
+  }
+  cudaFree(p);
 }
 
 static int validate(const pdfs_grid *g, const pdfs_opts *o) {
@@ -412,23 +485,44 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   cudaError_t e;
   if ((e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->dev)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
-  keep_pool(c->dev);
   mark("stream");
-  const bool need32 = o.precision != PDFS_PREC_FP64;
-  const bool need64 = o.precision != PDFS_PREC_FP32 || true;  // FP64 input always resident
-  if (need64 && (e = ctx_malloc(c, &c->in64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
-  if ((o.precision != PDFS_PREC_FP32) && (e = ctx_malloc(c, &c->u64, c->L64.elems * 8)) != cudaSuccess) return fail(e);
-  // polish: the per-block cap bounds
-  if (o.precision == PDFS_PREC_FP32_POLISH64) {
-    const size_t nb = (size_t)((g->nx + 7) / 8) * ((g->ny + 7) / 8) * ((g->nz + 7) / 8);
-    if ((e = ctx_malloc(c, &c->bcap64, nb * 8)) != cudaSuccess) return fail(e);
-    if ((e = ctx_malloc(c, &c->bcap32, nb * 4)) != cudaSuccess) return fail(e);
+  // Host tables first, then every device buffer of the context carved from
+  // one pool allocation (a batch creates hundreds of contexts, and a pool
+  // allocation's cost grows with the number of blocks the pool holds).
+  c->nbx = (g->nx + 7) / 8;
+  c->nby = (g->ny + 7) / 8;
+  c->nbz = (g->nz + 7) / 8;
+  c->nblocks = (long long)c->nbx * c->nby * c->nbz;
+  std::vector<uint16_t> wb;
+  if (o.scheduler == PDFS_SCHED_LEARNED) {
+    const float *blob = o.mlp_weights ? o.mlp_weights : default_mlp_blob();
+    wb.resize(PDFS_MLP_PARAMS);
+    for (int i = 0; i < PDFS_MLP_PARAMS; ++i) {  // bf16 values: the upper half of the float
+      uint32_t u;
+      std::memcpy(&u, &blob[i], 4);
+      wb[i] = (uint16_t)(u >> 16);
+    }
+    c->mlp_thr = blob[PDFS_MLP_PARAMS];
   }
-  if (need32 && (e = ctx_malloc(c, &c->u32, c->L32.elems * 4)) != cudaSuccess) return fail(e);
-  if ((e = ctx_malloc(c, &c->fmask, c->M.words * 4)) != cudaSuccess) return fail(e);
-  mark("fields");
+  // brick tiles: ticket orders and the completion flags (epoch 0 = never)
+  std::vector<int> bo[2];
+  size_t nflags = 0;
+  for (int k = 0; k < 2; ++k) {
+    const TileShape ts = k ? s64 : s32;
+    if (ts.bz == 0) continue;
+    int *nt = k ? c->nt64 : c->nt32;
+    nt[0] = (g->nx + ts.tx - 1) / ts.tx;
+    nt[1] = (g->ny + ts.ty - 1) / ts.ty;
+    nt[2] = (g->nz + ts.bz - 1) / ts.bz;
+    bo[k] = brick_order(nt[0], nt[1], nt[2]);
+    nflags = std::max(nflags, bo[k].size());
+  }
+  mark("brick orders");
+  const std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
+                         w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
+  mark("columns");
+  // per-row progress words and face mailboxes, sized for the larger of the two layouts
   {
-    // per-row progress words and face mailboxes, sized for the larger of the two layouts
     const int nb = mailbox_chunks(g->nz) * kMailboxChunk;
     size_t prog = 0, mb = 0;
     for (int k = 0; k < 2; ++k) {
@@ -438,79 +532,72 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
       mb = std::max(mb, ncol * (size_t)nb * (size_t)(L.tx + L.ty) * (size_t)L.esize);
     }
     c->progress_ints = prog;
-    if ((e = ctx_malloc(c, &c->progress, prog * 4)) != cudaSuccess) return fail(e);
-    if ((e = ctx_malloc(c, &c->mailbox, mb)) != cudaSuccess) return fail(e);
     c->mailbox_bytes = mb;
   }
-  mark("mailboxes");
-  if ((e = ctx_malloc(c, &c->ticket, 16)) != cudaSuccess) return fail(e);
-  if ((e = ctx_malloc(c, &c->dstat, sizeof(DevStatus))) != cudaSuccess) return fail(e);
+  // pencils: two faces of prow diagonals x 16 entries x 2 words per pencil
+  // (tag 0 never matches: epochs start at 1)
+  size_t pmail_words = 0;
+  if (s32.pencil || s64.pencil) {
+    c->prow = g->nz + 15;
+    pmail_words = (size_t)((g->nx + 15) / 16) * ((g->ny + 15) / 16) * 2 * (size_t)c->prow * 16 * 2;
+  }
+  std::vector<std::pair<void **, size_t>> plan;
+  auto want = [&](auto **p, size_t bytes) {
+    if (bytes) plan.emplace_back(reinterpret_cast<void **>(p), bytes);
+  };
+  const bool need32 = o.precision != PDFS_PREC_FP64;
+  want(&c->in64, c->L64.elems * 8);  // the FP64 input is always resident
+  if (o.precision != PDFS_PREC_FP32) want(&c->u64, c->L64.elems * 8);
+  if (o.precision == PDFS_PREC_FP32_POLISH64) {  // polish: the per-block cap bounds
+    want(&c->bcap64, (size_t)c->nblocks * 8);
+    want(&c->bcap32, (size_t)c->nblocks * 4);
+  }
+  if (need32) want(&c->u32, c->L32.elems * 4);
+  want(&c->fmask, c->M.words * 4);
+  want(&c->progress, c->progress_ints * 4);
+  want(&c->mailbox, c->mailbox_bytes);
+  want(&c->ticket, 16);
+  want(&c->dstat, sizeof(DevStatus));
+  want(&c->bchg, (size_t)c->nblocks * kRing * 4);
+  want(&c->bact, (size_t)c->nblocks);
+  if (!wb.empty()) {
+    want(&c->mlp_w, PDFS_MLP_PARAMS * 2);
+    want(&c->bmin, (size_t)c->nblocks * 4);
+  }
+  want(&c->tord32, bo[0].size() * 4);
+  want(&c->tord64, bo[1].size() * 4);
+  want(&c->tflag, nflags * 4);
+  want(&c->pmail, pmail_words * 8);
+  want(&c->order32, w32.size() * 4);
+  want(&c->order64, w64.size() * 4);
+  {
+    size_t total = 0;
+    for (auto &r : plan) total += (r.second + 255) & ~(size_t)255;  // 256-byte aligned pieces
+    if ((e = ctx_malloc(c, &c->arena, total)) != cudaSuccess) return fail(e);
+    c->arena_bytes = total;
+    char *p = reinterpret_cast<char *>(c->arena);
+    for (auto &r : plan) {
+      *r.first = p;
+      p += (r.second + 255) & ~(size_t)255;
+    }
+  }
+  mark("allocation");
   if ((e = cudaHostAlloc(&c->hstat, sizeof(DevStatus), cudaHostAllocDefault)) != cudaSuccess) return fail(e);
-  mark("status");
-  c->nbx = (g->nx + 7) / 8;
-  c->nby = (g->ny + 7) / 8;
-  c->nbz = (g->nz + 7) / 8;
-  c->nblocks = (long long)c->nbx * c->nby * c->nbz;
-  if ((e = ctx_malloc(c, &c->bchg, (size_t)c->nblocks * kRing * 4)) != cudaSuccess) return fail(e);
-  if ((e = ctx_malloc(c, &c->bact, (size_t)c->nblocks)) != cudaSuccess) return fail(e);
-  if (o.scheduler == PDFS_SCHED_LEARNED) {
-    const float *blob = o.mlp_weights ? o.mlp_weights : default_mlp_blob();
-    std::vector<uint16_t> wb(PDFS_MLP_PARAMS);
-    for (int i = 0; i < PDFS_MLP_PARAMS; ++i) {  // bf16 values: the upper half of the float
-      uint32_t u;
-      std::memcpy(&u, &blob[i], 4);
-      wb[i] = (uint16_t)(u >> 16);
-    }
-    c->mlp_thr = blob[PDFS_MLP_PARAMS];
-    if ((e = ctx_malloc(c, &c->mlp_w, PDFS_MLP_PARAMS * 2)) != cudaSuccess) return fail(e);
-    if ((e = ctx_malloc(c, &c->bmin, (size_t)c->nblocks * 4)) != cudaSuccess) return fail(e);
-    if ((e = cudaMemcpyAsync(c->mlp_w, wb.data(), PDFS_MLP_PARAMS * 2, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+  if (!wb.empty() &&
+      (e = cudaMemcpyAsync(c->mlp_w, wb.data(), PDFS_MLP_PARAMS * 2, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+    return fail(e);
+  for (int k = 0; k < 2; ++k) {
+    int *dst = k ? c->tord64 : c->tord32;
+    if (!bo[k].empty() &&
+        (e = cudaMemcpyAsync(dst, bo[k].data(), bo[k].size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
       return fail(e);
   }
-  mark("blocks");
-  {
-    // brick tiles: ticket orders and the completion flags (epoch 0 = never)
-    size_t nflags = 0;
-    for (int k = 0; k < 2; ++k) {
-      const TileShape ts = k ? s64 : s32;
-      if (ts.bz == 0) continue;
-      int *nt = k ? c->nt64 : c->nt32;
-      nt[0] = (g->nx + ts.tx - 1) / ts.tx;
-      nt[1] = (g->ny + ts.ty - 1) / ts.ty;
-      nt[2] = (g->nz + ts.bz - 1) / ts.bz;
-      std::vector<int> bo = brick_order(nt[0], nt[1], nt[2]);
-      int **dst = k ? &c->tord64 : &c->tord32;
-      if ((e = ctx_malloc(c, dst, bo.size() * 4)) != cudaSuccess) return fail(e);
-      if ((e = cudaMemcpyAsync(*dst, bo.data(), bo.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
-        return fail(e);
-      nflags = std::max(nflags, bo.size());
-    }
-    if (nflags) {
-      if ((e = ctx_malloc(c, &c->tflag, nflags * 4)) != cudaSuccess) return fail(e);
-      if ((e = cudaMemsetAsync(c->tflag, 0, nflags * 4, c->st)) != cudaSuccess) return fail(e);
-    }
-    mark("brick orders");
-    // pencils: two faces of prow diagonals x 16 entries x 2 words per pencil
-    // (tag 0 never matches: epochs start at 1)
-    if (s32.pencil || s64.pencil) {
-      const size_t ncol = (size_t)((g->nx + 15) / 16) * ((g->ny + 15) / 16);
-      c->prow = g->nz + 15;
-      const size_t words = ncol * 2 * (size_t)c->prow * 16 * 2;
-      if ((e = ctx_malloc(c, &c->pmail, words * 8)) != cudaSuccess) return fail(e);
-      if ((e = cudaMemsetAsync(c->pmail, 0, words * 8, c->st)) != cudaSuccess) return fail(e);
-    }
-  }
-  mark("pencil mail");
-  {
-    std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
-                     w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
-    if ((e = ctx_malloc(c, &c->order32, w32.size() * 4)) != cudaSuccess) return fail(e);
-    if ((e = ctx_malloc(c, &c->order64, w64.size() * 4)) != cudaSuccess) return fail(e);
-    if ((e = cudaMemcpyAsync(c->order32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
-      return fail(e);
-    if ((e = cudaMemcpyAsync(c->order64, w64.data(), w64.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
-      return fail(e);
-  }
+  if (nflags && (e = cudaMemsetAsync(c->tflag, 0, nflags * 4, c->st)) != cudaSuccess) return fail(e);
+  if (pmail_words && (e = cudaMemsetAsync(c->pmail, 0, pmail_words * 8, c->st)) != cudaSuccess) return fail(e);
+  if ((e = cudaMemcpyAsync(c->order32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+    return fail(e);
+  if ((e = cudaMemcpyAsync(c->order64, w64.data(), w64.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+    return fail(e);
   const auto t_alloc = std::chrono::steady_clock::now();
   // padding outside the halo-padded grid is never written by the sweeps; fill it with +inf once
   if (c->in64) k_fill<double><<<2 * c->sms, 256, 0, c->st>>>(c->in64, c->L64.elems, INFINITY);
@@ -533,7 +620,7 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
       fprintf(stderr, "%s %.1f, ", m.first, ms(t, m.second));
       t = m.second;
     }
-    fprintf(stderr, "columns %.1f, fills %.1f)\n", ms(t, t_alloc), ms(t_alloc, t_end));
+    fprintf(stderr, "tables %.1f, fills %.1f)\n", ms(t, t_alloc), ms(t_alloc, t_end));
   }
   *out = c;
   return PDFS_OK;
@@ -542,13 +629,11 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
 extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->dev);
-  void *bufs[] = {(void *)c->in64, (void *)c->u64, (void *)c->bcap64, (void *)c->bcap32, (void *)c->u32,
-                  (void *)c->fmask, (void *)c->stage, (void *)c->order32, (void *)c->order64, (void *)c->tflag,
-                  (void *)c->pmail, (void *)c->tord32, (void *)c->tord64, (void *)c->progress, (void *)c->mailbox,
-                  (void *)c->ticket, (void *)c->dstat, (void *)c->bchg, (void *)c->bact, (void *)c->bmin,
-                  (void *)c->mlp_w};
-  for (void *p : bufs) ctx_free(c, p);
+  // every block is idle before it goes back to the cache
+  if (c->st2) cudaStreamSynchronize(c->st2);
   if (c->st) cudaStreamSynchronize(c->st);
+  ctx_free(c, c->arena, c->arena_bytes);
+  ctx_free(c, c->stage, c->stage_bytes);
   if (c->hstat) cudaFreeHost(c->hstat);
   if (c->e0) cudaEventDestroy(c->e0);
   if (c->e1) cudaEventDestroy(c->e1);
@@ -570,7 +655,8 @@ static size_t ref_nodes(const pdfs_grid &g) { return (size_t)(g.nx + 2) * (g.ny 
 static int ensure_stage(pdfs_ctx *c) {
   const size_t b = ref_nodes(c->g) * 9;
   if (c->stage_bytes >= b) return PDFS_OK;
-  ctx_free(c, c->stage);
+  if (c->stage) CK(cudaStreamSynchronize(c->st));  // the old stage is idle
+  ctx_free(c, c->stage, c->stage_bytes);
   c->stage = nullptr;
   c->stage_bytes = 0;
   CK(ctx_malloc(c, &c->stage, b));
