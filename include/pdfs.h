@@ -153,7 +153,13 @@ int pdfs_ctx_load(pdfs_ctx *c, const double *field, const uint8_t *frozen);
 int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats);
 /* Copies the solution into field (host or device pointer, reference layout). */
 int pdfs_ctx_store(pdfs_ctx *c, double *field);
+/* Frees the context.  Its device blocks go to a per-process cache (at most a
+ * quarter of the device's memory), from which the next context of about the
+ * same size takes them: repeated solves skip cudaMalloc and cudaFree. */
 void pdfs_ctx_destroy(pdfs_ctx *c);
+/* Returns every cached block of the device to CUDA (for callers that need
+ * the memory elsewhere).  Contexts still alive keep their blocks. */
+int pdfs_release_cached(int device);
 
 /* The 8^3 node blocks of a context's grid: nbx = ceil(nx/8), nby, nbz alike.
  * Block (bx, by, bz) has index (bz*nby + by)*nbx + bx and holds interior

@@ -27,7 +27,7 @@ SCHED_NONE, SCHED_CHANGE, SCHED_LEARNED = 0, 1, 2
 # Every function declared in include/pdfs.h (the CPU tests check the exports).
 EXPORTS = [
     "pdfs_default_opts", "pdfs_solve", "pdfs_sweep", "pdfs_ctx_create", "pdfs_ctx_load", "pdfs_ctx_run",
-    "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_status_string", "pdfs_version",
+    "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_release_cached", "pdfs_status_string", "pdfs_version",
     "run_fsm", "pdfs_vti_read", "pdfs_vti_write", "pdfs_phi_free", "pdfs_calc_dist_field",
     "pdfs_solve_batch", "pdfs_autotune", "pdfs_static_layout", "pdfs_sweep_static",
     "pdfs_ctx_blocks", "pdfs_ctx_sweep",
@@ -101,6 +101,8 @@ def load(path: str = LIB_PATH):
     L.pdfs_ctx_store.restype = ip
     L.pdfs_ctx_destroy.argtypes = [vp]
     L.pdfs_ctx_destroy.restype = None
+    L.pdfs_release_cached.argtypes = [ip]
+    L.pdfs_release_cached.restype = ip
     L.pdfs_status_string.argtypes = [ip]
     L.pdfs_status_string.restype = C.c_char_p
     L.pdfs_version.argtypes = []

@@ -113,6 +113,14 @@ def solve_batch(fields, spacings, frozen=None, **kw):
     return [x.as_dict() for x in st]
 
 
+def release_cached(device: int = 0) -> None:
+    """Returns the device blocks that destroyed contexts left in the library's
+    cache to CUDA (pdfs_release_cached)."""
+    s = L.load().pdfs_release_cached(int(device))
+    if s != L.PDFS_OK:
+        raise PdfsError(s, "pdfs_release_cached")
+
+
 def autotune(nx, ny, nz, spacing, **kw) -> int:
     """Fastest tile pair for this grid shape (an opts.tile value)."""
     g = L.Grid(nx, ny, nz, *map(float, spacing))

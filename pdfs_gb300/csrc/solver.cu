@@ -400,6 +400,18 @@ static void ctx_free(pdfs_ctx *c, void *p, size_t bytes) {
   cudaFree(p);
 }
 
+extern "C" int pdfs_release_cached(int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return PDFS_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) return PDFS_ERR_INVALID;
+  CK(cudaSetDevice(device));
+  cache_release(device);
+  return PDFS_OK;
+}
+
 static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   if (!g || !o) return PDFS_ERR_INVALID;
   if (g->nx < 1 || g->ny < 1 || g->nz < 1) return PDFS_ERR_INVALID;
