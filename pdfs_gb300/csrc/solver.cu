@@ -499,8 +499,8 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
   mark("stream");
   // Host tables first, then every device buffer of the context carved from
-  // one pool allocation (a batch creates hundreds of contexts, and a pool
-  // allocation's cost grows with the number of blocks the pool holds).
+  // one allocation (a batch creates hundreds of contexts: one allocation, or
+  // one cached block, per context keeps their set-up short).
   c->nbx = (g->nx + 7) / 8;
   c->nby = (g->ny + 7) / 8;
   c->nbz = (g->nz + 7) / 8;
