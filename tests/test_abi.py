@@ -64,10 +64,18 @@ def test_invalid_options_rejected():
         o = api.make_opts()
         setattr(o, k, v)
         assert L.load().pdfs_solve(C.byref(g), f.ctypes.data, None, C.byref(o), None) == L.PDFS_ERR_INVALID, k
-    # FP32 pairs run on the FP64 bricks (tile 5) only
+    # FP32 pairs run on the FP64 bricks and pencils (tiles 5-8) only
     o = api.make_opts(arith=L.ARITH_PAIR, tile=1 << 8)
     assert L.load().pdfs_solve(C.byref(g), f.ctypes.data, None, C.byref(o), None) == L.PDFS_ERR_INVALID
     assert L.load().pdfs_sweep(C.byref(g), f.ctypes.data, None, 0, None, None) == L.PDFS_ERR_INVALID
+
+
+def test_release_cached_checks_its_device():
+    from conftest import have_gpu
+    s = L.load().pdfs_release_cached(-1)
+    assert s == (L.PDFS_ERR_INVALID if have_gpu() else L.PDFS_ERR_NO_DEVICE)
+    if not have_gpu():
+        assert L.load().pdfs_release_cached(0) == L.PDFS_ERR_NO_DEVICE
 
 
 def test_no_cpu_fallback_without_device():
