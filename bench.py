@@ -1,14 +1,18 @@
 """Benchmark of the GB300 FSM distance-field solve.
 
-Metric (the reference's headline): time-to-converge and Gvoxel-updates/s of
-the FP32-bulk + FP64-polish solve (with active-block scheduling) against the
-plain FP64 FSM, at <= 1e-6 relative error.
+Metric (the reference's headline, printed identically by both arms):
+time-to-converge and Gvoxel-updates/s of the learned-scheduler FP32-bulk +
+FP64-precision-polish solve against the plain FP64 FSM, at <= 1e-6
+relative error.  Gvox-updates/s are plain-equivalent: the plain FP64 FSM's
+node updates on the same input (interior nodes x its sweep count) divided by
+the time to converge.  The reference arm runs the plain FP64 FSM itself, so
+its rate is its own per-ordering rate.
 
 One step = one complete solve of the workload to convergence, from the input
-already resident in HBM (pdfs_ctx_run).  value = plain-equivalent
-Gvox-updates/s: (interior nodes x sweeps the plain FP64 FSM needs on this
-input) / (time of our solve).  e2e = the same through pdfs_solve() with pinned
-host buffers, host<->device copies and layout passes inside the timed region.
+already resident in HBM (pdfs_ctx_run), timed on the device by CUDA events
+on the solve's stream.  e2e = the same through pdfs_solve() with pinned host
+buffers, host<->device copies and layout passes inside the timed region,
+averaged over the same number of steps.
 
 Default workload: 768^3, dx = 1, union of 150 seeded spheres (radii
 log-uniform 4..50 cells), interface nodes frozen; inputs (3.6 GB) are larger
@@ -34,6 +38,10 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 
+METRIC = "time-to-converge & Gvox-updates/s: learned+FP32 vs plain FP64 FSM at 1e-6 err"
+UNIT = "Gvox-updates/s"
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -42,7 +50,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="C4")
     p.add_argument("--mode", default="polish", choices=["polish", "fp32", "fp64", "fp64ref"])
-    p.add_argument("--scheduler", default="none", choices=["none", "change", "learned"])
+    p.add_argument("--scheduler", default="learned", choices=["none", "change", "learned"])
     p.add_argument("--tol", type=float, default=1e-5, help="FP64 polish tolerance (max change)")
     p.add_argument("--polish-arith", default="pair", choices=["mixed", "pair", "fast"],
                    help="polish arithmetic: FP32 increments over an FP64 field (mixed) or an FP32-pair "
@@ -50,11 +58,13 @@ def parse():
     p.add_argument("--no-sched-table", action="store_true", help="skip timing the three schedulers")
     p.add_argument("--configs", action="store_true",
                    help="accuracy report: every config's FP32 + polish solve against the plain FP64 FSM")
+    p.add_argument("--config-list", default="", help="--configs: which configs (comma-separated, default C1..C4)")
     p.add_argument("--tile", type=int, default=0)
     p.add_argument("--fixed-sweeps", type=int, default=0, help="profiling: run exactly this many sweeps")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 FSM comparison solve")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--no-fp64-polish", action="store_true", help="skip the all-FP64 polish comparison solve")
     p.add_argument("--cpu-sweeps", type=int, default=0, help="CPU sample: sweeps of the full grid")
     return p.parse_args()
 
@@ -212,56 +222,67 @@ def traffic_per_launch(kind, prec, nodes, tile):
     except (OSError, ValueError):
         return None
     key = "fp32" if kind == "fp32" else ("fp64_replace" if prec == L.PREC_FP32_POLISH64 else "fp64_min")
-    k = kernel_kind(kind, tile)
-    if k != "column":
-        key += "_" + k
+    key += "_" + kernel_kind(kind, tile)
     e = t.get(key)
     return None if not e else float(e["dram_bytes_per_update"]) * nodes
 
 
-def cpu_baseline(w, sweeps, threads):
-    """The CPU restatement of the reference FSM (OpenMP over each hyperplane),
-    timed on the host cores on `sweeps` orderings of the full grid."""
+def _cpu_fsm(w, threads):
+    """The reference's CPU FSM path for one ordering of the full grid:
+    its own OpenACC loop built for host multicore (oracle/_ref, where the
+    reference's sources were present to build it), else the oracle port (OpenMP
+    over each hyperplane).  Returns (sweep(a, sn), kind, what)."""
     from oracle import oracle as O
-    O.build(ref=False)
-    a = w.field.copy()
     sp = (w.dx, w.dy, w.dz)
+    O.build(ref=False)
+    if O.have_ref(omp=True):
+        os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+        return (lambda a, sn: O.ref_sweep_raw(a, sp, sn, omp=True)), "reference", \
+            "the reference's mpi_openacc phi3D_fsm.c, OpenACC loop as OpenMP (interface not frozen: it has no mask)"
+    return (lambda a, sn: O.sweep(a, sp, sn, frozen=w.frozen, threads=threads)), "port", \
+        "the oracle port of the reference's FSM (OpenMP over hyperplanes)"
+
+
+def cpu_baseline(w, sweeps, threads):
+    """The reference's CPU FSM path timed on the host cores on `sweeps`
+    orderings of the full grid."""
+    run, kind, what = _cpu_fsm(w, threads)
+    a = w.field.copy()
     t0 = time.perf_counter()
     for s in range(sweeps):
-        O.sweep(a, sp, s % 8 + 1, frozen=w.frozen, threads=threads)
+        run(a, s % 8 + 1)
     dt = time.perf_counter() - t0
-    return w.interior * sweeps / dt / 1e9, dt
+    return w.interior * sweeps / dt / 1e9, dt, kind, what
 
 
 def run_reference(args, rank, world, pg):
-    """Reference arm: the reference's CPU FSM path on the host cores (the
-    oracle port; the reference sources are not available on the GPU machine)."""
+    """Reference arm: the reference's CPU FSM path on the host cores, one
+    ordering of the full grid per step.  The plain FP64 FSM's plain-equivalent
+    rate is its own rate, so the line carries the same metric and unit as our
+    arm's."""
     if rank != 0:
         return
-    from oracle import oracle as O
     w = workload(args.workload)
     threads = os.cpu_count() or 1
-    kind = "port"
-    sp = (w.dx, w.dy, w.dz)
+    run, kind, what = _cpu_fsm(w, threads)
     a = w.field.copy()
-    O.build(ref=False)
     for s in range(args.warmup):
-        O.sweep(a, sp, s % 8 + 1, frozen=w.frozen, threads=threads)
+        run(a, s % 8 + 1)
     times = []
     for s in range(args.steps):
         t0 = time.perf_counter()
-        O.sweep(a, sp, (args.warmup + s) % 8 + 1, frozen=w.frozen, threads=threads)
+        run(a, (args.warmup + s) % 8 + 1)
         times.append(time.perf_counter() - t0)
     t = float(np.mean(times))
     v = w.interior / t / 1e9
-    line = {"metric": "Gvox-updates/s (plain FP64 FSM, one ordering per step)", "value": v,
-            "unit": "Gvox-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "parallelism": "host threads"},
-            "cpu_baseline": {"value": v, "unit": "Gvox-updates/s", "cores": threads, "kind": kind,
-                             "sample": f"one FP64 ordering over the full {w.nx}x{w.ny}x{w.nz} grid per step"},
-            "e2e": {"value": v, "unit": "Gvox-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "parallelism": "host threads",
+                       "step": "one plain FP64 ordering of the full grid"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"one FP64 ordering over the full {w.nx}x{w.ny}x{w.nz} grid per step: {what}"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -332,43 +353,64 @@ def run_batch(args, rank, world, pg, device):
 
 
 def run_configs(args, device):
-    """One JSON line per config (C1..C4): the FP32 + pair-polish and
-    FP32 + mixed-polish solves and the FP32-only solve against the plain FP64
-    FSM on the same input -- max
-    and RMS relative error, sweeps and times.  C1 also runs the FP64
-    reference arithmetic (bit-exact with the reference at tol 1e-12)."""
+    """One JSON line per config (C1..C4): against the oracle's FP64 plain-FSM
+    fixed point (tol 1e-12, every host core), the max and RMS relative error
+    of the plain FP64 GPU solve, the FP32 + pair-polish, FP32 + FP64-polish
+    and FP32-only solves, and the learned-scheduler headline solve, with their
+    times end to end through pdfs_solve (host buffers).  C1 also runs the FP64
+    reference arithmetic, which must be bit-exact."""
+    from oracle import oracle as O
     from pdfs_gb300 import _lib as L
     from pdfs_gb300 import api
     from pdfs_gb300 import workloads as W
-    for name in ("C1", "C2", "C3", "C4"):
+    threads = os.cpu_count() or 1
+    names = args.config_list.split(",") if args.config_list else ["C1", "C2", "C3", "C4"]
+    for name in names:
         w = W.config(name)
         sp = (w.dx, w.dy, w.dz)
         h = min(sp)
         fz = dict(frozen=w.frozen, freeze=L.FREEZE_MASK, device=device)
-        ref = w.field.copy()
+        orc = w.field.copy()
         t0 = time.perf_counter()
-        ps = api.solve(ref, sp, precision=L.PREC_FP64, arith=L.ARITH_FAST, tol=1e-12, **fz)
-        t_plain = time.perf_counter() - t0
+        o_sweeps, _ = O.solve(orc, sp, tol=1e-12, frozen=w.frozen, threads=threads)
+        t_orc = time.perf_counter() - t0
         i = (slice(1, -1),) * 3
-        den = np.maximum(np.abs(ref[i]), h)
+        den = np.maximum(np.abs(orc[i]), h)
+
+        def err(f):
+            e = np.abs(f[i] - orc[i]) / den
+            return float(e.max()), float(np.sqrt(np.mean(e * e)))
+
         out = {"config": name, "workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "spacing": list(sp),
-               "plain_fp64": {"sweeps": ps["sweeps_fp64"], "time_s": t_plain}}
-        cases = [("fp32_polish_pair", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5 * h)),
-                 ("fp32_polish_mixed", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_MIXED, tol=1e-5 * h)),
+               "oracle": {"sweeps": o_sweeps, "time_s": t_orc, "threads": threads, "tol": 1e-12}}
+        cases = [("plain_fp64_fast", dict(precision=L.PREC_FP64, arith=L.ARITH_FAST, tol=1e-12)),
+                 ("fp32_polish_pair", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5 * h)),
+                 ("fp32_polish_pair_learned", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR,
+                                                   tol=1e-5 * h, scheduler=L.SCHED_LEARNED)),
+                 ("fp32_polish_fp64", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_FAST, tol=1e-5 * h)),
                  ("fp32_only", dict(precision=L.PREC_FP32))]
-        if name == "C1":
+        if name in ("C1", "C2"):
             cases.append(("fp64_reference_arith", dict(precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, tol=1e-12)))
+        t_plain = None
         for label, kw in cases:
             f = w.field.copy()
+            api.solve(f, sp, **kw, **fz)  # warm (allocations, module loads)
+            f[:] = w.field
             t0 = time.perf_counter()
             st = api.solve(f, sp, **kw, **fz)
             t = time.perf_counter() - t0
-            e = np.abs(f[i] - ref[i]) / den
-            out[label] = {"max_rel_err": float(e.max()), "rms_rel_err": float(np.sqrt(np.mean(e * e))),
-                          "sweeps_fp32": st["sweeps_fp32"], "sweeps_fp64": st["sweeps_fp64"], "time_s": t,
-                          "speedup_vs_plain": t_plain / t}
+            mx, rms = err(f)
+            out[label] = {"max_rel_err": mx, "rms_rel_err": rms, "sweeps_fp32": st["sweeps_fp32"],
+                          "sweeps_fp64": st["sweeps_fp64"], "time_s": t, "run_ms_device": st["ms_device"]}
+            if label == "plain_fp64_fast":
+                t_plain = t
+            elif t_plain:
+                out[label]["speedup_vs_plain_fp64"] = t_plain / t
+            if label == "fp64_reference_arith":
+                out[label]["bit_exact"] = bool(f.tobytes() == orc.tobytes())
+            del f
         print(json.dumps(out), flush=True)
-        del w, ref
+        del w, orc, den
 
 
 def main():
@@ -418,34 +460,59 @@ def main():
     t0 = time.perf_counter()
     stats = []
     for _ in range(args.steps):
-        stats.append(ctx.run())  # each run synchronises the device before returning
+        # each run synchronises its stream before returning; ms_device is the
+        # run's CUDA-event time on the solve's stream, first kernel to last
+        stats.append(ctx.run())
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     barrier(pg)
+    t_dev = sum(x["ms_device"] for x in stats) / 1e3
+    t_dev = max_over_ranks(pg, t_dev)
     wall = max_over_ranks(pg, wall)
-    t_step = wall / args.steps
+    t_step = t_dev / args.steps
     out = np.empty_like(w.field)
     ctx.store(out)
     ctx.close()
     st = stats[-1]
+    i = (slice(1, -1),) * 3
 
     # plain FP64 FSM on the same input: sweep count (for the plain-equivalent
     # rate), its time, and the error of our answer against it
-    plain = None
+    plain, ref = None, None
     if not args.no_plain and args.fixed_sweeps == 0:
         ref = w.field.copy()
         ps = api.solve(ref, sp, frozen=w.frozen, freeze=freeze, precision=L.PREC_FP64, arith=L.ARITH_FAST,
                        tol=1e-12, device=device)
-        i = (slice(1, -1),) * 3
-        err = float(np.max(np.abs(out[i] - ref[i]) / np.maximum(np.abs(ref[i]), min(sp))))
+        e = np.abs(out[i] - ref[i]) / np.maximum(np.abs(ref[i]), min(sp))
         plain = {"sweeps": ps["sweeps_fp64"], "time_s": (ps["ms_fp64"] + 0.0) / 1e3,
-                 "kernel_ms": ps["ms_kern_fp64"], "max_rel_err_vs_plain": err}
+                 "kernel_ms": ps["ms_kern_fp64"], "max_rel_err_vs_plain": float(e.max()),
+                 "rms_rel_err_vs_plain": float(np.sqrt(np.mean(e * e)))}
+        del e
     plain_sweeps = plain["sweeps"] if plain else (st["sweeps_fp32"] + st["sweeps_fp64"])
     # whole-job aggregate: every rank solves its own replica of the workload
     # (a single grid does not shard), timed by the slowest rank
     value = world * w.interior * plain_sweeps / t_step / 1e9
 
-    # e2e through pdfs_solve with pinned host buffers
+    # the same solve with the polish in true FP64 arithmetic (ARITH_FAST), one warm run
+    fp64_polish = None
+    if (not args.no_fp64_polish and args.fixed_sweeps == 0 and args.mode == "polish"
+            and args.polish_arith != "fast"):
+        o2 = dict(opts, arith=L.ARITH_FAST)
+        with api.Context(w.nx, w.ny, w.nz, sp, **o2) as c2:
+            c2.load(w.field, w.frozen)
+            c2.run()
+            s2 = c2.run()
+            o64 = np.empty_like(w.field)
+            c2.store(o64)
+        fp64_polish = {"time_s": s2["ms_device"] / 1e3, "sweeps_fp32": s2["sweeps_fp32"],
+                       "sweeps_fp64": s2["sweeps_fp64"], "arith": "fast (FP64)"}
+        if ref is not None:
+            e = np.abs(o64[i] - ref[i]) / np.maximum(np.abs(ref[i]), min(sp))
+            fp64_polish.update(max_rel_err=float(e.max()), rms_rel_err=float(np.sqrt(np.mean(e * e))))
+            del e
+        del o64
+
+    # e2e through pdfs_solve with pinned host buffers, averaged over the timed steps
     e2e = None
     if not args.no_e2e and args.fixed_sweeps == 0:
         try:
@@ -455,18 +522,23 @@ def main():
             hf.numpy()[:] = w.field
             hm.numpy()[:] = w.frozen
             f_np, m_np = hf.numpy(), hm.numpy()
+            pinned = True
         except Exception:
             f_np, m_np = w.field.copy(), w.frozen
+            pinned = False
+        api.solve(f_np, sp, frozen=m_np, **opts)  # warm
         ts = []
-        for k in range(2):
-            f_np[:] = w.field
+        for k in range(args.steps):
+            f_np[:] = w.field  # the step's input, outside the timed region
+            barrier(pg)
             t1 = time.perf_counter()
             api.solve(f_np, sp, frozen=m_np, **opts)
             ts.append(time.perf_counter() - t1)
-        te = max_over_ranks(pg, min(ts))
-        e2e = {"value": world * w.interior * plain_sweeps / te / 1e9, "unit": "Gvox-updates/s",
+        te = max_over_ranks(pg, float(np.mean(ts)))
+        e2e = {"value": world * w.interior * plain_sweeps / te / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": int(world * (w.field.nbytes + w.frozen.nbytes)),
-               "d2h_bytes_per_step": int(world * w.field.nbytes), "time_to_converge_s": te}
+               "d2h_bytes_per_step": int(world * w.field.nbytes), "time_to_converge_s": te,
+               "steps": len(ts), "host_buffers": "pinned" if pinned else "pageable"}
 
     # roofline of the dominant kernel
     pk = peaks()
@@ -475,21 +547,25 @@ def main():
     s32, s64 = st["sweeps_fp32"], st["sweeps_fp64"]
     dominant = "fp64" if k64 >= k32 else "fp32"
     mask_b = 1.0 / 8.0
+    # executed updates of the dominant phase (scheduled sweeps count only their active blocks)
     if dominant == "fp32":
-        per_launch = w.interior * (8 + mask_b)
-        dur = k32 / max(s32, 1)
+        upd = st["voxel_updates_fp32"] if "voxel_updates_fp32" in st else w.interior * s32
+        per_update = 8 + mask_b
+        dur = k32
     else:
         # 2 * sizeof(T) per voxel-update plus the frozen-mask bit; the polish's cap
-        # reads are not algorithmic bytes (bricks and pencils skip them where a
-        # block's smallest cap is above the new value)
-        per_launch = w.interior * (16 + mask_b)
-        dur = k64 / max(s64, 1)
-    achieved = per_launch / (dur / 1e3) / 1e9 if dur > 0 else 0.0
+        # reads are not algorithmic bytes (the kernels skip them where a block's
+        # smallest cap is above the new value)
+        upd = st["voxel_updates_fp64"] if "voxel_updates_fp64" in st else w.interior * s64
+        per_update = 16 + mask_b
+        dur = k64
+    achieved = upd * per_update / (dur / 1e3) / 1e9 if dur > 0 else 0.0
+    nsw = max(s32 if dominant == "fp32" else s64, 1)
     kname = kernel_name(dominant, st["tile"], prec, arith)
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": traffic_per_launch(dominant, prec, w.interior, st["tile"]), "kernel": kname,
+            "traffic": traffic_per_launch(dominant, prec, upd / nsw, st["tile"]), "kernel": kname,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s",
-            "bytes_per_update": per_launch / w.interior}
+            "bytes_per_update": per_update, "launches_per_step": nsw, "ms_per_launch": dur / nsw}
     fp32_roof = None
     if s32:
         a32 = w.interior * (8 + mask_b) / (k32 / s32 / 1e3) / 1e9
@@ -505,9 +581,8 @@ def main():
                 with api.Context(w.nx, w.ny, w.nz, sp, **o2) as c2:
                     c2.load(w.field, w.frozen)
                     c2.run()
-                    t1 = time.perf_counter()
                     s2 = c2.run()
-                    sched_table[name] = {"time_s": time.perf_counter() - t1,
+                    sched_table[name] = {"time_s": s2["ms_device"] / 1e3,
                                          "sweeps": s2["sweeps_fp32"] + s2["sweeps_fp64"],
                                          "full_sweeps": s2["full_sweeps"],
                                          "voxel_updates_per_node": s2["voxel_updates"] / w.interior}
@@ -518,28 +593,28 @@ def main():
     if rank == 0 and world >= 1 and not args.no_cpu and args.fixed_sweeps == 0:
         threads = os.cpu_count() or 1
         sweeps = args.cpu_sweeps or 2
-        v, dt = cpu_baseline(w, sweeps, threads)
-        cpu = {"value": v, "unit": "Gvox-updates/s", "cores": threads, "kind": "port",
-               "sample": f"{sweeps} FP64 orderings of the full grid ({dt:.1f} s), OpenMP over hyperplanes"}
+        v, dt, kind, what = cpu_baseline(w, sweeps, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{sweeps} FP64 orderings of the full grid ({dt:.1f} s): {what}"}
 
     if rank == 0:
+        dtype = {L.ARITH_PAIR: "f32+f32pair", L.ARITH_MIXED: "f32+f64mixed"}.get(arith, "f32+f64") \
+            if prec == L.PREC_FP32_POLISH64 else ("f32" if prec == L.PREC_FP32 else "f64")
         line = {
-            "metric": "time-to-converge & Gvox-updates/s (plain-equivalent): FP32 bulk + FP64 polish with "
-                      "active-block scheduling vs plain FP64 FSM at <=1e-6 rel err",
-            "value": value, "unit": "Gvox-updates/s", "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if prec == L.PREC_FP32_POLISH64 else
-            ("f32" if prec == L.PREC_FP32 else "f64"), "data": "synthetic (seeded spheres)",
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded spheres)",
             "config": {"workload": w.name, "nx": w.nx, "ny": w.ny, "nz": w.nz, "spacing": list(sp),
                        "mode": args.mode, "scheduler": args.scheduler, "polish_tol": args.tol,
                        "polish_arith": args.polish_arith if args.mode == "polish" else None,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (no flush needed)"},
-            "time_to_converge_s": t_step,
+            "time_to_converge_s": t_step, "wall_s_per_step": wall / args.steps,
             "sweeps": {"fp32": s32, "fp64": s64, "full": st["full_sweeps"],
                        "voxel_updates": st["voxel_updates"], "blocks_skipped": st["blocks_skipped"]},
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (plain["time_s"] / t_step) if plain else None,
+            "fp64_polish": fp64_polish,
             "roofline": roof, "roofline_fp32_sweep": fp32_roof, "schedulers": sched_table,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(sum(s["launches"] for s in stats)),
             "clocks": clk,

@@ -40,7 +40,10 @@ typedef struct {
 /* Arithmetic of the sweeps. */
 enum {
   PDFS_PREC_FP64 = 0,          /* every sweep in FP64                                        */
-  PDFS_PREC_FP32 = 1,          /* FP32 sweeps to an exact FP32 fixed point, widened to FP64   */
+  PDFS_PREC_FP32 = 1,          /* FP32 sweeps until a full sweep's max relative change
+                                  |u_new - u_old| / max(u_new, h) is <= 4e-6 (FP32 rounding
+                                  keeps sweeps changing by about 1e-7 relative), widened
+                                  to FP64                                                    */
   PDFS_PREC_FP32_POLISH64 = 2, /* FP32 bulk sweeps, then FP64 replace-update polish sweeps    */
 };
 
@@ -120,7 +123,10 @@ typedef struct {
   double ms_kern_fp64;        /* summed durations of the FP64 sweep kernels alone    */
   int tile;                   /* tile variant used (FP32 id | FP64 id << 8)         */
   int launches;               /* kernels this call launched                          */
-  int reserved[6];
+  double ms_device;           /* pdfs_ctx_run: device time from its first to its last
+                                 kernel (CUDA events on the context's stream)        */
+  long long voxel_updates_fp64; /* the part of voxel_updates done by FP64 sweeps     */
+  int reserved[2];
 } pdfs_stats;
 
 /* Fills *o with the defaults: FP64, reference arithmetic, no freezing, no
@@ -278,9 +284,15 @@ int pdfs_mlp_infer(const float *blob, const uint16_t *x, int n, float *logits);
  * count; entries outside the halo-padded grid are not read for any result
  * (fill them with +inf).
  *
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  Every call shares the one array and leaves its contents behind:
+ * The first call in a device's context looks up the array's device address
+ * (once per context, with that device current; after a cudaDeviceReset the
+ * next call looks it up again); make that first call before any stream
+ * capture.  CUDA loads modules lazily by default, so the array itself is
+ * reserved during that first call: make one call (a 1 x 1 x 1 grid will do)
+ * on each device during set-up, before the phase in which nothing may be
+ * allocated.  The wait bound and the test hook of the allocating path apply
+ * (PDFS_WAIT_MS, PDFS_TEST_POISON_COLUMN; a wait that gives up returns
+ * PDFS_ERR_TIMEOUT).  Every call shares the one array and leaves its contents behind:
  * each call clears the words that must start at zero, but calls whose work
  * overlaps on the GPU (concurrent streams, other host threads) race on it and
  * must be serialised by the caller. */

@@ -21,7 +21,25 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref_fsm.so")
 REF_OMP_PATH = os.path.join(HERE, "_ref", "libref_fsm_omp.so")
-REF_SRC = "/root/reference/mpi_openacc/src"
+
+
+def ref_root() -> str:
+    """The reference tree: $PDFS_REF_ROOT, else the default of oracle/Makefile
+    (the recipe that builds the reference's own solver from its sources)."""
+    r = os.environ.get("PDFS_REF_ROOT")
+    if r:
+        return r
+    try:
+        out = subprocess.run(["make", "-s", "-C", HERE, "print-ref-root"], check=True, capture_output=True,
+                             text=True).stdout.strip()
+        return out.splitlines()[-1] if out else ""
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+
+
+def ref_src() -> str:
+    """Directory of the reference's MPI/OpenACC solver sources (may not exist)."""
+    return os.path.join(ref_root(), "mpi_openacc", "src")
 
 _lib = None
 _ref = {}
@@ -32,8 +50,8 @@ _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 
 def build(ref: bool = True) -> None:
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref and os.path.isdir(REF_SRC):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if ref and os.path.isdir(ref_src()):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_ROOT=" + ref_root()], check=True)
 
 
 def lib():
@@ -125,6 +143,13 @@ def ref_sweep(u, spacing, sn, omp=False) -> float:
         d = np.abs(u - before)
     d = d[np.isfinite(d)]
     return float(d.max()) if d.size else 0.0
+
+
+def ref_sweep_raw(u, spacing, sn, omp=False) -> None:
+    """The reference's runFSM(pf, sn) on u, in place, without measuring the
+    change (for timing)."""
+    nx, ny, nz = _dims(u)
+    ref(omp).ref_sweep(nx, ny, nz, *spacing, u, sn)
 
 
 def ref_solve(u, spacing, tol=0.0, max_sweeps=10_000, omp=False):

@@ -59,10 +59,12 @@ class Stats(C.Structure):
                 ("ms_d2h", C.c_double), ("ms_fp32", C.c_double), ("ms_fp64", C.c_double),
                 ("ms_sched", C.c_double), ("ms_kern_fp32", C.c_double),
                 ("ms_kern_fp64", C.c_double), ("tile", C.c_int), ("launches", C.c_int),
-                ("reserved", C.c_int * 6)]
+                ("ms_device", C.c_double), ("voxel_updates_fp64", C.c_longlong), ("reserved", C.c_int * 2)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        d["voxel_updates_fp32"] = d["voxel_updates"] - d["voxel_updates_fp64"]
+        return d
 
 
 class Phi(C.Structure):

@@ -225,6 +225,7 @@ int batch_phase(BatchState &B, std::vector<pdfs_ctx *> &ctx, const std::vector<i
       pdfs_stats &S = st[g];
       const long long nodes = (long long)ctx[g]->g.nx * ctx[g]->g.ny * ctx[g]->g.nz;
       S.voxel_updates += nodes * 8;
+      if (!f32) S.voxel_updates_fp64 += nodes * 8;
       S.full_sweeps += 8;
       if (f32)
         S.sweeps_fp32 += 8;

@@ -164,6 +164,7 @@ struct pdfs_ctx {
   bool loaded = false, has_mask = false;
   int last_prec = -1;      // which working field holds the last result
   cudaEvent_t e0 = nullptr, e1 = nullptr, k0 = nullptr, k1 = nullptr, q0 = nullptr, q1 = nullptr;
+  cudaEvent_t r0 = nullptr, r1 = nullptr;  // around a whole pdfs_ctx_run
   // load / store pipeline: slab copies on st, layout kernels on st2
   cudaStream_t st2 = nullptr;
   static constexpr int kSlabs = 32;

@@ -12,14 +12,26 @@
 //
 // Host code must not pass g_scratch itself to a kernel: in host code the
 // name is only a host-side stand-in for the symbol.  Its device address is
-// looked up once per device with cudaGetSymbolAddress (the first call on a
-// device does it, so make that call before any stream capture), and that
-// address is what the kernel receives.  All calls share the array and leave
-// their contents behind; each call zeroes the words that must start at zero
-// (column progress, ticket, status), and calls that overlap on the GPU race
-// on the array, so the caller serialises them.
+// looked up with cudaGetSymbolAddress once per device context, with that
+// device current (the first call in a context does it, so make that call
+// before any stream capture), and that address is what the kernel receives.
+// The address is cached per device together with the id of the context it
+// belongs to, under a lock: after a cudaDeviceReset (a new primary context,
+// into which the module and its array are loaded again) or under another
+// driver context the lookup is repeated, so a stale address is never used.
+// CUDA loads modules lazily by default, so the array is reserved during the
+// first call on each device: make one call (a 1 x 1 x 1 grid is enough)
+// during set-up, before the phase in which nothing may be allocated.
+// All calls share the array and leave their contents behind; each call
+// zeroes the words that must start at zero (column progress, ticket,
+// status), and calls that overlap on the GPU race on the array, so the
+// caller serialises them.
+#include <cuda.h>
+
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "internal.h"
 
@@ -31,7 +43,62 @@ constexpr int kR = 1;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scratch[PDFS_STATIC_SCRATCH_BYTES];
-static void *g_scratch_dev[kMaxDevices];  // device address of g_scratch, per device (set once)
+
+// Device address of g_scratch per device, with the id of the context it was
+// looked up in (0 = none yet).  Guarded by g_scratch_mu.
+struct ScratchAddr {
+  unsigned long long ctx_id;
+  void *ptr;
+};
+static ScratchAddr g_scratch_dev[kMaxDevices];
+static std::mutex g_scratch_mu;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+template <class F>
+F driver_fn(const char *name, int version) {
+  void *p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, version, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    return reinterpret_cast<F>(p);
+  cudaGetLastError();
+  return nullptr;
+}
+
+// Id of the calling thread's current driver context, 0 if it cannot be told.
+unsigned long long current_ctx_id() {
+  static const CtxGetCurrentFn get_cur = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent", 4000);
+  static const CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId", 12000);
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_cur || !get_id || get_cur(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// g_scratch's device address in the current context of device dev.  The
+// lookup runs once per context (cudaGetSymbolAddress also makes the device's
+// primary context current if no context was); without a context id the
+// lookup runs on every call.
+cudaError_t scratch_address(int dev, unsigned char **out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  unsigned long long id = current_ctx_id();
+  ScratchAddr &e = g_scratch_dev[dev];
+  if (id != 0 && e.ctx_id == id && e.ptr) {
+    *out = static_cast<unsigned char *>(e.ptr);
+    return cudaSuccess;
+  }
+  void *ptr = nullptr;
+  cudaError_t err = cudaGetSymbolAddress(&ptr, g_scratch);
+  if (err != cudaSuccess) return err;
+  if (!ptr) return cudaErrorInvalidSymbol;
+  if (id == 0) id = current_ctx_id();  // the lookup may have made the primary context current
+  e.ctx_id = id;
+  e.ptr = ptr;
+  *out = static_cast<unsigned char *>(ptr);
+  return cudaSuccess;
+}
 
 // Offsets of the scratch regions (256-byte aligned) for one grid.
 struct ScratchPlan {
@@ -113,13 +180,8 @@ extern "C" int pdfs_sweep_static(const pdfs_grid *g, double *field_dev, int sn, 
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return status_of(e);
   if (dev < 0 || dev >= kMaxDevices) return PDFS_ERR_INVALID;
-  if (!g_scratch_dev[dev]) {  // once per device, with that device current
-    void *ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_scratch);
-    if (e != cudaSuccess || !ptr) return status_of(e != cudaSuccess ? e : cudaErrorInvalidSymbol);
-    g_scratch_dev[dev] = ptr;
-  }
-  unsigned char *base = static_cast<unsigned char *>(g_scratch_dev[dev]);
+  unsigned char *base = nullptr;
+  if ((e = scratch_address(dev, &base)) != cudaSuccess) return status_of(e);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   int sms = 0;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return status_of(e);
@@ -147,8 +209,13 @@ extern "C" int pdfs_sweep_static(const pdfs_grid *g, double *field_dev, int sn, 
   a.err = status->err;
   a.maxchg = &status->chg;
   a.hmin = (float)std::min(g->dx, std::min(g->dy, g->dz));
-  a.wait_cycles = 4000LL * 1000000LL * 21 / 10;  // 4 s at the highest SM clock
-  a.poison_col = -1;
+  // the same wait bound and test hook as the allocating path: PDFS_WAIT_MS
+  // (default 4 s, counted at the highest SM clock) and PDFS_TEST_POISON_COLUMN
+  // (a column that never publishes, so that the bounded waits give up)
+  long long wait_ms = 4000;
+  if (const char *w = getenv("PDFS_WAIT_MS")) wait_ms = atoll(w);
+  a.wait_cycles = wait_ms * 1000000LL * 21 / 10;
+  a.poison_col = getenv("PDFS_TEST_POISON_COLUMN") ? atoi(getenv("PDFS_TEST_POISON_COLUMN")) : -1;
   const double h[3] = {g->dx, g->dy, g->dz};
   for (int i = 0; i < 3; ++i) {
     a.k64.h[i] = h[i];

@@ -622,6 +622,8 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if ((e = cudaEventCreate(&c->k1)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->q0)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&c->q1)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->r0)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreate(&c->r1)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamSynchronize(c->st)) != cudaSuccess) return fail(e);
   if (verbose(o)) {
     const auto t_end = std::chrono::steady_clock::now();
@@ -653,6 +655,8 @@ extern "C" void pdfs_ctx_destroy(pdfs_ctx *c) {
   if (c->k1) cudaEventDestroy(c->k1);
   if (c->q0) cudaEventDestroy(c->q0);
   if (c->q1) cudaEventDestroy(c->q1);
+  if (c->r0) cudaEventDestroy(c->r0);
+  if (c->r1) cudaEventDestroy(c->r1);
   for (cudaEvent_t ev : c->slab_ev)
     if (ev) cudaEventDestroy(ev);
   if (c->st2) cudaStreamDestroy(c->st2);
@@ -958,6 +962,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   if (!c || !c->loaded) return PDFS_ERR_INVALID;
   CK(cudaSetDevice(c->dev));
   const auto t0 = std::chrono::steady_clock::now();
+  CK(cudaEventRecord(c->r0, c->st));
   pdfs_stats st;
   std::memset(&st, 0, sizeof(st));
   st.tile = c->t32 | (c->t64 << 8);
@@ -1032,11 +1037,12 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e active=%lld/%lld\n", which, s, sn,
                 full ? "full" : "skip", chg, nact, c->nblocks);
       ++s;
+      const long long upd = full ? nodes : (long long)((double)nodes * (double)nact / (double)c->nblocks);
+      st.voxel_updates += upd;
+      if (which != 0) st.voxel_updates_fp64 += upd;
       if (full) {
         st.full_sweeps++;
-        st.voxel_updates += nodes;
       } else {
-        st.voxel_updates += (long long)((double)nodes * (double)nact / (double)c->nblocks);
         st.blocks_skipped += c->nblocks - nact;
       }
       if (o.fixed_sweeps == 0 && (full || !certify) && chg <= tol) break;
@@ -1070,6 +1076,8 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   if (!r) r = rc;
   st.status = r;
   st.launches = c->launches;
+  if (cudaEventRecord(c->r1, c->st) == cudaSuccess && cudaEventSynchronize(c->r1) == cudaSuccess)
+    st.ms_device = ms_between(c->r0, c->r1);
   st.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats) *stats = st;
   if (verbose(o))

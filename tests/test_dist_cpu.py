@@ -58,4 +58,11 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1  # rank 0 alone prints
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
-    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    # the reference's own build where it could be made (oracle/_ref), else the oracle port
+    have_ref = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libref_fsm_omp.so"))
+    assert d["cpu_baseline"]["kind"] == ("reference" if have_ref else "port")
+    assert d["e2e"]["h2d_bytes_per_step"] == 0
+    # the same metric, unit and direction as our arm's line, so the two can be compared
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT and d["higher_is_better"] is True
