@@ -182,10 +182,13 @@ COLUMNS64 = {1: (4, 1), 2: (4, 2), 3: (8, 2), 4: (6, 1)}
 BRICKS32 = {8: (16, 16), 9: (16, 32), 11: (8, 48)}
 BRICKS64 = {5: (16, 16), 7: (16, 32), 8: (8, 32)}
 PENCILS32, PENCILS64 = (10,), (6,)
+LANECOL32, LANECOL64 = {12: 8}, {9: 8}  # lane-column tiles: rows per tile
 
 
 def kernel_kind(kind, tile):
     t = tile & 0xff if kind == "fp32" else tile >> 8
+    if t in (LANECOL32 if kind == "fp32" else LANECOL64):
+        return "lanecol"
     if t in (BRICKS32 if kind == "fp32" else BRICKS64):
         return "brick"
     if t in (PENCILS32 if kind == "fp32" else PENCILS64):
@@ -207,6 +210,9 @@ def kernel_name(kind, tile, prec, arith):
         return "t3_sweep_kernel<%s, %d, %d, %s, %s>" % (t, by, bz, mode, ar)
     if k == "pencil":
         return "pc_sweep_kernel<%s, %s, %s>" % (t, mode, ar)
+    if k == "lanecol":
+        rows = (LANECOL32 if kind == "fp32" else LANECOL64)[tid]
+        return "lc_sweep_kernel<%s, %d, %s>" % (t, rows, mode)
     ty = (COLUMNS32 if kind == "fp32" else COLUMNS64).get(tid, (0, 0))
     return "ws_sweep_kernel<%s, %d, %d, %s, %s>" % ((t,) + ty + (mode, ar))
 

@@ -262,10 +262,10 @@ extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fi
     // a batched launch runs the column kernels (one ticket space across the
     // grids); brick tiles and the default choice map to the column defaults
     int t32 = o.tile & 0xff, t64 = (o.tile >> 8) & 0xff;
-    if (t32 == 0 || tile32(t32).bz) t32 = 4;
+    if (t32 == 0 || tile32(t32).bz || tile32(t32).lc) t32 = 4;
     // FP32 pairs live on bricks only: the batch polishes in the mixed arithmetic
     if (o.arith == PDFS_ARITH_PAIR) o.arith = PDFS_ARITH_MIXED;
-    if (t64 == 0 || tile64(t64).bz) t64 = o.arith == PDFS_ARITH_MIXED ? 4 : 1;
+    if (t64 == 0 || tile64(t64).bz || tile64(t64).lc) t64 = o.arith == PDFS_ARITH_MIXED ? 4 : 1;
     o.tile = t32 | (t64 << 8);
   }
   std::vector<pdfs_ctx *> ctx(n, nullptr);
@@ -410,6 +410,7 @@ extern "C" int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o_in, int *til
     for (int t = 1; t <= (o.precision == PDFS_PREC_FP32_POLISH64 ? 2 : 3); ++t) c64.push_back(t);
   if (o.arith == PDFS_ARITH_FAST) c64.push_back(4);
   for (int t : {5, 6, 7, 8}) c64.push_back(t);  // bricks and pencils: every arithmetic
+  if (o.arith == PDFS_ARITH_PAIR) c64.push_back(9);  // lane columns: FP32 pairs
   for (int t : c64) {
     double ms = 0;
     if (time_tile(PDFS_PREC_FP64, t, &ms) == PDFS_OK && ms < b) {

@@ -17,16 +17,29 @@ namespace pdfs {
 // xo is the x offset of the index: V - 1 for the column kernels (interior x =
 // 1 + tx*cx on a 16-byte boundary), 0 for bricks and pencils (their boxes
 // start at the halo node x0 - 1 = 16*cx, on a 16-byte boundary).
+// zc != 0: the z-column layout of the lane-column tiles (lanecol.cuh), node
+// (x, y, z) at (y * px + x) * qz + kLcZ0 + z with px = nx + 2 columns per row
+// of columns; traversal steps T, last traversal position q_last; ncx x ncy
+// tiles of tx = 31 lanes by ty rows.
 struct Layout {
   int tx = 0, ty = 0, V = 0, esize = 0, xo = 0;
   int ncx = 0, ncy = 0;
   long long px = 0, ry = 0, plane = 0;
   size_t elems = 0;  // total elements including padding
-  __host__ __device__ long long index(int x, int y, int z) const { return (long long)z * plane + (long long)y * px + x + xo; }
+  int zc = 0, q_last = 0, T = 0;
+  long long qz = 0;
+  __host__ __device__ long long index(int x, int y, int z) const {
+    return zc ? ((long long)y * px + x) * qz + kLcZ0 + z : (long long)z * plane + (long long)y * px + x + xo;
+  }
 };
 
 // xo < 0: the column kernels' offset V - 1
 Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize, int xo = -1);
+// The z-column layout of lane-column tiles of `rows` rows.
+Layout make_layout_zc(const pdfs_grid &g, int rows, int esize);
+// Ticket order of lane-column tiles: every tile after the tiles it waits on,
+// by expected start level.
+std::vector<int> lc_order(int ntx, int nty, int rows);
 
 // Frozen bitmask layout, independent of the tile: node (x, y, z) is bit
 // (x-1)%32 of word z*fplane + ((x-1)/32)*fy + (y-1).  The rows of one 32-wide
@@ -48,6 +61,7 @@ struct TileShape {
   int tx, ty, c;
   int bz = 0;
   int pencil = 0;
+  int lc = 0;  // lane-column tile (lanecol.cuh): its rows; the field is in the ZC layout
 };
 // Tile ids (1-based) for FP32 and FP64 kernels.
 int tile_count32();
@@ -69,6 +83,10 @@ cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, 
 cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
                                  cudaStream_t st, int *grid_used);
 cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty);
+// One sweep by the lane-column kernel (lanecol.cu): which 0 = FP32 min, 1 =
+// pair min, 2 = pair replace.
+cudaError_t launch_sweep_lanecol(int which, bool iso, const LcArgs &a, int sms, cudaStream_t st,
+                                 int *grid_used);
 // Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
 std::vector<int> brick_order(int ntx, int nty, int ntz);
 cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by,
@@ -148,6 +166,9 @@ struct pdfs_ctx {
   int epoch = 0;  // flag value of the last brick or pencil sweep
   unsigned long long *pmail = nullptr;  // pencils: epoch-tagged face mailboxes
   int prow = 0;                          // their diagonals per face
+  // lane-column tiles: ticket orders, and the epoch-tagged face mailboxes
+  int *lcord32 = nullptr, *lcord64 = nullptr;
+  unsigned long long *lc_ymail = nullptr, *lc_xmail = nullptr;
   void *mailbox = nullptr;  // x- and y-face mailboxes of every column
   size_t mailbox_bytes = 0;
   size_t progress_ints = 0;

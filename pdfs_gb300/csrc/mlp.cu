@@ -161,7 +161,7 @@ __global__ void k_block_min(const T *__restrict__ u, Layout L, int nx, int ny, i
           f = p_hi(v);
         else
           f = (float)v;
-        m = fminf(m, f);
+        m = fminf(m, fabsf(f));  // z-column fields mark frozen nodes with the sign
       }
   }
 #pragma unroll

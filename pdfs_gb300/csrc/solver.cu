@@ -38,6 +38,53 @@ Layout make_layout(const pdfs_grid &g, int tx, int ty, int esize, int xo) {
   return L;
 }
 
+Layout make_layout_zc(const pdfs_grid &g, int rows, int esize) {
+  Layout L;
+  L.zc = 1;
+  L.tx = kLcLanes;
+  L.ty = rows;
+  L.esize = esize;
+  L.V = 16 / esize;
+  L.ncx = (g.nx + 1 + kLcLanes - 1) / kLcLanes;  // lanes 0..30 of the last tile reach lx = nx - 1
+  L.ncy = (g.ny + 30) / rows + 1;                // lane 30 of the last tile row reaches ly = ny - 1
+  L.px = g.nx + 2;
+  L.ry = g.ny + 2;
+  // the traversal runs over z = 0 .. 8 ceil(nz/8) + 7 (going down it passes
+  // every block's top boundary z == 0 mod 8); q_last == 7 (mod 8), T == 0 (mod 8)
+  L.q_last = kLcZ0 + 8 * ((g.nz + 7) / 8) + 7;
+  L.T = L.q_last - kLcZ0 + 1;
+  L.qz = L.q_last + 17;  // room for the look-ahead of the rows past the last step
+  L.plane = 0;
+  L.elems = (size_t)L.ry * (size_t)L.px * (size_t)L.qz;
+  return L;
+}
+
+// Expected start level of each tile: it trails the tile above by R + c
+// levels (its row 0 needs that tile's row R-1 at the same position) and the
+// tiles to the left by the offset of the rows it reads from them plus c
+// (c: a few levels of hand-off latency).  Every wait then points to a
+// strictly earlier start, so sorting by start lists each tile after the
+// tiles it waits on: the tickets are deadlock-free.
+std::vector<int> lc_order(int ntx, int nty, int rows) {
+  const int c = 4;
+  std::vector<long long> start((size_t)ntx * nty, 0);
+  for (int tx = 0; tx < ntx; ++tx)
+    for (int ty = 0; ty < nty; ++ty) {
+      long long st = 0;
+      if (ty > 0) st = std::max(st, start[(size_t)(ty - 1) * ntx + tx] + rows + c);
+      if (tx > 0)
+        for (int r = 0; r < rows; ++r) {
+          const int k = rows * ty + r + 30, ty2 = k / rows, r2 = k % rows;  // lane 30, row r2 of tile (tx-1, ty2)
+          if (ty2 < nty) st = std::max(st, start[(size_t)ty2 * ntx + tx - 1] + std::max(1, r2 - r + c));
+        }
+      start[(size_t)ty * ntx + tx] = st;
+    }
+  std::vector<int> o((size_t)ntx * nty);
+  for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
+  std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return start[a] < start[b]; });
+  return o;
+}
+
 MaskLayout make_mask_layout(const pdfs_grid &g) {
   MaskLayout M;
   M.fy = ((long long)g.ny + 32 + 3) / 4 * 4;
@@ -58,8 +105,7 @@ template <class T>
 __global__ void k_pack(const double *__restrict__ ref, T *__restrict__ dst, int nx, int ny, Layout L, int z0) {
   const int y = blockIdx.x, z = blockIdx.y + z0;
   const double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
-  T *out = dst + L.index(0, y, z);
-  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) out[x] = (T)row[x];
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) dst[L.index(x, y, z)] = (T)row[x];
 }
 
 // internal layout -> reference layout (double).  FP32 source: frozen nodes
@@ -70,9 +116,8 @@ __global__ void k_unpack(const T *__restrict__ src, Layout L, const double *__re
                          int z0) {
   const int y = blockIdx.x, z = blockIdx.y + z0;
   double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
-  const T *s = src + L.index(0, y, z);
   for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
-    double v = (double)s[x];
+    double v = fabs((double)src[L.index(x, y, z)]);  // ZC fields mark frozen nodes with the sign
     if (fmask && x >= 1 && x <= nx && y >= 1 && y <= ny) {
       const uint32_t w = fmask[M.word(x, y, z)];
       if ((w >> ((x - 1) & 31)) & 1u) v = in64[L64.index(x, y, z)];
@@ -85,9 +130,45 @@ __global__ void k_unpack(const T *__restrict__ src, Layout L, const double *__re
 template <class S, class D>
 __global__ void k_convert(const S *__restrict__ src, Layout Ls, D *__restrict__ dst, Layout Ld, int nx) {
   const int y = blockIdx.x, z = blockIdx.y;
-  const S *s = src + Ls.index(0, y, z);
-  D *d = dst + Ld.index(0, y, z);
-  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) d[x] = (D)s[x];
+  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) dst[Ld.index(x, y, z)] = (D)src[Ls.index(x, y, z)];
+}
+
+// Every element of a z-column (ZC) working field, in column order: the
+// input's value (FP32, or its nearest pair) -- or, with from32, the FP32
+// field's value as a pair -- with the sign bit set on the nodes the sweeps
+// must not change (frozen nodes and the halo: their exact input, as a pair
+// for pairs), and -inf in the padding at both ends of each column.
+template <class T>
+__global__ void k_zc_fill(T *__restrict__ dst, Layout Ld, const double *__restrict__ in64, Layout L64,
+                          const float *__restrict__ u32, Layout L32, bool from32, const uint32_t *__restrict__ fmask,
+                          MaskLayout M, int nx, int ny, int nz) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < Ld.elems; i += (size_t)gridDim.x * blockDim.x) {
+    const long long col = (long long)(i / (size_t)Ld.qz);
+    const int z = (int)(i - (size_t)col * (size_t)Ld.qz) - kLcZ0;
+    const int y = (int)(col / Ld.px), x = (int)(col - (long long)y * Ld.px);
+    if (z < 0 || z > nz + 1) {
+      if constexpr (sizeof(T) == 4)
+        dst[i] = -INFINITY;
+      else
+        dst[i] = p_make(-INFINITY, 0.0f);
+      continue;
+    }
+    bool frz = x < 1 || x > nx || y < 1 || y > ny || z < 1 || z > nz;
+    if (!frz && fmask) frz = (fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u;
+    if constexpr (sizeof(T) == 4) {
+      const float v = (float)in64[L64.index(x, y, z)];
+      dst[i] = frz ? -fabsf(v) : v;
+    } else {
+      double pv;
+      if (frz || !from32) {
+        pv = p_from_double(in64[L64.index(x, y, z)]);
+      } else {
+        pv = p_make(fabsf(u32[L32.index(x, y, z)]), 0.0f);
+      }
+      if (frz) pv = __longlong_as_double(__double_as_longlong(pv) | 0x80000000LL);  // hi's sign bit
+      dst[i] = pv;
+    }
+  }
 }
 
 // FP32 working field -> FP64 working field (polish start): frozen nodes and
@@ -430,8 +511,9 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4);
   // bricks (5: 16 x 16 x 16, 7: 16 x 16 x 32) and pencils (6) for every
   // arithmetic; FP32 pairs on bricks and pencils only
+  if (t64 == 9 && o->arith != PDFS_ARITH_PAIR) return PDFS_ERR_INVALID;  // lane columns: FP32 pairs only
   if (o->arith == PDFS_ARITH_PAIR) {
-    if (t64 != 0 && t64 < 5) return PDFS_ERR_INVALID;  // FP32 pairs: bricks and pencils
+    if (t64 != 0 && t64 < 5) return PDFS_ERR_INVALID;  // FP32 pairs: bricks, pencils and lane columns
   } else if (o->arith == PDFS_ARITH_MIXED) {
     if (t64 == 2 || t64 == 3) return PDFS_ERR_INVALID;
   } else {
@@ -452,8 +534,8 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
 // columns (the reference arithmetic is even: both are FP64-pipe-bound).
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
-  c->t32 = t32 ? t32 : 10;
-  c->t64 = t64 ? t64 : 6;
+  c->t32 = t32 ? t32 : 12;
+  c->t64 = t64 ? t64 : (c->o.arith == PDFS_ARITH_PAIR ? 9 : 6);
 }
 
 extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_ctx **out) {
@@ -480,9 +562,10 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   c->dev = o.device;
   pick_tiles(c);
   const TileShape s32 = tile32(c->t32), s64 = tile64(c->t64);
-  // bricks and pencils (c == 0) index from the halo node; columns from the interior
-  c->L32 = make_layout(*g, s32.tx, s32.ty, 4, s32.c == 0 ? 0 : -1);
-  c->L64 = make_layout(*g, s64.tx, s64.ty, 8, s64.c == 0 ? 0 : -1);
+  // bricks and pencils (c == 0) index from the halo node; columns from the
+  // interior; lane-column tiles use the z-column layout
+  c->L32 = s32.lc ? make_layout_zc(*g, s32.lc, 4) : make_layout(*g, s32.tx, s32.ty, 4, s32.c == 0 ? 0 : -1);
+  c->L64 = s64.lc ? make_layout_zc(*g, s64.lc, 8) : make_layout(*g, s64.tx, s64.ty, 8, s64.c == 0 ? 0 : -1);
   c->M = make_mask_layout(*g);
   int rc = PDFS_OK;
   auto fail = [&](cudaError_t e) {
@@ -532,7 +615,22 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   mark("brick orders");
   const std::vector<int> w32 = wavefront_order(c->L32.ncx, c->L32.ncy, c->L32.tx, c->L32.ty),
                          w64 = wavefront_order(c->L64.ncx, c->L64.ncy, c->L64.tx, c->L64.ty);
+  std::vector<int> lo32, lo64;
+  if (s32.lc) lo32 = lc_order(c->L32.ncx, c->L32.ncy, s32.lc);
+  if (s64.lc) lo64 = lc_order(c->L64.ncx, c->L64.ncy, s64.lc);
   mark("columns");
+  // lane-column tiles: per tile, row R-1's face for every traversal step (32
+  // lanes); per tile column, lane 30's face by (ly + 32, step); FP32 values
+  // take one tagged word, pairs two
+  size_t lc_y = 0, lc_x = 0;
+  for (int k = 0; k < 2; ++k) {
+    const TileShape ts = k ? s64 : s32;
+    if (!ts.lc) continue;
+    const Layout &L = k ? c->L64 : c->L32;
+    const size_t wv = k ? 2 : 1;
+    lc_y = std::max(lc_y, (size_t)L.ncx * L.ncy * (size_t)L.T * 32 * wv);
+    lc_x = std::max(lc_x, (size_t)L.ncx * (size_t)(ts.lc * L.ncy + 2) * (size_t)L.T * wv);
+  }
   // per-row progress words and face mailboxes, sized for the larger of the two layouts
   {
     const int nb = mailbox_chunks(g->nz) * kMailboxChunk;
@@ -582,6 +680,10 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   want(&c->pmail, pmail_words * 8);
   want(&c->order32, w32.size() * 4);
   want(&c->order64, w64.size() * 4);
+  want(&c->lcord32, lo32.size() * 4);
+  want(&c->lcord64, lo64.size() * 4);
+  want(&c->lc_ymail, lc_y * 8);
+  want(&c->lc_xmail, lc_x * 8);
   {
     size_t total = 0;
     for (auto &r : plan) total += (r.second + 255) & ~(size_t)255;  // 256-byte aligned pieces
@@ -606,6 +708,15 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   }
   if (nflags && (e = cudaMemsetAsync(c->tflag, 0, nflags * 4, c->st)) != cudaSuccess) return fail(e);
   if (pmail_words && (e = cudaMemsetAsync(c->pmail, 0, pmail_words * 8, c->st)) != cudaSuccess) return fail(e);
+  // lane-column mailboxes: tag 0 never matches (epochs start at 1)
+  if (lc_y && (e = cudaMemsetAsync(c->lc_ymail, 0, lc_y * 8, c->st)) != cudaSuccess) return fail(e);
+  if (lc_x && (e = cudaMemsetAsync(c->lc_xmail, 0, lc_x * 8, c->st)) != cudaSuccess) return fail(e);
+  for (int k = 0; k < 2; ++k) {
+    const std::vector<int> &lo = k ? lo64 : lo32;
+    int *dst = k ? c->lcord64 : c->lcord32;
+    if (!lo.empty() && (e = cudaMemcpyAsync(dst, lo.data(), lo.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
+      return fail(e);
+  }
   if ((e = cudaMemcpyAsync(c->order32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
     return fail(e);
   if ((e = cudaMemcpyAsync(c->order64, w64.data(), w64.size() * 4, cudaMemcpyHostToDevice, c->st)) != cudaSuccess)
@@ -864,6 +975,46 @@ int pdfs::ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, 
   return run_sweep(c, which, sn, active, blk_chg, chg);
 }
 
+// The lane-column kernel's arguments from the sweep arguments a of context c.
+static void fill_lc_args(const pdfs_ctx *c, int which, const SweepArgs &a, LcArgs *out) {
+  const bool f32 = which == 0;
+  const Layout &L = f32 ? c->L32 : c->L64;
+  LcArgs &l = *out;
+  std::memset(&l, 0, sizeof(l));
+  l.u = a.u;
+  l.cap = which == 2 ? c->in64 : nullptr;
+  l.bcap32 = which == 2 ? c->bcap32 : nullptr;
+  l.cxp = L.px;
+  l.qz = L.qz;
+  l.q_last = L.q_last;
+  l.T = L.T;
+  l.nx = a.nx;
+  l.ny = a.ny;
+  l.nz = a.nz;
+  l.sx = a.sx;
+  l.sy = a.sy;
+  l.sz = a.sz;
+  l.ntx = L.ncx;
+  l.nty = L.ncy;
+  l.order = f32 ? c->lcord32 : c->lcord64;
+  l.ticket = a.ticket;
+  l.err = a.err;
+  l.maxchg = a.maxchg;
+  l.hmin = a.hmin;
+  l.ymail = c->lc_ymail;
+  l.xmail = c->lc_xmail;
+  l.xrows = L.ty * L.ncy + 2;
+  l.epoch = a.epoch;
+  l.wait_cycles = a.wait_cycles;
+  l.poison_tile = a.poison_col;
+  l.blk_active = a.blk_active;
+  l.blk_chg = a.blk_chg;
+  l.nbx = a.nbx;
+  l.nby = a.nby;
+  l.nbz = a.nbz;
+  l.k32 = a.k32;
+}
+
 static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
@@ -874,6 +1025,41 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
 
   const int tile = f32 ? c->t32 : c->t64;
   const TileShape ts = f32 ? tile32(tile) : tile64(tile);
+  if (ts.lc) {
+    // lane-column tiles: every sweep, with or without a block mask
+    CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
+    if (blk_chg) CK(cudaMemsetAsync(blk_chg, 0, (size_t)c->nblocks * 4, c->st));
+    CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
+    a.epoch = ++c->epoch;  // mailbox words of every earlier sweep carry a smaller tag
+    LcArgs l;
+    fill_lc_args(c, which, a, &l);
+    int grid = 0;
+    CK(cudaEventRecord(c->k0, c->st));
+    CK(launch_sweep_lanecol(f32 ? 0 : (which == 2 ? 2 : 1), iso, l, c->sms, c->st, &grid));
+    CK(cudaEventRecord(c->k1, c->st));
+    CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->kern_ms += ms_between(c->k0, c->k1);
+    c->launches++;
+    if (c->hstat->err[0]) {
+      if (verbose(c->o))
+        fprintf(stderr, "pdfs: sweep sn=%d device error %d (tile %d)\n", sn, c->hstat->err[0], c->hstat->err[2]);
+      return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
+    }
+    if (chg) {
+      if (f32) {
+        unsigned int b = (unsigned int)c->hstat->chg;
+        float f;
+        std::memcpy(&f, &b, 4);
+        *chg = f;
+      } else {
+        double d;
+        std::memcpy(&d, &c->hstat->chg, 8);
+        *chg = d;
+      }
+    }
+    return PDFS_OK;
+  }
   // pencils sweep unmasked sweeps; a block mask or block-change output goes to bricks
   const bool pencil = ts.pencil && !active && !blk_chg;
   if (ts.bz == 0 || pencil) CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
@@ -921,7 +1107,20 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
   return PDFS_OK;
 }
 
+// A z-column working field from the input (FP32, or pairs) or, for pairs
+// with from32, from the FP32 field: frozen nodes and the halo signed.
+template <class T>
+static int zc_fill(pdfs_ctx *c, T *dst, const Layout &Ld, bool from32) {
+  const pdfs_grid &g = c->g;
+  k_zc_fill<T><<<8 * c->sms, 256, 0, c->st>>>(dst, Ld, c->in64, c->L64, c->u32, c->L32, from32,
+                                              c->has_mask ? c->fmask : nullptr, c->M, g.nx, g.ny, g.nz);
+  c->launches++;
+  CK(cudaGetLastError());
+  return PDFS_OK;
+}
+
 int pdfs::ctx_fp64_start(pdfs_ctx *c) {  // FP64 working field <- the input
+  if (c->L64.zc) return zc_fill<double>(c, c->u64, c->L64, false);
   if (c->o.arith == PDFS_ARITH_PAIR) {
     k_to_pair<<<4 * c->sms, 256, 0, c->st>>>(c->in64, c->u64, c->L64.elems);
     c->launches++;
@@ -934,6 +1133,7 @@ int pdfs::ctx_fp64_start(pdfs_ctx *c) {  // FP64 working field <- the input
 
 int pdfs::ctx_widen(pdfs_ctx *c) {
   const pdfs_grid &g = c->g;
+  if (c->L64.zc) return zc_fill<double>(c, c->u64, c->L64, true);
   dim3 grid(g.ny + 2, g.nz + 2);
   if (c->o.arith == PDFS_ARITH_PAIR) {
     k_widen_pair<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64,
@@ -951,6 +1151,7 @@ int pdfs::ctx_widen(pdfs_ctx *c) {
 
 int pdfs::ctx_narrow(pdfs_ctx *c) {  // FP64 input -> FP32 working field
   const pdfs_grid &g = c->g;
+  if (c->L32.zc) return zc_fill<float>(c, c->u32, c->L32, false);
   dim3 grid(g.ny + 2, g.nz + 2);
   k_convert<double, float><<<grid, 128, 0, c->st>>>(c->in64, c->L64, c->u32, c->L32, g.nx);
   c->launches++;

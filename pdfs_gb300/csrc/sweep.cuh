@@ -52,6 +52,12 @@
 namespace pdfs {
 
 enum { MODE_MIN = 0, MODE_REPLACE = 1 };
+
+// Lane-column tiles (lanecol.cuh) and their z-column ("ZC") field layout.
+constexpr int kLcZ0 = 16;     // column position of the halo plane z = 0
+constexpr int kLcLanes = 31;  // computing lanes of a tile
+constexpr int kLcRows32 = 8;  // rows of an FP32 tile
+constexpr int kLcRows64 = 8;  // rows of an FP32-pair tile
 enum { ARITH_REF = 0, ARITH_FAST = 1, ARITH_MIXED = 2, ARITH_PAIR = 3 };
 enum { DEV_ERR_TIMEOUT = 1, DEV_ERR_SMEM_ALIGN = 2 };
 
@@ -98,6 +104,35 @@ struct SweepArgs {
   // value below it is below every cap of the block, so the cap is not read.
   const double *bcap64;
   const float *bcap32;
+};
+
+// Arguments of the lane-column sweep (lanecol.cuh).
+struct LcArgs {
+  void *u;               // working field (ZC layout): FP32, or FP32 pairs in 64-bit slots
+  const double *cap;     // replace-update: the FP64 input in the same ZC layout
+  const float *bcap32;   // replace-update: per 8^3 block, the smallest cap rounded down
+  long long cxp;         // columns per row of columns (nx + 2)
+  long long qz;          // elements per column
+  int q_last;            // position of the last traversal step in +z order (== 7 mod 8)
+  int T;                 // traversal steps per column (== 0 mod 8)
+  int nx, ny, nz;
+  int sx, sy, sz;        // +1 / -1 sweep direction per axis
+  int ntx, nty;          // tiles
+  const int *order;      // ticket -> tile id (ty * ntx + tx), every tile after the tiles it waits on
+  int *ticket;
+  int *err;              // [0] error code, [1] abort flag, [2] tile that timed out
+  void *maxchg;          // FP32: uint bits of the max relative change; pairs: u64 bits of the max change
+  float hmin;
+  unsigned long long *ymail;  // [tile][T][32][words]: row R-1 of each tile
+  unsigned long long *xmail;  // [tx][xrows][T][words]: lane 30 of each tile, by ly + 32
+  int xrows;
+  int epoch;
+  long long wait_cycles;
+  int poison_tile;       // test hook: this tile never publishes (-1 = off)
+  const uint8_t *blk_active;  // per 8^3 block: update its nodes?  (nullptr = all)
+  unsigned int *blk_chg;      // per 8^3 block: float bits of this sweep's max change (nullptr = off)
+  int nbx, nby, nbz;
+  GodConst32 k32;
 };
 
 // A batched sweep: tickets enumerate (grid, local column) pairs, each grid's

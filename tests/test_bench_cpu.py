@@ -23,13 +23,16 @@ def bench():
 
 
 def tile_table(name):
-    """Entries {tx, ty, c[, bz[, pencil]]} of kT32 / kT64 in sweep.cu."""
+    """Entries {tx, ty, c[, bz[, pencil[, lc]]]} of kT32 / kT64 in sweep.cu
+    (named row counts from sweep.cuh)."""
     src = open(os.path.join(ROOT, "pdfs_gb300", "csrc", "sweep.cu")).read()
+    hdr = open(os.path.join(ROOT, "pdfs_gb300", "csrc", "sweep.cuh")).read()
+    consts = {m.group(1): int(m.group(2)) for m in re.finditer(r"constexpr int (kLc\w+) = (\d+);", hdr)}
     body = re.search(r"static const TileShape %s\[\] = \{(.*?)\};" % name, src, re.S).group(1)
     out = []
     for m in re.finditer(r"\{([^{}]*)\}", body):
-        v = [int(x) for x in m.group(1).split(",")]
-        v += [0] * (5 - len(v))
+        v = [consts[x.strip()] if x.strip() in consts else int(x) for x in m.group(1).split(",")]
+        v += [0] * (6 - len(v))
         out.append(tuple(v))
     return out
 
@@ -38,7 +41,8 @@ def default_tiles():
     """The default tile ids (pick_tiles in solver.cu)."""
     src = open(os.path.join(ROOT, "pdfs_gb300", "csrc", "solver.cu")).read()
     t32 = int(re.search(r"c->t32 = t32 \? t32 : (\d+);", src).group(1))
-    t64 = int(re.search(r"c->t64 = t64 \? t64 : (\d+);", src).group(1))
+    # the FP64 default for the pair arithmetic (the headline polish)
+    t64 = int(re.search(r"c->t64 = t64 \? t64 : \(c->o.arith == PDFS_ARITH_PAIR \? (\d+) : \d+\);", src).group(1))
     return t32, t64
 
 
@@ -48,16 +52,19 @@ def test_bench_kernel_tables_match_library(bench, kind):
     cols = bench.COLUMNS32 if kind == "fp32" else bench.COLUMNS64
     bricks = bench.BRICKS32 if kind == "fp32" else bench.BRICKS64
     pencils = bench.PENCILS32 if kind == "fp32" else bench.PENCILS64
-    for tid, (tx, ty, c, bz, pencil) in enumerate(table, start=1):
+    lanecols = bench.LANECOL32 if kind == "fp32" else bench.LANECOL64
+    for tid, (tx, ty, c, bz, pencil, lc) in enumerate(table, start=1):
         tile = tid if kind == "fp32" else tid << 8
         k = bench.kernel_kind(kind, tile)
-        if pencil:
+        if lc:
+            assert k == "lanecol" and lanecols[tid] == lc
+        elif pencil:
             assert k == "pencil" and tid in pencils
         elif bz:
             assert k == "brick" and bricks[tid] == (ty, bz)
         else:
             assert k == "column" and cols[tid] == (ty, c)
-    assert set(cols) | set(bricks) | set(pencils) == set(range(1, len(table) + 1))
+    assert set(cols) | set(bricks) | set(pencils) | set(lanecols) == set(range(1, len(table) + 1))
 
 
 def test_default_kernels_have_profiles_and_traffic(bench):
@@ -65,8 +72,8 @@ def test_default_kernels_have_profiles_and_traffic(bench):
     tile = t32 | (t64 << 8)
     n32 = bench.kernel_name("fp32", tile, L.PREC_FP32_POLISH64, L.ARITH_PAIR)
     n64 = bench.kernel_name("fp64", tile, L.PREC_FP32_POLISH64, L.ARITH_PAIR)
-    assert n32 == "pc_sweep_kernel<float, MIN, FAST>"
-    assert n64 == "pc_sweep_kernel<double, REPLACE, PAIR>"
+    assert n32 == "lc_sweep_kernel<float, 8, MIN>"
+    assert n64 == "lc_sweep_kernel<double, 8, REPLACE>"
     traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     for kind, name in (("fp32", n32), ("fp64", n64)):
         t = bench.traffic_per_launch(kind, L.PREC_FP32_POLISH64, 1000, tile)

@@ -3,7 +3,8 @@ the device allocator while they run (code confined to a pool handed over by
 a host application, real-time loops that must not call cudaMalloc, plugins
 whose host forbids allocation after set-up).  Checked through the C ABI
 against the allocating entry point pdfs_sweep and the oracle on two calls in
-a row (bit-exact: both run the reference's FP64 arithmetic), with the
+a row (bit-exact: both run the reference's FP64 arithmetic; against the
+oracle every NaN counts as one value, see same()), with the
 device's free memory unchanged across the second call; against the bounded
 wait's timeout path; and across a cudaDeviceReset in a child process.
 
@@ -55,6 +56,16 @@ def case():
     return W.random_spheres(71, 45, 33, 0.7, 1.0, 0.5, 6, 2.0, 9.0, seed=17)
 
 
+def same(a, b):
+    """Bit-exact, with every NaN counted as one value.  On this anisotropic
+    grid the reference's own arithmetic (phi3D_fsm.c:167-177, the expanded
+    quadratic) turns far nodes (1e10) into NaN, and the GPU and the host CPU
+    give NaN different sign bits; the oracle reproduces the reference's NaNs
+    where they arise."""
+    na, nb = np.isnan(a), np.isnan(b)
+    return bool(np.array_equal(na, nb) and a[~na].tobytes() == b[~nb].tobytes())
+
+
 def test_static_sweep_matches_allocating_sweep_twice():
     torch = pytest.importorskip("torch")
     w = case()
@@ -79,7 +90,7 @@ def test_static_sweep_matches_allocating_sweep_twice():
         got = from_internal(dev.cpu().numpy(), w.field.shape, px, ry)
         # tolerance: the same FP64 reference arithmetic as pdfs_sweep and the oracle, so bit-exact
         assert got.tobytes() == expect.tobytes(), f"ordering {sn} vs pdfs_sweep"
-        assert got.tobytes() == orc.tobytes(), f"ordering {sn} vs the oracle"
+        assert same(got, orc), f"ordering {sn} vs the oracle"
         assert ch.value == ch_ref
 
 
@@ -115,7 +126,7 @@ def test_static_sweep_timeout_then_clean_call(monkeypatch):
     torch.cuda.synchronize()
     expect = w.field.copy()
     O.sweep(expect, sp, 1)
-    assert from_internal(dev.cpu().numpy(), w.field.shape, px, ry).tobytes() == expect.tobytes()
+    assert same(from_internal(dev.cpu().numpy(), w.field.shape, px, ry), expect)
 
 
 def _reset_check() -> None:
@@ -141,7 +152,7 @@ def _reset_check() -> None:
         assert rt.cudaMemcpy(out.ctypes.data_as(C.c_void_p), p, C.c_size_t(host.nbytes), 2) == 0
         assert rt.cudaFree(p) == 0
         O.sweep(expect, sp, sn)
-        assert from_internal(out, w.field.shape, px, ry).tobytes() == expect.tobytes(), f"call {k + 1}"
+        assert same(from_internal(out, w.field.shape, px, ry), expect), f"call {k + 1}"
         host = out
     print("reset check ok")
 
