@@ -182,27 +182,26 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
     // kLcZ0 + t going up, q_last - t going down (memory order reversed)
     const int qv0 = SZ > 0 ? kLcZ0 : a.q_last - (VW - 1);  // column position of vector 0
     auto vaddr = [&](int r, int v) -> T * { return ubase + (r * ys32 + qv0 + SZ * VW * v); };
-    T wa[NR][VW], wb[NR][VW];  // vector sets: even vectors in wa, odd ones in wb
-    T res[R];                  // each row's new value of the previous level (its z-upwind value)
-    unsigned chg = 0;          // bit r: row r changed a node of its current vector
+    // Each row's window: cur = the vector of its position t, nxt = the next
+    // one (in flight until the row reaches the last element of cur).  A row
+    // entering a vector moves nxt into cur and loads the vector after it.
+    T cur[NR][VW], nxt[NR][VW];
+    T res[R];          // each row's new value of the previous level (its z-upwind value)
+    unsigned chg = 0;  // bit r: row r changed a node of its current vector
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
 #pragma unroll
-      for (int e = 0; e < VW; ++e) wa[r][e] = wb[r][e] = V::ninf();
+      for (int e = 0; e < VW; ++e) cur[r][e] = nxt[r][e] = V::ninf();
       const int v0 = -((r + VW - 1) / VW);  // vector of position t = -r (row r at level 0)
       if ((rowok >> r) & 1) {
-        if ((v0 & 1) == 0) {
-          lc_ld(wa[r], vaddr(r, v0));
-          lc_ld(wb[r], vaddr(r, v0 + 1));
+        if (((-r) & (VW - 1)) == 0) {
+          lc_ld(nxt[r], vaddr(r, v0));  // level 0 moves it into cur
         } else {
-          lc_ld(wb[r], vaddr(r, v0));
-          lc_ld(wa[r], vaddr(r, v0 + 1));
+          lc_ld(cur[r], vaddr(r, v0));
+          lc_ld(nxt[r], vaddr(r, v0 + 1));
         }
       }
     }
-#pragma unroll
-    for (int r = 0; r < R; ++r) res[r] = V::ninf();
-
     // ---- 8^3 block bookkeeping: the row's current block (-1 outside the interior) ----
     int bxy[R], bcur[R];
     float bch[R], bnd[R];
@@ -246,11 +245,11 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
     fetch(0, 0);
     fetch(1, 1);
 
-    const int M = (T_ + R - 1 + 7) / 8;  // row R-1 reaches the last position T-1 at level T + R - 2
+    const int M = (T_ + R - 1 + VW - 1) / VW;  // row R-1 reaches the last position T-1 at level T + R - 2
     for (int m = 0; m < M; ++m) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int g = 8 * m + j;
+      for (int j = 0; j < VW; ++j) {
+        const int g = VW * m + j;
         const int sl = j & 1;
         // -------- 1. the upwind faces of this level (prefetched two levels ago) --------
         if (!__all_sync(FULL, tags_ok(sl))) {
@@ -287,17 +286,14 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
         const T xv = V::from((unsigned)px0[sl], (unsigned)px1[sl]);
         fetch(g + 2, sl);
 
-        // -------- 2. a row entering a vector loads the one after it --------
+        // -------- 2. a row entering a vector takes the next one and loads the one after --------
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
           if (((j - r) & (VW - 1)) == 0) {
             const int c = (j - r + 16) / VW - 16 / VW;  // floor((j - r) / VW)
-            if ((rowok >> r) & 1) {
-              if (((c + 1) & 1) == 0)
-                lc_ld(wa[r], vaddr(r, (8 / VW) * m + c + 1));
-              else
-                lc_ld(wb[r], vaddr(r, (8 / VW) * m + c + 1));
-            }
+#pragma unroll
+            for (int e = 0; e < VW; ++e) cur[r][e] = nxt[r][e];
+            if ((rowok >> r) & 1) lc_ld(nxt[r], vaddr(r, m + c + 1));
           }
         }
 
@@ -305,22 +301,17 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
 #pragma unroll
         for (int r = R - 1; r >= 0; --r) {
           const int p = (j - r) & (VW - 1);           // t mod VW
-          const int c = (j - r + 16) / VW - 16 / VW;  // vector of t, relative to (8/VW) m
+          const int c = (j - r + 16) / VW - 16 / VW;  // vector of t, relative to m
           const int e = SZ > 0 ? p : VW - 1 - p;      // element of t
           const int pn = (p + 1) & (VW - 1);
           const int en = SZ > 0 ? pn : VW - 1 - pn;   // element of t + 1
-          T(&cur)[VW] = (c & 1) ? wb[r] : wa[r];
-          T(&nxt)[VW] = (c & 1) ? wa[r] : wb[r];
           // row r+1 sits one position behind: its next position is our t
           const int p1 = (j - r - 1) & (VW - 1);
-          const int c1 = (j - r - 1 + 16) / VW - 16 / VW;
           const int pn1 = (p1 + 1) & (VW - 1);
           const int en1 = SZ > 0 ? pn1 : VW - 1 - pn1;
-          T(&cur1)[VW] = (c1 & 1) ? wb[r + 1] : wa[r + 1];
-          T(&nxt1)[VW] = (c1 & 1) ? wa[r + 1] : wb[r + 1];
-          const T cv = cur[e];
-          const T zdn = p < VW - 1 ? cur[en] : nxt[en];
-          const T dn = p1 < VW - 1 ? cur1[en1] : nxt1[en1];
+          const T cv = cur[r][e];
+          const T zdn = p < VW - 1 ? cur[r][en] : nxt[r][en];
+          const T dn = p1 < VW - 1 ? cur[r + 1][en1] : nxt[r + 1][en1];
           const T up = r == 0 ? yv : res[r - 1];
           T xup = __shfl_up_sync(FULL, up, 1);
           const T xl = __shfl_sync(FULL, xv, r);
@@ -334,8 +325,7 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
           if constexpr (BLK || MODE == MODE_REPLACE) {
             // entering an 8^3 block: z == 1 (mod 8) going up, z == 0 (mod 8)
             // going down (the column's padding puts z = 8 ceil(nz/8) on the path)
-            const bool boundary = SZ > 0 ? (((j - r) & 7) == 1) : (((j - r) & 7) == 7);
-            if (boundary) {
+            if (((t - (SZ > 0 ? 1 : 7)) & 7) == 0) {
               const int z = SZ > 0 ? t : a.q_last - kLcZ0 - t;
               const int bz = (z - 1) >> 3;
               const int nb = (bz >= 0 && bz < a.nbz && bxy[r] >= 0) ? bz * a.nby * a.nbx + bxy[r] : -1;
@@ -387,11 +377,11 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
             chg |= 1u << r;
             if constexpr (BLK) bch[r] = fmaxf(bch[r], change_f<T, ARITH>(d));
           }
-          cur[e] = nv;
+          cur[r][e] = nv;
           res[r] = nv;
           // leaving the vector: write it back if one of its nodes changed
           if (p == VW - 1) {
-            if (((chg >> r) & 1) && lane < kLcLanes) lc_st(vaddr(r, (8 / VW) * m + c), cur);
+            if (((chg >> r) & 1) && lane < kLcLanes) lc_st(vaddr(r, m + c), cur[r]);
             chg &= ~(1u << r);
           }
         }

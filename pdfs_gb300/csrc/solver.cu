@@ -53,7 +53,7 @@ Layout make_layout_zc(const pdfs_grid &g, int rows, int esize) {
   // every block's top boundary z == 0 mod 8); q_last == 7 (mod 8), T == 0 (mod 8)
   L.q_last = kLcZ0 + 8 * ((g.nz + 7) / 8) + 7;
   L.T = L.q_last - kLcZ0 + 1;
-  L.qz = L.q_last + 17;  // room for the look-ahead of the rows past the last step
+  L.qz = L.q_last + 25;  // room for the look-ahead of the rows past the last step
   L.plane = 0;
   L.elems = (size_t)L.ry * (size_t)L.px * (size_t)L.qz;
   return L;
@@ -117,7 +117,8 @@ __global__ void k_unpack(const T *__restrict__ src, Layout L, const double *__re
   const int y = blockIdx.x, z = blockIdx.y + z0;
   double *row = ref + ((size_t)z * (ny + 2) + y) * (size_t)(nx + 2);
   for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
-    double v = fabs((double)src[L.index(x, y, z)]);  // ZC fields mark frozen nodes with the sign
+    double v = (double)src[L.index(x, y, z)];
+    if (L.zc) v = fabs(v);  // z-column fields mark frozen nodes with the sign
     if (fmask && x >= 1 && x <= nx && y >= 1 && y <= ny) {
       const uint32_t w = fmask[M.word(x, y, z)];
       if ((w >> ((x - 1) & 31)) & 1u) v = in64[L64.index(x, y, z)];
@@ -141,7 +142,7 @@ __global__ void k_convert(const S *__restrict__ src, Layout Ls, D *__restrict__ 
 template <class T>
 __global__ void k_zc_fill(T *__restrict__ dst, Layout Ld, const double *__restrict__ in64, Layout L64,
                           const float *__restrict__ u32, Layout L32, bool from32, const uint32_t *__restrict__ fmask,
-                          MaskLayout M, int nx, int ny, int nz) {
+                          MaskLayout M, int nx, int ny, int nz, int *neg) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < Ld.elems; i += (size_t)gridDim.x * blockDim.x) {
     const long long col = (long long)(i / (size_t)Ld.qz);
     const int z = (int)(i - (size_t)col * (size_t)Ld.qz) - kLcZ0;
@@ -155,6 +156,8 @@ __global__ void k_zc_fill(T *__restrict__ dst, Layout Ld, const double *__restri
     }
     bool frz = x < 1 || x > nx || y < 1 || y > ny || z < 1 || z > nz;
     if (!frz && fmask) frz = (fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u;
+    // the sign bit marks frozen nodes: a node the sweeps update must not carry one
+    if (!frz && signbit(in64[L64.index(x, y, z)])) *neg = 1;
     if constexpr (sizeof(T) == 4) {
       const float v = (float)in64[L64.index(x, y, z)];
       dst[i] = frz ? -fabsf(v) : v;
@@ -1109,13 +1112,24 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
 
 // A z-column working field from the input (FP32, or pairs) or, for pairs
 // with from32, from the FP32 field: frozen nodes and the halo signed.
+// Lane-column tiles take fields whose updated nodes are >= 0 (distances):
+// a negative input there returns PDFS_ERR_INVALID (the pencil tiles take any sign).
 template <class T>
 static int zc_fill(pdfs_ctx *c, T *dst, const Layout &Ld, bool from32) {
   const pdfs_grid &g = c->g;
+  int *neg = &c->dstat->err[3];
+  CK(cudaMemsetAsync(neg, 0, 4, c->st));
   k_zc_fill<T><<<8 * c->sms, 256, 0, c->st>>>(dst, Ld, c->in64, c->L64, c->u32, c->L32, from32,
-                                              c->has_mask ? c->fmask : nullptr, c->M, g.nx, g.ny, g.nz);
+                                              c->has_mask ? c->fmask : nullptr, c->M, g.nx, g.ny, g.nz, neg);
   c->launches++;
   CK(cudaGetLastError());
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, neg, 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (h) {
+    if (verbose(c->o)) fprintf(stderr, "pdfs: lane-column tiles need a field >= 0 at the nodes they update\n");
+    return PDFS_ERR_INVALID;
+  }
   return PDFS_OK;
 }
 

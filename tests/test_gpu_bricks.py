@@ -259,7 +259,7 @@ def test_pair_polish_within_1e6(iso):
     a = w.field.copy()
     st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
                    arith=L.ARITH_PAIR, tol=1e-6 * min(sp), max_sweeps=200)
-    assert (st["tile"] >> 8) in (5, 6, 7, 8) and st["sweeps_fp64"] > 0  # bricks or pencils
+    assert (st["tile"] >> 8) in (5, 6, 7, 8, 9) and st["sweeps_fp64"] > 0  # bricks, pencils or lane columns
     b = w.field.copy()
     O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
     # tolerance: 1e-6 relative, as for the mixed arithmetic
