@@ -182,7 +182,7 @@ COLUMNS64 = {1: (4, 1), 2: (4, 2), 3: (8, 2), 4: (6, 1)}
 BRICKS32 = {8: (16, 16), 9: (16, 32), 11: (8, 48)}
 BRICKS64 = {5: (16, 16), 7: (16, 32), 8: (8, 32)}
 PENCILS32, PENCILS64 = (10,), (6,)
-LANECOL32, LANECOL64 = {12: 8}, {9: 8}  # lane-column tiles: rows per tile
+LANECOL32, LANECOL64 = {12: 8, 13: 4}, {9: 8, 10: 4}  # lane-column tiles: rows per tile
 
 
 def kernel_kind(kind, tile):

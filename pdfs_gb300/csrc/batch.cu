@@ -410,7 +410,8 @@ extern "C" int pdfs_autotune(const pdfs_grid *g, const pdfs_opts *o_in, int *til
     for (int t = 1; t <= (o.precision == PDFS_PREC_FP32_POLISH64 ? 2 : 3); ++t) c64.push_back(t);
   if (o.arith == PDFS_ARITH_FAST) c64.push_back(4);
   for (int t : {5, 6, 7, 8}) c64.push_back(t);  // bricks and pencils: every arithmetic
-  if (o.arith == PDFS_ARITH_PAIR) c64.push_back(9);  // lane columns: FP32 pairs
+  if (o.arith == PDFS_ARITH_PAIR)
+    for (int t : {9, 10}) c64.push_back(t);  // lane columns: FP32 pairs
   for (int t : c64) {
     double ms = 0;
     if (time_tile(PDFS_PREC_FP64, t, &ms) == PDFS_OK && ms < b) {

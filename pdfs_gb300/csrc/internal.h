@@ -84,8 +84,8 @@ cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs
                                  cudaStream_t st, int *grid_used);
 cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty);
 // One sweep by the lane-column kernel (lanecol.cu): which 0 = FP32 min, 1 =
-// pair min, 2 = pair replace.
-cudaError_t launch_sweep_lanecol(int which, bool iso, const LcArgs &a, int sms, cudaStream_t st,
+// pair min, 2 = pair replace; tiles of rows = 4 or 8 rows.
+cudaError_t launch_sweep_lanecol(int which, int rows, bool iso, const LcArgs &a, int sms, cudaStream_t st,
                                  int *grid_used);
 // Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
 std::vector<int> brick_order(int ntx, int nty, int ntz);

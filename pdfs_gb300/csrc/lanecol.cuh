@@ -51,27 +51,31 @@ namespace pdfs {
 
 // ---- memory helpers: one 16-byte vector of a column (four FP32 values or two
 // pairs); the L2::256B hint has L2 fetch the next 256 bytes of the column too
+// The field loads and stores are ordinary (schedulable) accesses: a lane
+// reads each element of its columns once, before it or any other tile writes
+// it, and writes only its own columns.
 __device__ __forceinline__ void lc_ld(float (&v)[4], const float *p) {
-  asm volatile("ld.global.L2::256B.v4.f32 {%0, %1, %2, %3}, [%4];\n"
-               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
-               : "l"(p));
+  asm("ld.global.L2::256B.v4.f32 {%0, %1, %2, %3}, [%4];\n"
+      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+      : "l"(p));
 }
 __device__ __forceinline__ void lc_ld(double (&v)[2], const double *p) {
-  asm volatile("ld.global.L2::256B.v2.f64 {%0, %1}, [%2];\n" : "=d"(v[0]), "=d"(v[1]) : "l"(p));
+  asm("ld.global.L2::256B.v2.f64 {%0, %1}, [%2];\n" : "=d"(v[0]), "=d"(v[1]) : "l"(p));
 }
 __device__ __forceinline__ void lc_st(float *p, const float (&v)[4]) {
-  asm volatile("st.global.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"l"(p), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
-               : "memory");
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
 __device__ __forceinline__ void lc_st(double *p, const double (&v)[2]) {
-  asm volatile("st.global.v2.f64 [%0], {%1, %2};\n" ::"l"(p), "d"(v[0]), "d"(v[1]) : "memory");
+  *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
 }
+// Mailbox words: relaxed at GPU scope (single-copy atomic 64-bit words); a
+// poll re-reads the word every time (volatile asm), nothing else is ordered.
 __device__ __forceinline__ void lc_put(unsigned long long *p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;\n" ::"l"(p), "l"(v) : "memory");
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;\n" ::"l"(p), "l"(v));
 }
 __device__ __forceinline__ unsigned long long lc_get(const unsigned long long *p) {
   unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];\n" : "=l"(v) : "l"(p));
   return v;
 }
 

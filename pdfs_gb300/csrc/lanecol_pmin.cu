@@ -3,5 +3,5 @@
 #include "lanecol.cuh"
 
 namespace pdfs {
-template cudaError_t launch_lc_dir<double, kLcRows64, MODE_MIN>(bool, bool, const LcArgs &, int, cudaStream_t, int *);
+template cudaError_t launch_lc_dir<double, 8, MODE_MIN>(bool, bool, const LcArgs &, int, cudaStream_t, int *);
 }  // namespace pdfs

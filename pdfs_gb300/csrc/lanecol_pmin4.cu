@@ -1,0 +1,7 @@
+// lanecol_pmin4.cu -- 4-row FP32-pair min-update instantiations of the lane-column sweep.
+#include "internal.h"
+#include "lanecol.cuh"
+
+namespace pdfs {
+template cudaError_t launch_lc_dir<double, 4, MODE_MIN>(bool, bool, const LcArgs &, int, cudaStream_t, int *);
+}  // namespace pdfs

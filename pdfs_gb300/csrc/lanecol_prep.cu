@@ -3,6 +3,5 @@
 #include "lanecol.cuh"
 
 namespace pdfs {
-template cudaError_t launch_lc_dir<double, kLcRows64, MODE_REPLACE>(bool, bool, const LcArgs &, int, cudaStream_t,
-                                                                    int *);
+template cudaError_t launch_lc_dir<double, 8, MODE_REPLACE>(bool, bool, const LcArgs &, int, cudaStream_t, int *);
 }  // namespace pdfs

@@ -1,0 +1,7 @@
+// lanecol_prep4.cu -- 4-row FP32-pair replace-update (polish) instantiations of the lane-column sweep.
+#include "internal.h"
+#include "lanecol.cuh"
+
+namespace pdfs {
+template cudaError_t launch_lc_dir<double, 4, MODE_REPLACE>(bool, bool, const LcArgs &, int, cudaStream_t, int *);
+}  // namespace pdfs

@@ -514,7 +514,7 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
   // reference one (polish: 1-2); 1-4 for the fast one (polish: 1, 2, 4);
   // bricks (5: 16 x 16 x 16, 7: 16 x 16 x 32) and pencils (6) for every
   // arithmetic; FP32 pairs on bricks and pencils only
-  if (t64 == 9 && o->arith != PDFS_ARITH_PAIR) return PDFS_ERR_INVALID;  // lane columns: FP32 pairs only
+  if ((t64 == 9 || t64 == 10) && o->arith != PDFS_ARITH_PAIR) return PDFS_ERR_INVALID;  // lane columns: pairs only
   if (o->arith == PDFS_ARITH_PAIR) {
     if (t64 != 0 && t64 < 5) return PDFS_ERR_INVALID;  // FP32 pairs: bricks, pencils and lane columns
   } else if (o->arith == PDFS_ARITH_MIXED) {
@@ -1038,7 +1038,7 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
     fill_lc_args(c, which, a, &l);
     int grid = 0;
     CK(cudaEventRecord(c->k0, c->st));
-    CK(launch_sweep_lanecol(f32 ? 0 : (which == 2 ? 2 : 1), iso, l, c->sms, c->st, &grid));
+    CK(launch_sweep_lanecol(f32 ? 0 : (which == 2 ? 2 : 1), ts.lc, iso, l, c->sms, c->st, &grid));
     CK(cudaEventRecord(c->k1, c->st));
     CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));

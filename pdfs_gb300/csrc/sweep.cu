@@ -14,15 +14,15 @@ namespace pdfs {
 // Bricks may also be 16 x 8 x BZ.  Pencils (pencil.cuh) are 16 x 16
 // cross-sections marched along z: {16, 16, 0, BZ, 1}; their block-masked
 // sweeps run on 16 x 16 x BZ bricks.
-// Lane-column tiles (lanecol.cuh): 31 lanes x R rows of z-columns, {31, R, 0,
-// 0, 0, R}; their block-masked sweeps run on the same kernel.
+// Lane-column tiles (lanecol.cuh): 31 lanes x R rows of z-columns (R = 8 or
+// 4), {31, R, 0, 0, 0, R}; their block-masked sweeps run on the same kernel.
 static const TileShape kT32[] = {{32, 8, 2},  {32, 8, 4},  {32, 16, 4},     {32, 8, 1},      {32, 4, 2},
                                  {32, 6, 1},  {32, 10, 1}, {16, 16, 0, 16}, {16, 16, 0, 32}, {16, 16, 0, 32, 1},
-                                 {16, 8, 0, 48}, {31, kLcRows32, 0, 0, 0, kLcRows32}};
+                                 {16, 8, 0, 48}, {31, 8, 0, 0, 0, 8},      {31, 4, 0, 0, 0, 4}};
 // tile 4 (32 x 6, one row per warp) exists for the fast and mixed arithmetic
 static const TileShape kT64[] = {{32, 4, 1},      {32, 4, 2},         {32, 8, 2},     {32, 6, 1},
                                  {16, 16, 0, 16}, {16, 16, 0, 16, 1}, {16, 16, 0, 32}, {16, 8, 0, 32},
-                                 {31, kLcRows64, 0, 0, 0, kLcRows64}};
+                                 {31, 8, 0, 0, 0, 8}, {31, 4, 0, 0, 0, 4}};
 
 int tile_count32() { return (int)(sizeof(kT32) / sizeof(kT32[0])); }
 int tile_count64() { return (int)(sizeof(kT64) / sizeof(kT64[0])); }

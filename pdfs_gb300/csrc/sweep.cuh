@@ -56,8 +56,7 @@ enum { MODE_MIN = 0, MODE_REPLACE = 1 };
 // Lane-column tiles (lanecol.cuh) and their z-column ("ZC") field layout.
 constexpr int kLcZ0 = 16;     // column position of the halo plane z = 0
 constexpr int kLcLanes = 31;  // computing lanes of a tile
-constexpr int kLcRows32 = 8;  // rows of an FP32 tile
-constexpr int kLcRows64 = 8;  // rows of an FP32-pair tile
+
 enum { ARITH_REF = 0, ARITH_FAST = 1, ARITH_MIXED = 2, ARITH_PAIR = 3 };
 enum { DEV_ERR_TIMEOUT = 1, DEV_ERR_SMEM_ALIGN = 2 };
 

@@ -16,7 +16,8 @@ from pdfs_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-LC32, LC64 = 12, 9 << 8   # lane-column tiles
+LC32, LC64 = 12, 9 << 8   # lane-column tiles, 8 rows
+LC32_4, LC64_4 = 13, 10 << 8  # lane-column tiles, 4 rows
 P32, P64 = 10, 6 << 8     # pencils (their masked sweeps run on bricks)
 
 SHAPES = [(1, 1, 1), (2, 3, 5), (31, 1, 1), (32, 2, 2), (33, 40, 7), (70, 1, 9), (1, 70, 6), (65, 31, 47)]
@@ -44,26 +45,28 @@ def sweeps(w, tile, seq, **kw):
     return out, ch
 
 
+@pytest.mark.parametrize("lc", [LC32, LC32_4])
 @pytest.mark.parametrize("aniso", [False, True])
 @pytest.mark.parametrize("shape", SHAPES)
-def test_fp32_sweeps_equal_pencils(shape, aniso):
+def test_fp32_sweeps_equal_pencils(shape, aniso, lc):
     w = grid(shape, aniso, seed=3)
     seq = [1, 2, 3, 4, 5, 6, 7, 8, 3, 6]
-    a, ca = sweeps(w, LC32, seq, precision=L.PREC_FP32)
+    a, ca = sweeps(w, lc, seq, precision=L.PREC_FP32)
     b, cb = sweeps(w, P32, seq, precision=L.PREC_FP32)
     for k in range(len(seq)):
         assert a[k].tobytes() == b[k].tobytes(), f"sweep {k} ordering {seq[k]}"
         assert ca[k] == cb[k], f"max change of sweep {k}"
 
 
+@pytest.mark.parametrize("lc", [LC64, LC64_4])
 @pytest.mark.parametrize("aniso", [False, True])
 @pytest.mark.parametrize("shape", SHAPES)
-def test_pair_min_sweeps_equal_pencils(shape, aniso):
+def test_pair_min_sweeps_equal_pencils(shape, aniso, lc):
     """FP32-pair min-update sweeps (an FP64-precision solve in pairs)."""
     w = grid(shape, aniso, seed=4)
     seq = [1, 2, 3, 4, 5, 6, 7, 8]
     kw = dict(precision=L.PREC_FP64, arith=L.ARITH_PAIR)
-    a, ca = sweeps(w, LC64, seq, **kw)
+    a, ca = sweeps(w, lc, seq, **kw)
     b, cb = sweeps(w, P64, seq, **kw)
     for k in range(len(seq)):
         assert a[k].tobytes() == b[k].tobytes(), f"sweep {k} ordering {seq[k]}"
@@ -77,13 +80,14 @@ def test_polish_solve_equals_pencils(shape, aniso):
     w = grid(shape, aniso, seed=5)
     sp = (w.dx, w.dy, w.dz)
     res = []
-    for tile in (LC32 | LC64, P32 | P64):
+    for tile in (LC32 | LC64, LC32_4 | LC64_4, P32 | P64):
         a = w.field.copy()
         st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
                        arith=L.ARITH_PAIR, tol=1e-5 * min(sp), tile=tile)
         res.append((a, st["sweeps_fp32"], st["sweeps_fp64"]))
-    assert res[0][1:] == res[1][1:]
-    assert res[0][0].tobytes() == res[1][0].tobytes()
+    for r in res[1:]:
+        assert res[0][1:] == r[1:]
+        assert res[0][0].tobytes() == r[0].tobytes()
     ref = w.field.copy()
     O.solve(ref, sp, tol=1e-12, frozen=w.frozen, threads=8)
     i = (slice(1, -1),) * 3
@@ -91,15 +95,16 @@ def test_polish_solve_equals_pencils(shape, aniso):
     assert err <= 1e-6, err
 
 
+@pytest.mark.parametrize("rows", [8, 4])
 @pytest.mark.parametrize("prec", ["fp32", "pair"])
 @pytest.mark.parametrize("shape", [(33, 40, 7), (65, 31, 47)])
-def test_masked_sweeps_equal_pencils(shape, prec):
+def test_masked_sweeps_equal_pencils(shape, prec, rows):
     """Block-masked sweeps with per-block change output: the lane columns
     against the pencils' masked path (bricks), sweep by sweep, the field and
     every block's change word."""
     w = grid(shape, True, seed=6)
     kw = dict(precision=L.PREC_FP32) if prec == "fp32" else dict(precision=L.PREC_FP64, arith=L.ARITH_PAIR)
-    tiles = (LC32, P32) if prec == "fp32" else (LC64, P64)
+    tiles = ((LC32 if rows == 8 else LC32_4), P32) if prec == "fp32" else ((LC64 if rows == 8 else LC64_4), P64)
     rng = np.random.default_rng(7)
     outs = []
     for tile in tiles:
