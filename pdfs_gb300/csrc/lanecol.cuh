@@ -134,8 +134,9 @@ __device__ __forceinline__ T lc_godunov(T m0, T m1, T m2, const GodConst32 &k) {
 // or replace-update).  R rows per tile; VW positions per vector load (four
 // FP32 values or two pairs: 16 bytes).  SZ is the sweep's z direction.  BLK:
 // block mask and per-block change output in use.
+// Four-row tiles fit 16 warps per SM (128 registers), eight-row tiles 12.
 template <class T, int R, int MODE, bool ISO, int SZ, bool BLK>
-__global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant__ LcArgs a) {
+__global__ void __launch_bounds__(128, R <= 4 ? 4 : 3) lc_sweep_kernel(const __grid_constant__ LcArgs a) {
   using V = LcVal<T>;
   constexpr int WV = V::WV;
   constexpr int VW = 16 / (int)sizeof(T);
@@ -153,7 +154,9 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
   T *__restrict__ u = reinterpret_cast<T *>(a.u);
   const int T_ = a.T;
   const long long ys = a.cxp * a.qz;  // elements per +1 in y
-  T tmax = T(0);
+  T tmx[R];  // each row's max change (separate chains, folded at the end)
+#pragma unroll
+  for (int r = 0; r < R; ++r) tmx[r] = T(0);
 
   for (;;) {
     int tk = 0, ab = 0;
@@ -191,7 +194,9 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
     // entering a vector moves nxt into cur and loads the vector after it.
     T cur[NR][VW], nxt[NR][VW];
     T res[R];          // each row's new value of the previous level (its z-upwind value)
-    unsigned chg = 0;  // bit r: row r changed a node of its current vector
+    bool chg[R];       // row r changed a node of its current vector
+#pragma unroll
+    for (int r = 0; r < R; ++r) chg[r] = false;
 #pragma unroll
     for (int r = 0; r < NR; ++r) {
 #pragma unroll
@@ -301,30 +306,48 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
           }
         }
 
-        // -------- 3. the nodes of this level, bottom row first --------
+        // -------- 3. the nodes of this level --------
+        // Stage by stage across the rows: the rows of a level do not depend on
+        // one another (row r reads row r-1's value of the previous level and
+        // row r+1's old values), so each stage gives the scheduler R
+        // independent operations.
+        T cvv[R], up[R], dn[R], zdn[R], xup[R], xdn[R], gv[R];
 #pragma unroll
-        for (int r = R - 1; r >= 0; --r) {
-          const int p = (j - r) & (VW - 1);           // t mod VW
-          const int c = (j - r + 16) / VW - 16 / VW;  // vector of t, relative to m
-          const int e = SZ > 0 ? p : VW - 1 - p;      // element of t
+        for (int r = 0; r < R; ++r) {
+          const int p = (j - r) & (VW - 1);  // t mod VW
           const int pn = (p + 1) & (VW - 1);
-          const int en = SZ > 0 ? pn : VW - 1 - pn;   // element of t + 1
+          const int e = SZ > 0 ? p : VW - 1 - p, en = SZ > 0 ? pn : VW - 1 - pn;
           // row r+1 sits one position behind: its next position is our t
           const int p1 = (j - r - 1) & (VW - 1);
           const int pn1 = (p1 + 1) & (VW - 1);
           const int en1 = SZ > 0 ? pn1 : VW - 1 - pn1;
-          const T cv = cur[r][e];
-          const T zdn = p < VW - 1 ? cur[r][en] : nxt[r][en];
-          const T dn = p1 < VW - 1 ? cur[r + 1][en1] : nxt[r + 1][en1];
-          const T up = r == 0 ? yv : res[r - 1];
-          T xup = __shfl_up_sync(FULL, up, 1);
+          cvv[r] = cur[r][e];
+          zdn[r] = p < VW - 1 ? cur[r][en] : nxt[r][en];
+          dn[r] = p1 < VW - 1 ? cur[r + 1][en1] : nxt[r + 1][en1];
+          up[r] = r == 0 ? yv : res[r - 1];
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) xup[r] = __shfl_up_sync(FULL, up[r], 1);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
           const T xl = __shfl_sync(FULL, xv, r);
-          if (lane == 0) xup = xl;
-          const T xdn = __shfl_down_sync(FULL, dn, 1);
-          const T m0 = lc_min<T>(V::absv(xup), V::absv(xdn), fx);
-          const T m1 = lc_min<T>(V::absv(up), V::absv(dn), fy);
-          const T m2 = lc_min<T>(V::absv(res[r]), V::absv(zdn), SZ > 0);
-          const T gv = lc_godunov<T, ISO>(m0, m1, m2, k32);
+          if (lane == 0) xup[r] = xl;
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) xdn[r] = __shfl_down_sync(FULL, dn[r], 1);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const T m0 = lc_min<T>(V::absv(xup[r]), V::absv(xdn[r]), fx);
+          const T m1 = lc_min<T>(V::absv(up[r]), V::absv(dn[r]), fy);
+          const T m2 = lc_min<T>(V::absv(res[r]), V::absv(zdn[r]), SZ > 0);
+          gv[r] = lc_godunov<T, ISO>(m0, m1, m2, k32);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int p = (j - r) & (VW - 1);
+          const int c = (j - r + 16) / VW - 16 / VW;  // vector of t, relative to m
+          const int e = SZ > 0 ? p : VW - 1 - p;
+          const T cv = cvv[r];
           const int t = g - r;
           if constexpr (BLK || MODE == MODE_REPLACE) {
             // entering an 8^3 block: z == 1 (mod 8) going up, z == 0 (mod 8)
@@ -359,34 +382,36 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
           T nv;
           if constexpr (MODE == MODE_MIN) {
             if constexpr (sizeof(T) == 4)
-              nv = fminf(cv, gv);  // frozen values are negative: they stay
+              nv = fminf(cv, gv[r]);  // frozen values are negative: they stay
             else
-              nv = V::frozen(cv) ? cv : pmin(cv, gv);
+              nv = V::frozen(cv) ? cv : pmin(cv, gv[r]);
           } else {
             if (V::frozen(cv)) {
               nv = cv;
-            } else if (CapBound<T, ARITH>::below(gv, bnd[r])) {
-              nv = gv;
+            } else if (CapBound<T, ARITH>::below(gv[r], bnd[r])) {
+              nv = gv[r];
             } else {
               const long long q = SZ > 0 ? (long long)kLcZ0 + t : (long long)a.q_last - t;
-              nv = pmin(cap_value<T, ARITH>(reinterpret_cast<const T *>(a.cap) + (ubase - u) + (r * ys32 + (int)q)), gv);
+              nv = pmin(cap_value<T, ARITH>(reinterpret_cast<const T *>(a.cap) + (ubase - u) + (r * ys32 + (int)q)),
+                        gv[r]);
             }
           }
           if constexpr (BLK) {
             if (a.blk_active && !(bcur[r] >= 0 && __ldg(a.blk_active + bcur[r]))) nv = cv;
           }
-          if (vdiffers<T, ARITH>(nv, cv)) {
+          const bool changed = vdiffers<T, ARITH>(nv, cv);
+          if (changed) {
             const T d = node_change<T, ARITH>(cv, nv, hmin);
-            tmax = vmax_nonneg<T, ARITH>(tmax, d);
-            chg |= 1u << r;
+            tmx[r] = vmax_nonneg<T, ARITH>(tmx[r], d);
             if constexpr (BLK) bch[r] = fmaxf(bch[r], change_f<T, ARITH>(d));
           }
+          chg[r] = chg[r] || changed;
           cur[r][e] = nv;
           res[r] = nv;
           // leaving the vector: write it back if one of its nodes changed
           if (p == VW - 1) {
-            if (((chg >> r) & 1) && lane < kLcLanes) lc_st(vaddr(r, m + c), cur[r]);
-            chg &= ~(1u << r);
+            if (chg[r] && lane < kLcLanes) lc_st(vaddr(r, m + c), cur[r]);
+            chg[r] = false;
           }
         }
 
@@ -421,6 +446,9 @@ __global__ void __launch_bounds__(128, 3) lc_sweep_kernel(const __grid_constant_
     }
   }
   // the warp's max change -> the grid's counter (lane 31 only copies the next tile's column)
+  T tmax = tmx[0];
+#pragma unroll
+  for (int r = 1; r < R; ++r) tmax = vmax_nonneg<T, ARITH>(tmax, tmx[r]);
   T v = lane < kLcLanes ? tmax : T(0);
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(FULL, v, off));
