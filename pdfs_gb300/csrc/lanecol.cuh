@@ -236,64 +236,75 @@ __global__ void __launch_bounds__(128, R <= 4 ? 4 : 3) lc_sweep_kernel(const __g
         a.xmail + ((size_t)(tx > 0 ? tx - 1 : 0) * a.xrows + (size_t)(has_left ? xrow_in : 0)) * T_ * WV;
     unsigned long long *xpub = a.xmail + ((size_t)tx * a.xrows + (size_t)R * ty + 1) * T_ * WV;
 
-    // mailbox words of two levels: slot g & 1 holds level g
-    unsigned long long py0[2], py1[2], px0[2], px1[2];
+    // Mailbox words.  The x face of level g is fetched at the end of level
+    // g-1; the y face (row 0's upwind row) is fetched at the start of level
+    // g and only needed after rows R-1..1 of the level are done, so its
+    // latency hides behind them.
+    unsigned long long py0, py1, px0, px1;
     auto need_y = [&](int g) { return has_up && g < T_; };
     auto need_x = [&](int g) { return has_left && g - lane >= 0 && g - lane < T_; };
-    auto fetch = [&](int g, int sl) {
-      const bool ny_ = need_y(g), nx_ = need_x(g);
-      py0[sl] = ny_ ? lc_get(ybox + (size_t)g * 32 * WV) : (tag | 0x7f800000ull);
-      py1[sl] = (WV == 2 && ny_) ? lc_get(ybox + (size_t)g * 32 * WV + 1) : tag;
-      px0[sl] = nx_ ? lc_get(xbox + (size_t)(g - lane) * WV) : (tag | 0x7f800000ull);
-      px1[sl] = (WV == 2 && nx_) ? lc_get(xbox + (size_t)(g - lane) * WV + 1) : tag;
+    auto fetch_y = [&](int g) {
+      const bool n = need_y(g);
+      py0 = n ? lc_get(ybox + (size_t)g * 32 * WV) : (tag | 0x7f800000ull);
+      py1 = (WV == 2 && n) ? lc_get(ybox + (size_t)g * 32 * WV + 1) : tag;
     };
-    auto tags_ok = [&](int sl) {
-      return (unsigned)(py0[sl] >> 32) == etag && (WV == 1 || (unsigned)(py1[sl] >> 32) == etag) &&
-             (unsigned)(px0[sl] >> 32) == etag && (WV == 1 || (unsigned)(px1[sl] >> 32) == etag);
+    auto fetch_x = [&](int g) {
+      const bool n = need_x(g);
+      px0 = n ? lc_get(xbox + (size_t)(g - lane) * WV) : (tag | 0x7f800000ull);
+      px1 = (WV == 2 && n) ? lc_get(xbox + (size_t)(g - lane) * WV + 1) : tag;
     };
-    fetch(0, 0);
-    fetch(1, 1);
+    auto ok_y = [&]() { return (unsigned)(py0 >> 32) == etag && (WV == 1 || (unsigned)(py1 >> 32) == etag); };
+    auto ok_x = [&]() { return (unsigned)(px0 >> 32) == etag && (WV == 1 || (unsigned)(px1 >> 32) == etag); };
+    // Bounded wait until the words of level g carry this sweep's tag: a few
+    // tight polls (each an L2 round trip), then sleeps of growing length.
+    // false: the wait gave up (timeout recorded) or another tile aborted.
+    auto wait_faces = [&](int g, bool ys) -> bool {
+      const long long t0 = clock64();
+      unsigned nap = 0;
+      for (int it = 0;; ++it) {
+        if (ys) {
+          if (need_y(g)) {
+            py0 = lc_get(ybox + (size_t)g * 32 * WV);
+            if (WV == 2) py1 = lc_get(ybox + (size_t)g * 32 * WV + 1);
+          }
+          if (__all_sync(FULL, ok_y())) return true;
+        } else {
+          if (need_x(g)) {
+            px0 = lc_get(xbox + (size_t)(g - lane) * WV);
+            if (WV == 2) px1 = lc_get(xbox + (size_t)(g - lane) * WV + 1);
+          }
+          if (__all_sync(FULL, ok_x())) return true;
+        }
+        int stop = 0;
+        if (lane == 0) {
+          if (*(volatile int *)(a.err + 1)) {
+            stop = 1;
+          } else if (clock64() - t0 > a.wait_cycles) {
+            atomicCAS(a.err, 0, DEV_ERR_TIMEOUT);
+            atomicExch(a.err + 2, tile);
+            atomicExch(a.err + 1, 1);
+            stop = 1;
+          }
+        }
+        if (__shfl_sync(FULL, stop, 0)) return false;
+        if (it >= 8) {
+          __nanosleep(nap);
+          nap = nap < 32 ? 32 : min(nap * 2u, 256u);
+        }
+      }
+    };
+    fetch_x(0);
 
     const int M = (T_ + R - 1 + VW - 1) / VW;  // row R-1 reaches the last position T-1 at level T + R - 2
     for (int m = 0; m < M; ++m) {
 #pragma unroll
       for (int j = 0; j < VW; ++j) {
         const int g = VW * m + j;
-        const int sl = j & 1;
-        // -------- 1. the upwind faces of this level (prefetched two levels ago) --------
-        if (!__all_sync(FULL, tags_ok(sl))) {
-          const long long t0 = clock64();
-          unsigned nap = 32;
-          for (;;) {
-            const bool ny_ = need_y(g), nx_ = need_x(g);
-            if (ny_) {
-              py0[sl] = lc_get(ybox + (size_t)g * 32 * WV);
-              if (WV == 2) py1[sl] = lc_get(ybox + (size_t)g * 32 * WV + 1);
-            }
-            if (nx_) {
-              px0[sl] = lc_get(xbox + (size_t)(g - lane) * WV);
-              if (WV == 2) px1[sl] = lc_get(xbox + (size_t)(g - lane) * WV + 1);
-            }
-            if (__all_sync(FULL, tags_ok(sl))) break;
-            int stop = 0;
-            if (lane == 0) {
-              if (*(volatile int *)(a.err + 1)) {
-                stop = 1;
-              } else if (clock64() - t0 > a.wait_cycles) {
-                atomicCAS(a.err, 0, DEV_ERR_TIMEOUT);
-                atomicExch(a.err + 2, tile);
-                atomicExch(a.err + 1, 1);
-                stop = 1;
-              }
-            }
-            if (__shfl_sync(FULL, stop, 0)) return;  // the whole warp leaves; nothing is in flight
-            __nanosleep(nap);
-            nap = min(nap * 2u, 256u);
-          }
-        }
-        const T yv = V::from((unsigned)py0[sl], (unsigned)py1[sl]);
-        const T xv = V::from((unsigned)px0[sl], (unsigned)px1[sl]);
-        fetch(g + 2, sl);
+        // -------- 1. faces: the x face of this level (fetched last level), the y face's fetch --------
+        if (!__all_sync(FULL, ok_x()) && !wait_faces(g, false)) return;  // the warp leaves; nothing in flight
+        const T xv = V::from((unsigned)px0, (unsigned)px1);
+        fetch_x(g + 1);
+        fetch_y(g);
 
         // -------- 2. a row entering a vector takes the next one and loads the one after --------
 #pragma unroll
@@ -306,132 +317,144 @@ __global__ void __launch_bounds__(128, R <= 4 ? 4 : 3) lc_sweep_kernel(const __g
           }
         }
 
-        // -------- 3. the nodes of this level --------
-        // Stage by stage across the rows: the rows of a level do not depend on
-        // one another (row r reads row r-1's value of the previous level and
-        // row r+1's old values), so each stage gives the scheduler R
+        // -------- 3. the nodes of this level: rows R-1..1, then row 0 --------
+        // The rows of a level do not depend on one another (row r reads row
+        // r-1's value of the previous level and row r+1's old values); rows
+        // R-1..1 need nothing from the tile above, row 0 needs its y face.
+        // Each stage runs across the pass's rows, giving the scheduler
         // independent operations.
-        T cvv[R], up[R], dn[R], zdn[R], xup[R], xdn[R], gv[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int p = (j - r) & (VW - 1);  // t mod VW
-          const int pn = (p + 1) & (VW - 1);
-          const int e = SZ > 0 ? p : VW - 1 - p, en = SZ > 0 ? pn : VW - 1 - pn;
-          // row r+1 sits one position behind: its next position is our t
-          const int p1 = (j - r - 1) & (VW - 1);
-          const int pn1 = (p1 + 1) & (VW - 1);
-          const int en1 = SZ > 0 ? pn1 : VW - 1 - pn1;
-          cvv[r] = cur[r][e];
-          zdn[r] = p < VW - 1 ? cur[r][en] : nxt[r][en];
-          dn[r] = p1 < VW - 1 ? cur[r + 1][en1] : nxt[r + 1][en1];
-          up[r] = r == 0 ? yv : res[r - 1];
-        }
+        for (int pass = 0; pass < 2; ++pass) {
+          if (pass == 1) {
+            // publish what rows R-1..1 computed: row R-1 is the next tile's y face
+            if (publish) {
+              const int tb = g - (R - 1);
+              if (tb >= 0 && tb < T_) {
+                unsigned long long *pp = ypub + (size_t)tb * 32 * WV;
+                lc_put(pp, tag | V::word(res[R - 1], 0));
+                if (WV == 2) lc_put(pp + 1, tag | V::word(res[R - 1], 1));
+              }
+            }
+            if (!__all_sync(FULL, ok_y()) && !wait_faces(g, true)) return;
+          }
+          const T yv = V::from((unsigned)py0, (unsigned)py1);
+          T cvv[R], up[R], dn[R], zdn[R], xup[R], xdn[R], gv[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) xup[r] = __shfl_up_sync(FULL, up[r], 1);
+          for (int r = 0; r < R; ++r) {
+            if ((pass == 0) == (r == 0)) continue;
+            const int p = (j - r) & (VW - 1);  // t mod VW
+            const int pn = (p + 1) & (VW - 1);
+            const int e = SZ > 0 ? p : VW - 1 - p, en = SZ > 0 ? pn : VW - 1 - pn;
+            // row r+1 sits one position behind: its next position is our t
+            const int p1 = (j - r - 1) & (VW - 1);
+            const int pn1 = (p1 + 1) & (VW - 1);
+            const int en1 = SZ > 0 ? pn1 : VW - 1 - pn1;
+            cvv[r] = cur[r][e];
+            zdn[r] = p < VW - 1 ? cur[r][en] : nxt[r][en];
+            dn[r] = p1 < VW - 1 ? cur[r + 1][en1] : nxt[r + 1][en1];
+            up[r] = r == 0 ? yv : res[r - 1];
+          }
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const T xl = __shfl_sync(FULL, xv, r);
-          if (lane == 0) xup[r] = xl;
-        }
+          for (int r = 0; r < R; ++r) {
+            if ((pass == 0) == (r == 0)) continue;
+            xup[r] = __shfl_up_sync(FULL, up[r], 1);
+          }
 #pragma unroll
-        for (int r = 0; r < R; ++r) xdn[r] = __shfl_down_sync(FULL, dn[r], 1);
+          for (int r = 0; r < R; ++r) {
+            if ((pass == 0) == (r == 0)) continue;
+            const T xl = __shfl_sync(FULL, xv, r);
+            if (lane == 0) xup[r] = xl;
+          }
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const T m0 = lc_min<T>(V::absv(xup[r]), V::absv(xdn[r]), fx);
-          const T m1 = lc_min<T>(V::absv(up[r]), V::absv(dn[r]), fy);
-          const T m2 = lc_min<T>(V::absv(res[r]), V::absv(zdn[r]), SZ > 0);
-          gv[r] = lc_godunov<T, ISO>(m0, m1, m2, k32);
-        }
+          for (int r = 0; r < R; ++r) {
+            if ((pass == 0) == (r == 0)) continue;
+            xdn[r] = __shfl_down_sync(FULL, dn[r], 1);
+          }
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int p = (j - r) & (VW - 1);
-          const int c = (j - r + 16) / VW - 16 / VW;  // vector of t, relative to m
-          const int e = SZ > 0 ? p : VW - 1 - p;
-          const T cv = cvv[r];
-          const int t = g - r;
-          if constexpr (BLK || MODE == MODE_REPLACE) {
-            // entering an 8^3 block: z == 1 (mod 8) going up, z == 0 (mod 8)
-            // going down (the column's padding puts z = 8 ceil(nz/8) on the path)
-            if (((t - (SZ > 0 ? 1 : 7)) & 7) == 0) {
-              const int z = SZ > 0 ? t : a.q_last - kLcZ0 - t;
-              const int bz = (z - 1) >> 3;
-              const int nb = (bz >= 0 && bz < a.nbz && bxy[r] >= 0) ? bz * a.nby * a.nbx + bxy[r] : -1;
-              if constexpr (BLK) {
-                // the change of the block the row leaves: the lanes of a row
-                // that share a block form one contiguous run (both block
-                // coordinates are monotone in the lane), reduced in-warp
-                if (a.blk_chg && __any_sync(FULL, bch[r] > 0.0f)) {
-                  const int key = lane < kLcLanes ? bcur[r] : -1;
-                  float mv = bch[r];
+          for (int r = 0; r < R; ++r) {
+            if ((pass == 0) == (r == 0)) continue;
+            const T m0 = lc_min<T>(V::absv(xup[r]), V::absv(xdn[r]), fx);
+            const T m1 = lc_min<T>(V::absv(up[r]), V::absv(dn[r]), fy);
+            const T m2 = lc_min<T>(V::absv(res[r]), V::absv(zdn[r]), SZ > 0);
+            gv[r] = lc_godunov<T, ISO>(m0, m1, m2, k32);
+          }
 #pragma unroll
-                  for (int off = 1; off < 32; off <<= 1) {
-                    const float ov = __shfl_down_sync(FULL, mv, off);
-                    const int ko = __shfl_down_sync(FULL, key, off);
-                    if (lane + off < 32 && ko == key) mv = fmaxf(mv, ov);
+          for (int r = 0; r < R; ++r) {
+            if ((pass == 0) == (r == 0)) continue;
+            const int p = (j - r) & (VW - 1);
+            const int c = (j - r + 16) / VW - 16 / VW;  // vector of t, relative to m
+            const int e = SZ > 0 ? p : VW - 1 - p;
+            const T cv = cvv[r];
+            const int t = g - r;
+            if constexpr (BLK || MODE == MODE_REPLACE) {
+              // entering an 8^3 block: z == 1 (mod 8) going up, z == 0 (mod 8)
+              // going down (the column's padding puts z = 8 ceil(nz/8) on the path)
+              if (((t - (SZ > 0 ? 1 : 7)) & 7) == 0) {
+                const int z = SZ > 0 ? t : a.q_last - kLcZ0 - t;
+                const int bz = (z - 1) >> 3;
+                const int nb = (bz >= 0 && bz < a.nbz && bxy[r] >= 0) ? bz * a.nby * a.nbx + bxy[r] : -1;
+                if constexpr (BLK) {
+                  // the change of the block the row leaves: the lanes of a row
+                  // that share a block form one contiguous run (both block
+                  // coordinates are monotone in the lane), reduced in-warp
+                  if (a.blk_chg && __any_sync(FULL, bch[r] > 0.0f)) {
+                    const int key = lane < kLcLanes ? bcur[r] : -1;
+                    float mv = bch[r];
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                      const float ov = __shfl_down_sync(FULL, mv, off);
+                      const int ko = __shfl_down_sync(FULL, key, off);
+                      if (lane + off < 32 && ko == key) mv = fmaxf(mv, ov);
+                    }
+                    const int kp = __shfl_up_sync(FULL, key, 1);
+                    if (key >= 0 && mv > 0.0f && (lane == 0 || kp != key))
+                      atomicMax(a.blk_chg + key, __float_as_uint(mv));
                   }
-                  const int kp = __shfl_up_sync(FULL, key, 1);
-                  if (key >= 0 && mv > 0.0f && (lane == 0 || kp != key))
-                    atomicMax(a.blk_chg + key, __float_as_uint(mv));
+                  bch[r] = 0.0f;
                 }
-                bch[r] = 0.0f;
+                bcur[r] = nb;
+                if constexpr (MODE == MODE_REPLACE) bnd[r] = nb >= 0 ? __ldg(a.bcap32 + nb) : -INFINITY;
               }
-              bcur[r] = nb;
-              if constexpr (MODE == MODE_REPLACE) bnd[r] = nb >= 0 ? __ldg(a.bcap32 + nb) : -INFINITY;
             }
-          }
-          T nv;
-          if constexpr (MODE == MODE_MIN) {
-            if constexpr (sizeof(T) == 4)
-              nv = fminf(cv, gv[r]);  // frozen values are negative: they stay
-            else
-              nv = V::frozen(cv) ? cv : pmin(cv, gv[r]);
-          } else {
-            if (V::frozen(cv)) {
-              nv = cv;
-            } else if (CapBound<T, ARITH>::below(gv[r], bnd[r])) {
-              nv = gv[r];
+            T nv;
+            if constexpr (MODE == MODE_MIN) {
+              if constexpr (sizeof(T) == 4)
+                nv = fminf(cv, gv[r]);  // frozen values are negative: they stay
+              else
+                nv = V::frozen(cv) ? cv : pmin(cv, gv[r]);
             } else {
-              const long long q = SZ > 0 ? (long long)kLcZ0 + t : (long long)a.q_last - t;
-              nv = pmin(cap_value<T, ARITH>(reinterpret_cast<const T *>(a.cap) + (ubase - u) + (r * ys32 + (int)q)),
-                        gv[r]);
-            }
-          }
-          if constexpr (BLK) {
-            if (a.blk_active && !(bcur[r] >= 0 && __ldg(a.blk_active + bcur[r]))) nv = cv;
-          }
-          const bool changed = vdiffers<T, ARITH>(nv, cv);
-          if (changed) {
-            const T d = node_change<T, ARITH>(cv, nv, hmin);
-            tmx[r] = vmax_nonneg<T, ARITH>(tmx[r], d);
-            if constexpr (BLK) bch[r] = fmaxf(bch[r], change_f<T, ARITH>(d));
-          }
-          chg[r] = chg[r] || changed;
-          cur[r][e] = nv;
-          res[r] = nv;
-          // leaving the vector: write it back if one of its nodes changed
-          if (p == VW - 1) {
-            if (chg[r] && lane < kLcLanes) lc_st(vaddr(r, m + c), cur[r]);
-            chg[r] = false;
-          }
-        }
-
-        // -------- 4. publish this level's faces --------
-        if (publish) {
-          const int tb = g - (R - 1);  // row R-1's position
-          if (tb >= 0 && tb < T_) {
-            unsigned long long *pp = ypub + (size_t)tb * 32 * WV;
-            lc_put(pp, tag | V::word(res[R - 1], 0));
-            if (WV == 2) lc_put(pp + 1, tag | V::word(res[R - 1], 1));
-          }
-          if (lane == kLcLanes - 1) {
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-              const int tr = g - r;
-              if (tr >= 0 && tr < T_) {
-                unsigned long long *pp = xpub + ((size_t)r * T_ + tr) * WV;
-                lc_put(pp, tag | V::word(res[r], 0));
-                if (WV == 2) lc_put(pp + 1, tag | V::word(res[r], 1));
+              if (V::frozen(cv)) {
+                nv = cv;
+              } else if (CapBound<T, ARITH>::below(gv[r], bnd[r])) {
+                nv = gv[r];
+              } else {
+                const long long q = SZ > 0 ? (long long)kLcZ0 + t : (long long)a.q_last - t;
+                nv = pmin(cap_value<T, ARITH>(reinterpret_cast<const T *>(a.cap) + (ubase - u) + (r * ys32 + (int)q)),
+                          gv[r]);
               }
+            }
+            if constexpr (BLK) {
+              if (a.blk_active && !(bcur[r] >= 0 && __ldg(a.blk_active + bcur[r]))) nv = cv;
+            }
+            const bool changed = vdiffers<T, ARITH>(nv, cv);
+            if (changed) {
+              const T d = node_change<T, ARITH>(cv, nv, hmin);
+              tmx[r] = vmax_nonneg<T, ARITH>(tmx[r], d);
+              if constexpr (BLK) bch[r] = fmaxf(bch[r], change_f<T, ARITH>(d));
+            }
+            chg[r] = chg[r] || changed;
+            cur[r][e] = nv;
+            res[r] = nv;
+            // leaving the vector: write it back if one of its nodes changed
+            if (p == VW - 1) {
+              if (chg[r] && lane < kLcLanes) lc_st(vaddr(r, m + c), cur[r]);
+              chg[r] = false;
+            }
+            // lane 30's value is the next tile's x face
+            if (publish && lane == kLcLanes - 1 && t >= 0 && t < T_) {
+              unsigned long long *pp = xpub + ((size_t)r * T_ + t) * WV;
+              lc_put(pp, tag | V::word(nv, 0));
+              if (WV == 2) lc_put(pp + 1, tag | V::word(nv, 1));
             }
           }
         }
