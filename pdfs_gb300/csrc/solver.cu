@@ -535,10 +535,13 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
 // sweep, against 8.1 ms for 16 x 16 x 16 bricks and 15.9 ms for mixed 32 x 6
 // columns; 51 ms per plain fast-arithmetic sweep against 55 ms for 32 x 4
 // columns (the reference arithmetic is even: both are FP64-pipe-bound).
+// The lane-column tiles (FP32 12/13, pairs 9/10) measured 6.1 / 3.7 ms per
+// FP32 sweep and 26.6 / 11.6 ms per pair polish sweep (8 / 4 rows): they stay
+// selectable (and autotuned), not the default.
 static void pick_tiles(pdfs_ctx *c) {
   const int t32 = c->o.tile & 0xff, t64 = (c->o.tile >> 8) & 0xff;
-  c->t32 = t32 ? t32 : 12;
-  c->t64 = t64 ? t64 : (c->o.arith == PDFS_ARITH_PAIR ? 9 : 6);
+  c->t32 = t32 ? t32 : 10;
+  c->t64 = t64 ? t64 : 6;
 }
 
 extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_ctx **out) {

@@ -41,8 +41,7 @@ def default_tiles():
     """The default tile ids (pick_tiles in solver.cu)."""
     src = open(os.path.join(ROOT, "pdfs_gb300", "csrc", "solver.cu")).read()
     t32 = int(re.search(r"c->t32 = t32 \? t32 : (\d+);", src).group(1))
-    # the FP64 default for the pair arithmetic (the headline polish)
-    t64 = int(re.search(r"c->t64 = t64 \? t64 : \(c->o.arith == PDFS_ARITH_PAIR \? (\d+) : \d+\);", src).group(1))
+    t64 = int(re.search(r"c->t64 = t64 \? t64 : (\d+);", src).group(1))
     return t32, t64
 
 
@@ -72,8 +71,8 @@ def test_default_kernels_have_profiles_and_traffic(bench):
     tile = t32 | (t64 << 8)
     n32 = bench.kernel_name("fp32", tile, L.PREC_FP32_POLISH64, L.ARITH_PAIR)
     n64 = bench.kernel_name("fp64", tile, L.PREC_FP32_POLISH64, L.ARITH_PAIR)
-    assert n32 == "lc_sweep_kernel<float, 8, MIN>"
-    assert n64 == "lc_sweep_kernel<double, 8, REPLACE>"
+    assert n32 == "pc_sweep_kernel<float, MIN, FAST>"
+    assert n64 == "pc_sweep_kernel<double, REPLACE, PAIR>"
     traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     for kind, name in (("fp32", n32), ("fp64", n64)):
         t = bench.traffic_per_launch(kind, L.PREC_FP32_POLISH64, 1000, tile)
