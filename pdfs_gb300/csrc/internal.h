@@ -162,6 +162,9 @@ struct pdfs_ctx {
   int *order32 = nullptr, *order64 = nullptr, *progress = nullptr, *ticket = nullptr;
   // brick tiles (tile3d.cuh): per-brick completion epochs, ticket orders, brick grids
   int *tflag = nullptr, *tord32 = nullptr, *tord64 = nullptr;
+  // block-masked brick sweeps: per brick, an active block?  and [count, tickets...]
+  uint8_t *tact = nullptr;
+  int *tsparse = nullptr;
   int nt32[3] = {0, 0, 0}, nt64[3] = {0, 0, 0};
   int epoch = 0;  // flag value of the last brick or pencil sweep
   unsigned long long *pmail = nullptr;  // pencils: epoch-tagged face mailboxes

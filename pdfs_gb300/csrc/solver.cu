@@ -683,6 +683,8 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   want(&c->tord32, bo[0].size() * 4);
   want(&c->tord64, bo[1].size() * 4);
   want(&c->tflag, nflags * 4);
+  want(&c->tact, nflags);
+  want(&c->tsparse, nflags ? (nflags + 1) * 4 : 0);
   want(&c->pmail, pmail_words * 8);
   want(&c->order32, w32.size() * 4);
   want(&c->order64, w64.size() * 4);
@@ -950,6 +952,8 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
   const int *nt = f32 ? c->nt32 : c->nt64;
   a.tflag = c->tflag;
   a.torder = f32 ? c->tord32 : c->tord64;
+  a.tact = active ? c->tact : nullptr;
+  a.nticket = active ? c->tsparse : nullptr;
   a.ntx = nt[0];
   a.nty = nt[1];
   a.ntz = nt[2];
@@ -1200,12 +1204,16 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   // FP32 + polish: the polish's full sweeps certify the fixed point, so the
   // FP32 phase may end on a quiet scheduled sweep (no judging sweep), and the
   // polish -- one full cycle and a certifying sweep -- visits every block.
+  // (Scheduling the polish as well was measured: its changes are small and
+  // spread, blocks skipped below tol drift, and the certifying sweeps kept
+  // finding them -- 36 to 54 polish sweeps instead of 9 on the 768^3 grid.)
   const bool polish = o.precision == PDFS_PREC_FP32_POLISH64;
   auto phase = [&](int which, double tol, int *count, double *ms, double *kms) -> int {
     c->kern_ms = 0.0;
     CK(cudaEventRecord(c->e0, c->st));
     const bool sched = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0 && !(polish && which == 2);
     const bool certify = !(polish && which == 0);  // must the phase end on a full sweep?
+    const int nfull = 8;  // sweeps that visit every block before the scheduler starts
     const float thr = (float)tol;
     // per-block changes: ring slot cur = this sweep, (cur - k) mod kRing = k sweeps ago
     int cur = 0;
@@ -1222,7 +1230,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         break;
       }
       const int sn = (first + s) % 8 + 1;
-      const bool full = !sched || s < 8 || need_full;
+      const bool full = !sched || s < nfull || need_full;
       const uint8_t *act = nullptr;
       long long nact = c->nblocks;
       if (!full) {
@@ -1244,6 +1252,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         CK(cudaEventRecord(c->q1, c->st));
         act = c->bact;
       }
+      const double kms0 = c->kern_ms;
       int r = run_sweep(c, which, sn, act, sched ? c->bchg + (size_t)cur * c->nblocks : nullptr, &chg);
       if (r) return r;
       if (!full) {
@@ -1252,8 +1261,8 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         if (c->hstat->sched_err) return PDFS_ERR_TIMEOUT;
       }
       if (verbose(o))
-        fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e active=%lld/%lld\n", which, s, sn,
-                full ? "full" : "skip", chg, nact, c->nblocks);
+        fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e active=%lld/%lld kernel %.3f ms\n", which, s,
+                sn, full ? "full" : "skip", chg, nact, c->nblocks, c->kern_ms - kms0);
       ++s;
       const long long upd = full ? nodes : (long long)((double)nodes * (double)nact / (double)c->nblocks);
       st.voxel_updates += upd;

@@ -103,6 +103,11 @@ struct SweepArgs {
   // value below it is below every cap of the block, so the cap is not read.
   const double *bcap64;
   const float *bcap32;
+  // block-masked brick sweeps: per brick (global brick id), does it hold an
+  // active 8^3 block; the tickets then list only those bricks (torder holds
+  // them in wavefront order, *nticket of them)
+  const uint8_t *tact;
+  const int *nticket;
 };
 
 // Arguments of the lane-column sweep (lanecol.cuh).

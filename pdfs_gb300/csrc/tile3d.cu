@@ -73,11 +73,76 @@ static cudaError_t dispatch_t3(int which, int arith, bool iso, const SweepArgs &
   }
 }
 
-cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, const SweepArgs &a, const Layout &L,
+// Block-masked sweeps: per brick (global brick id), whether one of its 8^3
+// blocks is active -- one thread per brick ...
+__global__ void k_brick_active(int ntx, int nty, int ntz, int bx, int by, int bz, const uint8_t *__restrict__ active,
+                               int nbx, int nby, int nbz, uint8_t *__restrict__ tact) {
+  const int n = ntx * nty * ntz;
+  for (int tile = blockIdx.x * blockDim.x + threadIdx.x; tile < n; tile += gridDim.x * blockDim.x) {
+    const int bi = tile % ntx, bj = (tile / ntx) % nty, bk = tile / (ntx * nty);
+    bool act = false;
+    for (int q = 0; q < bz && !act; ++q)
+      for (int p = 0; p < by && !act; ++p)
+        for (int o = 0; o < bx && !act; ++o) {
+          const int X = bi * bx + o, Y = bj * by + p, Z = bk * bz + q;
+          act = X < nbx && Y < nby && Z < nbz && active[((long long)Z * nby + Y) * nbx + X];
+        }
+    tact[tile] = act ? 1 : 0;
+  }
+}
+
+// ... and the tickets of the active bricks in the sweep's wavefront order
+// (out, *count of them).  One CTA: each thread takes a contiguous run of
+// tickets, the counts are scanned, the runs are written in order -- so the
+// compacted list keeps every brick after its upwind bricks.
+__global__ void k_brick_compact(const int *__restrict__ torder, int ntx, int nty, int ntz, int sx, int sy, int sz,
+                                const uint8_t *__restrict__ tact, int *__restrict__ out, int *__restrict__ count) {
+  __shared__ int s_sum[1024];
+  const int n = ntx * nty * ntz, tid = threadIdx.x, nt = blockDim.x;
+  const int per = (n + nt - 1) / nt, t0 = min(n, tid * per), t1 = min(n, t0 + per);
+  auto active = [&](int tk) {
+    const int lt = torder[tk], li = lt % ntx, lj = (lt / ntx) % nty, lk = lt / (ntx * nty);
+    const int bi = sx > 0 ? li : ntx - 1 - li, bj = sy > 0 ? lj : nty - 1 - lj, bk = sz > 0 ? lk : ntz - 1 - lk;
+    return tact[(bk * nty + bj) * ntx + bi] != 0;
+  };
+  int cnt = 0;
+  for (int tk = t0; tk < t1; ++tk) cnt += active(tk) ? 1 : 0;
+  s_sum[tid] = cnt;
+  __syncthreads();
+  for (int off = 1; off < nt; off <<= 1) {  // inclusive scan of the counts
+    const int v = tid >= off ? s_sum[tid - off] : 0;
+    __syncthreads();
+    s_sum[tid] += v;
+    __syncthreads();
+  }
+  int pos = s_sum[tid] - cnt;
+  for (int tk = t0; tk < t1; ++tk)
+    if (active(tk)) out[pos++] = torder[tk];
+  if (tid == nt - 1) *count = s_sum[tid];
+}
+
+cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, const SweepArgs &a0, const Layout &L,
                                 int sms, cudaStream_t st, int *g) {
-  if (!a.tflag || !a.torder || a.ntx < 1 || a.nty < 1 || a.ntz < 1 || L.ty != by || L.tx != 16 || L.xo != 0 ||
-      (which == 2 && (!a.bcap64 || !a.bcap32)))
+  if (!a0.tflag || !a0.torder || a0.ntx < 1 || a0.nty < 1 || a0.ntz < 1 || L.ty != by || L.tx != 16 ||
+      L.xo != 0 || (which == 2 && (!a0.bcap64 || !a0.bcap32)))
     return cudaErrorInvalidValue;
+  SweepArgs a = a0;
+  if (a0.blk_active && a0.tact && a0.nticket) {
+    // block-masked: tickets for the bricks that hold an active block only
+    int *list = const_cast<int *>(a0.nticket) + 1;  // the compacted order follows the count
+    const int n = a0.ntx * a0.nty * a0.ntz;
+    k_brick_active<<<std::min((n + 255) / 256, 4 * sms), 256, 0, st>>>(a0.ntx, a0.nty, a0.ntz, 2, by / 8, bz / 8,
+                                                                      a0.blk_active, a0.nbx, a0.nby, a0.nbz,
+                                                                      const_cast<uint8_t *>(a0.tact));
+    k_brick_compact<<<1, 1024, 0, st>>>(a0.torder, a0.ntx, a0.nty, a0.ntz, a0.sx, a0.sy, a0.sz, a0.tact, list,
+                                        const_cast<int *>(a0.nticket));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    a.torder = list;
+  } else {
+    a.tact = nullptr;
+    a.nticket = nullptr;
+  }
   if (by == 16 && bz == 16) return dispatch_t3<16, 16>(which, arith, iso, a, L, sms, st, g);
   if (by == 16 && bz == 32) return dispatch_t3<16, 32>(which, arith, iso, a, L, sms, st, g);
   if (by == 8 && bz == 32) return dispatch_t3<8, 32>(which, arith, iso, a, L, sms, st, g);

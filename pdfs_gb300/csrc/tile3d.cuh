@@ -89,7 +89,9 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
   const int gyl = syd > 0 ? ly : BY - 1 - ly;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int ntx = a.ntx, nty = a.nty, ntz = a.ntz;
-  const int ntile = ntx * nty * ntz;
+  // a block-masked sweep takes tickets only for the bricks with an active block
+  const int ntile = a.nticket ? *a.nticket : ntx * nty * ntz;
+  const uint8_t *__restrict__ tact = a.tact;
   const long long plane = a.plane, px = a.px;
   const float hmin = a.hmin;
   const GodConst64 k64 = a.k64;
@@ -207,6 +209,8 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       if (tid == 0 && li > 0) up = tile - sxd;
       if (tid == 1 && lj > 0) up = tile - syd * ntx;
       if (tid == 2 && lk > 0) up = tile - szd * ntx * nty;
+      // an upwind brick without an active block keeps its values: nothing to wait for
+      if (up >= 0 && tact && !tact[up]) up = -1;
       if (up >= 0 && ld_acquire_gpu(a.tflag + up) < epoch) {
         const long long t0 = cycles();
         unsigned nap = 32;
