@@ -117,6 +117,9 @@ constexpr float kTol32 = 4.0e-6f;
 // the last cycle).
 constexpr int kHist = 8;
 constexpr int kRing = kHist + 1;
+// The learned scheduler recomputes its band feature every kBandEvery
+// scheduled sweeps (a pass over the field each time).
+constexpr int kBandEvery = 4;
 
 // Weights of the learned scheduler compiled into the library (a blob of
 // PDFS_MLP_BLOB floats), or nullptr when none were built in.

@@ -1223,6 +1223,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     }
     bool need_full = true;
     int s = 0;
+    int band_sweep = -1;  // learned scheduler: the sweep of the last block-minimum pass
     for (;;) {
       if (o.fixed_sweeps > 0 && s >= o.fixed_sweeps) break;
       if (o.fixed_sweeps == 0 && s >= max_sweeps) {
@@ -1238,12 +1239,19 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         CK(cudaMemsetAsync(&c->dstat->active_blocks, 0, 4, c->st));
         if (o.scheduler == PDFS_SCHED_LEARNED) {
           const bool f32 = which == 0;
-          CK(block_min(f32 ? (const void *)c->u32 : (const void *)c->u64, f32 ? 0 : (o.arith == PDFS_ARITH_PAIR ? 2 : 1),
-                       f32 ? c->L32 : c->L64, g, c->nbx, c->nby, c->nbz, c->bmin, c->st));
+          // the band feature (per-block field minimum) moves little once the
+          // scheduler runs: it is refreshed every kBandEvery scheduled sweeps
+          if (band_sweep < 0 || s - band_sweep >= kBandEvery) {
+            CK(block_min(f32 ? (const void *)c->u32 : (const void *)c->u64,
+                         f32 ? 0 : (o.arith == PDFS_ARITH_PAIR ? 2 : 1), f32 ? c->L32 : c->L64, g, c->nbx, c->nby,
+                         c->nbz, c->bmin, c->st));
+            band_sweep = s;
+            c->launches++;
+          }
           CK(sched_learned(c->mlp_w, c->mlp_thr, c->bchg, cur, std::min(s, kHist), c->bmin, c->nbx, c->nby,
                            c->nbz, sn, s, f32 ? 0 : 1, thr, (float)std::min(g.dx, std::min(g.dy, g.dz)), c->bact,
                            &c->dstat->active_blocks, &c->dstat->sched_err, c->sms, c->st));
-          c->launches += 2;
+          c->launches++;
         } else {
           CK(sched_change(c->bchg, cur, std::min(s, kHist), thr, c->bact, c->nbx, c->nby, c->nbz,
                           &c->dstat->active_blocks, c->sms, c->st));
