@@ -603,6 +603,29 @@ def main():
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"{sweeps} FP64 orderings of the full grid ({dt:.1f} s): {what}"}
 
+    # the reference's own CUDA solver beside the CPU baseline: its sweep kernel
+    # built unmodified from its sources (a cubin), its host level loop (one
+    # launch per hyperplane, a device synchronisation after each), one
+    # run_fsm round of the 8 orderings on the same input
+    ref_gpu = None
+    if rank == 0 and not args.no_cpu and args.fixed_sweeps == 0:
+        from oracle import oracle as O
+        if O.have_ref_cuda("nvcc"):
+            try:
+                ms_sw, ms_all = O.ref_cuda_run(w.field.copy(), sp, first=1, nsweeps=8, sync_each=True)
+                ms_q, _ = O.ref_cuda_run(w.field.copy(), sp, first=1, nsweeps=8, sync_each=False)
+                per = ms_sw / 8
+                ref_gpu = {"kernel": "fast_sweep_kernel (single_gpu_cuda/src/phi3D_fsm.cu), nvcc defaults, sm_103a",
+                           "ms_per_sweep": per, "ms_per_sweep_no_level_sync": ms_q / 8,
+                           "round_ms_with_copies": ms_all,
+                           "gvox_updates_per_s": w.interior * 8 / (ms_sw / 1e3) / 1e9,
+                           "time_to_converge_s_est": per * plain_sweeps / 1e3,
+                           "ours_speedup": per * plain_sweeps / 1e3 / t_step}
+            except Exception as e:
+                ref_gpu = {"unavailable": str(e)[:200]}
+        else:
+            ref_gpu = {"unavailable": "the reference's CUDA kernel was not built (no reference sources at build time)"}
+
     if rank == 0:
         dtype = {L.ARITH_PAIR: "f32+f32pair", L.ARITH_MIXED: "f32+f64mixed"}.get(arith, "f32+f64") \
             if prec == L.PREC_FP32_POLISH64 else ("f32" if prec == L.PREC_FP32 else "f64")
@@ -622,7 +645,7 @@ def main():
             "speedup_vs_plain_fp64": (plain["time_s"] / t_step) if plain else None,
             "fp64_polish": fp64_polish,
             "roofline": roof, "roofline_fp32_sweep": fp32_roof, "schedulers": sched_table,
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(sum(s["launches"] for s in stats)),
+            "cpu_baseline": cpu, "reference_gpu": ref_gpu, "e2e": e2e, "gpu_launches": int(sum(s["launches"] for s in stats)),
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

@@ -1,10 +1,14 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
-Two libraries:
+Libraries:
   * oracle/_build/liboracle.so  -- this project's C restatement of the FSM
     (fsm_oracle.c), built by `make -C oracle`; available on every machine.
   * oracle/_ref/libref_fsm.so   -- the reference's own mpi_openacc/src/phi3D_fsm.c,
     built unmodified by `make -C oracle ref` where the reference sources exist.
+  * oracle/_ref/ref_fsm_cuda*.cubin -- the reference's own CUDA sweep kernel
+    (single_gpu_cuda/src/phi3D_fsm.cu), built unmodified by `make -C oracle
+    refcu`, and oracle/_build/libref_cuda.so (ref_cuda_host.c), the host
+    level loop that runs it on a GPU through the driver API.
 
 Only tests, the smoke check and the benchmark's CPU-baseline leg import this
 module, and only as the checker.
@@ -21,6 +25,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref_fsm.so")
 REF_OMP_PATH = os.path.join(HERE, "_ref", "libref_fsm_omp.so")
+REF_CUBIN = {"nvcc": os.path.join(HERE, "_ref", "ref_fsm_cuda.cubin"),
+             "nofma": os.path.join(HERE, "_ref", "ref_fsm_cuda_nofma.cubin")}
+RC_PATH = os.path.join(HERE, "_build", "libref_cuda.so")
 
 
 def ref_root() -> str:
@@ -50,8 +57,14 @@ _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 
 def build(ref: bool = True) -> None:
     subprocess.run(["make", "-s", "-C", HERE], check=True)
+    # the host driver of the reference's CUDA kernel: needs only the CUDA
+    # toolkit's header and driver stub, so it builds wherever the library does
+    if os.path.exists(os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include", "cuda.h")):
+        subprocess.run(["make", "-s", "-C", HERE, "cudahost"], check=True)
     if ref and os.path.isdir(ref_src()):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_ROOT=" + ref_root()], check=True)
+        if os.path.isdir(os.path.join(ref_root(), "single_gpu_cuda", "src")):
+            subprocess.run(["make", "-s", "-C", HERE, "refcu", "REF_ROOT=" + ref_root()], check=True)
 
 
 def lib():
@@ -164,3 +177,44 @@ def ref_solve(u, spacing, tol=0.0, max_sweeps=10_000, omp=False):
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+# ---------------- the reference's own CUDA kernel (single_gpu_cuda) ----------------
+_rc = {"lib": None, "cubin": None}
+
+
+def have_ref_cuda(variant: str = "nvcc") -> bool:
+    """True where the reference's CUDA kernel was built (oracle/_ref) and its
+    host driver too; the GPU itself is checked by ref_cuda_run."""
+    return os.path.exists(REF_CUBIN[variant]) and os.path.exists(RC_PATH)
+
+
+def _rc_lib(variant: str):
+    if _rc["lib"] is None:
+        L = C.CDLL(RC_PATH)
+        L.rc_error.restype = C.c_char_p
+        L.rc_open.argtypes = [C.c_char_p]
+        L.rc_run.argtypes = ([_dp] + [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int] * 3 +
+                             [C.POINTER(C.c_double)] * 2)
+        _rc["lib"] = L
+    L = _rc["lib"]
+    if _rc["cubin"] != variant:
+        if L.rc_open(REF_CUBIN[variant].encode()) != 0:
+            raise RuntimeError("reference CUDA kernel: " + L.rc_error().decode())
+        _rc["cubin"] = variant
+    return L
+
+
+def ref_cuda_run(u, spacing, first=1, nsweeps=8, sync_each=True, variant="nvcc"):
+    """nsweeps orderings from `first` (the reference's run_fsm round is 1, 8)
+    by the reference's own CUDA kernel and level loop, in place on u (the
+    reference layout).  variant "nvcc": built as the reference's Makefile
+    builds it; "nofma": without multiply-add contraction.  Returns
+    (sweep ms on the device, whole-call ms)."""
+    nx, ny, nz = _dims(u)
+    L = _rc_lib(variant)
+    a, b = C.c_double(0.0), C.c_double(0.0)
+    r = L.rc_run(u, nx, ny, nz, *spacing, int(first), int(nsweeps), 1 if sync_each else 0, C.byref(a), C.byref(b))
+    if r != 0:
+        raise RuntimeError("reference CUDA kernel: " + L.rc_error().decode())
+    return a.value, b.value

@@ -1,0 +1,96 @@
+"""The reference's own CUDA solver on the GB300: its sweep kernel
+(single_gpu_cuda/src/phi3D_fsm.cu:199-295), compiled unmodified from the
+reference's sources into a cubin (`make -C oracle refcu`), run by the host
+level loop of oracle/ref_cuda_host.c (phi3D_fsm.cu:127-190 restated on the
+driver API).
+
+  * Built without multiply-add contraction, it gives the CPU reference's bits:
+    every ordering, and one run_fsm round, equal the oracle (the restatement
+    pinned to the reference's phi3D_fsm.c) and this library's FP64 solve in
+    the reference arithmetic.
+  * Built as the reference's Makefile builds it (nvcc's default contraction),
+    it differs from them only by rounding, bounded here.
+
+The cubins travel with the repository's built files; where they were not
+built (no reference tree on the build machine) the tests are skipped."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pdfs_gb300 import _lib as L
+from pdfs_gb300 import api
+from pdfs_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def need(variant):
+    if not O.have_ref_cuda(variant):
+        pytest.skip("the reference's CUDA kernel was not built (oracle/_ref/ref_fsm_cuda*.cubin)")
+
+
+def same(a, b):
+    """Bit-exact, every NaN counted as one value (the reference arithmetic
+    turns far nodes into NaN on anisotropic grids, and NaN sign bits differ
+    between devices)."""
+    na, nb = np.isnan(a), np.isnan(b)
+    return bool(np.array_equal(na, nb) and a[~na].tobytes() == b[~nb].tobytes())
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+@pytest.mark.parametrize("sn", range(1, 9))
+def test_each_ordering_equals_oracle(sn, aniso):
+    need("nofma")
+    sp = (0.7, 1.0, 0.5) if aniso else (1.0, 1.0, 1.0)
+    w = W.random_spheres(37, 29, 23, *sp, 4, 1.5, 8.0, seed=20 + sn)
+    a = w.field.copy()
+    O.ref_cuda_run(a, sp, first=sn, nsweeps=1, variant="nofma")
+    b = w.field.copy()
+    O.sweep(b, sp, sn)
+    assert same(a, b), f"ordering {sn}"
+
+
+def test_run_fsm_round_c1_equals_oracle_and_library():
+    """The reference program's own call, run_fsm(pf, 1) (phi3D.c:118-119): one
+    round of the 8 orderings on the 64^3 sphere workload."""
+    need("nofma")
+    w = W.config("C1")
+    sp = (w.dx, w.dy, w.dz)
+    a = w.field.copy()
+    ms, _ = O.ref_cuda_run(a, sp, first=1, nsweeps=8, variant="nofma")
+    b = w.field.copy()
+    for sn in range(1, 9):
+        O.sweep(b, sp, sn)
+    assert same(a, b)
+    c = w.field.copy()
+    api.solve(c, sp, precision=L.PREC_FP64, arith=L.ARITH_REFERENCE, fixed_sweeps=8)
+    assert same(a, c)
+    assert ms > 0.0
+
+
+def test_reference_build_within_rounding():
+    """nvcc's default contraction of the expanded quadratic changes only
+    rounding: within 1e-12 relative of the CPU reference after a round."""
+    need("nvcc")
+    w = W.config("C1")
+    sp = (w.dx, w.dy, w.dz)
+    a = w.field.copy()
+    O.ref_cuda_run(a, sp, first=1, nsweeps=8, variant="nvcc")
+    b = w.field.copy()
+    for sn in range(1, 9):
+        O.sweep(b, sp, sn)
+    i = (slice(1, -1),) * 3
+    err = float(np.max(np.abs(a[i] - b[i]) / np.maximum(np.abs(b[i]), min(sp))))
+    assert err <= 1e-12, err
+
+
+def test_queued_launches_equal_synchronised():
+    """Without the per-level synchronisation the launches still run in
+    stream order: the same bits."""
+    need("nvcc")
+    w = W.random_spheres(40, 33, 27, 1.0, 1.0, 1.0, 3, 2.0, 8.0, seed=31)
+    sp = (w.dx, w.dy, w.dz)
+    a, b = w.field.copy(), w.field.copy()
+    O.ref_cuda_run(a, sp, first=3, nsweeps=5, sync_each=True)
+    O.ref_cuda_run(b, sp, first=3, nsweeps=5, sync_each=False)
+    assert a.tobytes() == b.tobytes()
