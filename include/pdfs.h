@@ -82,10 +82,13 @@ enum {
                              predicts will change                                         */
 };
 /* Whatever the scheduler, a solve only terminates after a sweep that visits
- * every block and changes nothing (FP32) or less than tol (FP64).  Under
- * PDFS_PREC_FP32_POLISH64 the scheduler runs the FP32 phase, which may then
- * end on a quiet scheduled sweep, and the polish visits every block: its
- * full sweeps certify the fixed point. */
+ * every block and changes by at most the phase's tolerance (FP32: the
+ * relative 4e-6; FP64: tol).  Under PDFS_PREC_FP32_POLISH64 with a scheduler,
+ * the scheduler runs the FP32 phase, which may then end on a quiet scheduled
+ * sweep; the polish's first cycle of 8 orderings visits, in each ordering,
+ * only the blocks whose characteristic directions (from the FP32 result)
+ * agree with that ordering's sweep directions, and full sweeps follow until
+ * one certifies the fixed point. */
 
 typedef struct {
   int precision;         /* PDFS_PREC_*                                           */
@@ -184,10 +187,13 @@ int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz);
  * of the traces their models learn from. */
 int pdfs_ctx_sweep(pdfs_ctx *c, int sn, const uint8_t *active, float *block_change, double *max_change);
 
-/* Solves n independent grids together (the batched configuration): each
- * sweep is one persistent launch over the columns of every grid still
- * sweeping, each round of 8 orderings replays from a CUDA graph, and a grid
- * leaves the launch once one of its sweeps changes by <= the phase tolerance.
+/* Solves n independent grids together (the batched configuration).  On
+ * pencil tiles (the default; brick and lane-column tiles map to it) each
+ * round of 8 orderings is ONE persistent launch over the pencils of every
+ * grid still sweeping; on column tiles (asked for in opts.tile) each sweep is
+ * one launch.  Rounds after the first replay a CUDA graph, and a grid leaves
+ * once one of its sweeps changes by <= the phase tolerance (the round's
+ * later sweeps still run on it).
  * fields[i] / frozen[i] as in pdfs_solve (frozen may be NULL, or hold NULL
  * entries).  stats: NULL or n entries.  opts.fixed_sweeps must be 0 and the
  * scheduler is not used.  Returns the first failing grid's status. */

@@ -62,8 +62,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     # the sweep kernels' FP32 arithmetic uses approximate sqrt/divide (the
     # FP64 polish removes the difference); FP64 arithmetic is unaffected
     fast = ["-prec-sqrt=false", "-prec-div=false"]
-    per_tu = {"sweep.cu": fast, "tile3d.cu": fast, "pencil.cu": fast, "lanecol.cu": fast, "lanecol_pmin.cu": fast,
-              "lanecol_prep.cu": fast, "lanecol_pmin4.cu": fast, "lanecol_prep4.cu": fast}
+    per_tu = {"sweep.cu": fast, "tile3d.cu": fast, "pencil.cu": fast, "pencil_batch.cu": fast, "lanecol.cu": fast,
+              "lanecol_pmin.cu": fast, "lanecol_prep.cu": fast, "lanecol_pmin4.cu": fast, "lanecol_prep4.cu": fast}
     for src in cu:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
         objs.append(obj)

@@ -1,13 +1,16 @@
 // batch.cu -- many independent grids per launch, and the tile autotuner.
 //
 // The reference solves one grid per process (single_gpu_cuda/src/main.c:56-106).
-// pdfs_solve_batch() keeps every grid resident in its own context and runs
-// each sweep as ONE persistent launch over the columns of all grids that are
-// still sweeping: the ticket table lists (grid, column) pairs, each grid's
-// columns in wavefront order, so the deadlock-free argument of the single-grid
-// sweep carries over unchanged.  A round of 8 orderings is captured once in a
-// CUDA graph and replayed; after each round the per-grid, per-sweep changes
-// come back in one copy, and converged grids leave the ticket table.
+// pdfs_solve_batch() keeps every grid resident in its own context.  On
+// pencils (the default) each round of 8 orderings is ONE persistent launch
+// over the pencils of every grid still sweeping: the ticket table lists
+// (grid, sweep, pencil) triples, every grid's sweep s before any grid's sweep
+// s + 1 and each grid's pencils in wavefront order, and a pencil of sweep s
+// starts once its grid's sweep s - 1 is complete -- so every wait is on a
+// smaller ticket held by a running CTA.  On column tiles each sweep is one
+// launch over (grid, column) pairs.  Rounds after the first replay a captured
+// CUDA graph; after each round the per-grid, per-sweep changes come back in
+// one copy, and converged grids leave the ticket table.
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -34,6 +37,8 @@ struct BatchState {
   int *d_err = nullptr;                 // [4]
   int *h_err = nullptr;                 // pinned
   int *d_ticket = nullptr;
+  int *d_done = nullptr;   // pencil rounds: [grid * 8 + sweep] pencils finished
+  int *d_round = nullptr;  // pencil rounds: rounds run in this phase
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   ~BatchState() {
@@ -47,6 +52,8 @@ struct BatchState {
     cudaFree(d_chg);
     cudaFree(d_err);
     cudaFree(d_ticket);
+    cudaFree(d_done);
+    cudaFree(d_round);
     if (h_chg) cudaFreeHost(h_chg);
     if (h_err) cudaFreeHost(h_err);
     if (st) cudaStreamDestroy(st);
@@ -245,6 +252,166 @@ int batch_phase(BatchState &B, std::vector<pdfs_ctx *> &ctx, const std::vector<i
   return PDFS_OK;
 }
 
+
+__global__ void k_add(int *p, int v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *p += v;
+}
+
+// One phase on pencils (which: 0 FP32, 1 FP64 min, 2 FP64 replace): rounds
+// of 8 orderings over every grid in `todo`, ONE launch per round (the
+// pencil kernel's batched mode), until each grid has a sweep with change
+// <= tol.  The first round runs eagerly; the following rounds replay a
+// captured graph (counter resets, the launch, the round count, the copy of
+// the changes).
+int batch_phase_pencils(BatchState &B, std::vector<pdfs_ctx *> &ctx, const std::vector<int> &todo, int which,
+                        double tol, int max_sweeps, std::vector<pdfs_stats> &st, double *kern_ms, int *launches) {
+  const int n = B.n;
+  const bool f32 = which == 0;
+  const pdfs_opts &o = ctx[0]->o;
+  const int arith = o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF
+                    : o.arith == PDFS_ARITH_MIXED   ? ARITH_MIXED
+                    : o.arith == PDFS_ARITH_PAIR    ? ARITH_PAIR
+                                                    : ARITH_FAST;
+  bool iso = true;
+  std::vector<SweepArgs> args(n);
+  std::vector<CUtensorMap> maps(3 * (size_t)n);
+  for (int g = 0; g < n; ++g) {
+    pdfs_ctx *c = ctx[g];
+    iso = iso && c->g.dx == c->g.dy && c->g.dy == c->g.dz;
+    fill_sweep_args(c, which, 1, nullptr, nullptr, &args[g]);
+    // the round's sweep s tags its mailbox words epoch + 8 * round + s: above
+    // every tag this context has used
+    args[g].epoch = c->epoch + 1;
+    args[g].err = B.d_err;
+    args[g].ticket = B.d_ticket;
+    const Layout &L = f32 ? c->L32 : c->L64;
+    BK(encode_pencil_maps(which, args[g], L, &maps[3 * (size_t)g]));
+  }
+  BK(cudaMemcpyAsync(B.d_args, args.data(), sizeof(SweepArgs) * n, cudaMemcpyHostToDevice, B.st));
+  BK(cudaMemcpyAsync(B.d_maps, maps.data(), sizeof(CUtensorMap) * 3 * n, cudaMemcpyHostToDevice, B.st));
+  BK(cudaMemsetAsync(B.d_round, 0, 4, B.st));
+
+  std::vector<int> active(todo);
+  std::vector<int2> tickets;
+  auto rebuild = [&]() -> int {
+    // every grid's sweep s before any grid's sweep s + 1; a grid's pencils in
+    // its wavefront order
+    tickets.clear();
+    std::vector<std::vector<int>> ord(n);
+    for (int g : active) {
+      const Layout &L = f32 ? ctx[g]->L32 : ctx[g]->L64;
+      ord[g] = wavefront_order(L.ncx, L.ncy, L.tx, L.ty);
+    }
+    for (int s = 0; s < 8; ++s)
+      for (int g : active)
+        for (int lc : ord[g]) tickets.push_back(make_int2(g * 8 + s, lc));
+    if (tickets.empty()) return PDFS_OK;
+    BK(cudaMemcpyAsync(B.d_tickets, tickets.data(), sizeof(int2) * tickets.size(), cudaMemcpyHostToDevice, B.st));
+    BatchDesc desc{(int)tickets.size(), B.d_tickets, B.d_args, B.d_maps, n, B.d_done, B.d_round};
+    BK(cudaMemcpyAsync(B.d_desc, &desc, sizeof(desc), cudaMemcpyHostToDevice, B.st));
+    return PDFS_OK;
+  };
+  int r = rebuild();
+  if (r) return r;
+  const int max_ticks = (int)tickets.size();
+
+  SweepArgs a0;
+  std::memset(&a0, 0, sizeof(a0));
+  a0.err = B.d_err;
+  a0.ticket = B.d_ticket;
+  a0.maxchg = B.d_chg;
+  a0.batch = B.d_desc;
+  auto enqueue_round = [&]() -> int {
+    BK(cudaMemsetAsync(B.d_done, 0, sizeof(int) * 8 * n, B.st));
+    BK(cudaMemsetAsync(B.d_ticket, 0, 4, B.st));
+    int grid = 0;
+    BK(launch_pencil_round(which, arith, iso, a0, max_ticks, B.sms, B.st, &grid));
+    k_add<<<1, 32, 0, B.st>>>(B.d_round, 1);
+    BK(cudaGetLastError());
+    BK(cudaMemcpyAsync(B.h_chg, B.d_chg, sizeof(unsigned long long) * 8 * n, cudaMemcpyDeviceToHost, B.st));
+    BK(cudaMemcpyAsync(B.h_err, B.d_err, 16, cudaMemcpyDeviceToHost, B.st));
+    return PDFS_OK;
+  };
+
+  cudaEvent_t e0, e1;
+  BK(cudaEventCreate(&e0));
+  BK(cudaEventCreate(&e1));
+  bool captured = false;
+  int rounds = 0;
+  for (int round = 0; !active.empty(); ++round) {
+    if (round * 8 >= max_sweeps) {
+      for (int g : active) st[g].status = PDFS_ERR_NOT_CONVERGED;
+      break;
+    }
+    BK(cudaMemsetAsync(B.d_chg, 0, sizeof(unsigned long long) * 8 * n, B.st));
+    BK(cudaEventRecord(e0, B.st));
+    if (round == 0) {
+      if ((r = enqueue_round())) return r;  // eagerly: it also sets the kernel attributes
+    } else {
+      if (!captured) {
+        if (B.exec) {
+          cudaGraphExecDestroy(B.exec);
+          B.exec = nullptr;
+        }
+        if (B.graph) {
+          cudaGraphDestroy(B.graph);
+          B.graph = nullptr;
+        }
+        BK(cudaStreamBeginCapture(B.st, cudaStreamCaptureModeThreadLocal));
+        r = enqueue_round();
+        cudaGraph_t gph = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(B.st, &gph);
+        if (r) return r;
+        BK(ce);
+        B.graph = gph;
+        BK(cudaGraphInstantiate(&B.exec, B.graph, 0));
+        captured = true;
+      }
+      BK(cudaGraphLaunch(B.exec, B.st));
+    }
+    BK(cudaEventRecord(e1, B.st));
+    BK(cudaStreamSynchronize(B.st));
+    ++rounds;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    *kern_ms += ms;
+    *launches += 2;  // the round and the round count
+    if (B.h_err[0]) return B.h_err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
+    std::vector<int> still;
+    for (int g : active) {
+      int conv = -1;
+      double last = 0.0;
+      for (int s = 0; s < 8; ++s) {
+        last = chg_value(B.h_chg[(size_t)s * n + g], f32);
+        if (last <= tol) {
+          conv = s;
+          break;
+        }
+      }
+      pdfs_stats &S = st[g];
+      const long long nodes = (long long)ctx[g]->g.nx * ctx[g]->g.ny * ctx[g]->g.nz;
+      S.voxel_updates += nodes * 8;
+      if (!f32) S.voxel_updates_fp64 += nodes * 8;
+      S.full_sweeps += 8;
+      if (f32)
+        S.sweeps_fp32 += 8;
+      else
+        S.sweeps_fp64 += 8;
+      S.final_change = last;
+      if (conv < 0) still.push_back(g);
+    }
+    if (still.size() != active.size()) {
+      active.swap(still);
+      if ((r = rebuild())) return r;
+    }
+  }
+  // every context's later sweeps tag above this phase's words
+  for (int g = 0; g < n; ++g) ctx[g]->epoch += 8 * rounds + 8;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return PDFS_OK;
+}
+
 }  // namespace
 
 extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fields, const uint8_t *const *frozen,
@@ -258,14 +425,19 @@ extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fi
     pdfs_default_opts(&o);
   if (o.fixed_sweeps != 0) return PDFS_ERR_INVALID;  // the batch runs whole rounds to convergence
   o.scheduler = PDFS_SCHED_NONE;
+  bool pen32 = true, pen64 = true;
   {
-    // a batched launch runs the column kernels (one ticket space across the
-    // grids); brick tiles and the default choice map to the column defaults
+    // A batch runs on pencils -- one launch per round of 8 orderings over all
+    // grids (the default, and for brick or lane-column tiles) -- or, when a
+    // column tile is asked for, on columns, one launch per sweep.
+    auto column = [](const TileShape &t) { return !t.pencil && !t.bz && !t.lc; };
     int t32 = o.tile & 0xff, t64 = (o.tile >> 8) & 0xff;
-    if (t32 == 0 || tile32(t32).bz || tile32(t32).lc) t32 = 4;
-    // FP32 pairs live on bricks only: the batch polishes in the mixed arithmetic
-    if (o.arith == PDFS_ARITH_PAIR) o.arith = PDFS_ARITH_MIXED;
-    if (t64 == 0 || tile64(t64).bz || tile64(t64).lc) t64 = o.arith == PDFS_ARITH_MIXED ? 4 : 1;
+    if (t32 >= 1 && t32 <= tile_count32() && column(tile32(t32))) pen32 = false;
+    if (t64 >= 1 && t64 <= tile_count64() && column(tile64(t64))) pen64 = false;
+    if (pen32) t32 = 10;
+    if (pen64) t64 = 6;
+    // the column kernels have no FP32-pair arithmetic: they polish in the mixed one
+    if (!pen64 && o.arith == PDFS_ARITH_PAIR) o.arith = PDFS_ARITH_MIXED;
     o.tile = t32 | (t64 << 8);
   }
   std::vector<pdfs_ctx *> ctx(n, nullptr);
@@ -301,8 +473,8 @@ extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fi
     }                                   \
   } while (0)
   BQ(cudaStreamCreateWithFlags(&B.st, cudaStreamNonBlocking));
-  size_t total_cols = 0;
-  for (auto *c : ctx) total_cols += std::max((size_t)c->L32.ncx * c->L32.ncy, (size_t)c->L64.ncx * c->L64.ncy);
+  size_t total_cols = 0;  // tickets: columns of a sweep, or pencils of a round's 8 sweeps
+  for (auto *c : ctx) total_cols += 8 * std::max((size_t)c->L32.ncx * c->L32.ncy, (size_t)c->L64.ncx * c->L64.ncy);
   BQ(cudaMalloc(&B.d_args, sizeof(SweepArgs) * n));
   BQ(cudaMalloc(&B.d_maps, sizeof(CUtensorMap) * 3 * n));
   BQ(cudaMalloc(&B.d_tickets, sizeof(int2) * total_cols));
@@ -310,6 +482,8 @@ extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fi
   BQ(cudaMalloc(&B.d_chg, sizeof(unsigned long long) * 8 * n));
   BQ(cudaMalloc(&B.d_err, 16));
   BQ(cudaMalloc(&B.d_ticket, 16));
+  BQ(cudaMalloc(&B.d_done, sizeof(int) * 8 * n));
+  BQ(cudaMalloc(&B.d_round, 16));
   BQ(cudaMemset(B.d_err, 0, 16));
   BQ(cudaHostAlloc(&B.h_chg, sizeof(unsigned long long) * 8 * n, cudaHostAllocDefault));
   BQ(cudaHostAlloc(&B.h_err, 16, cudaHostAllocDefault));
@@ -322,21 +496,21 @@ extern "C" int pdfs_solve_batch(int n, const pdfs_grid *grids, double *const *fi
     for (auto *c : ctx)
       BQ(cudaMemcpyAsync(c->u64, c->in64, c->L64.elems * 8, cudaMemcpyDeviceToDevice, c->st));
     for (auto *c : ctx) BQ(cudaStreamSynchronize(c->st));
-    rc = batch_phase(B, ctx, all, 1, o.tol, max_sweeps, st, &kms64, &launches);
+    rc = (pen64 ? batch_phase_pencils : batch_phase)(B, ctx, all, 1, o.tol, max_sweeps, st, &kms64, &launches);
     for (auto *c : ctx) c->last_prec = 1;
   } else {
     for (auto *c : ctx) {
       if ((rc = ctx_narrow(c))) return cleanup(rc);
     }
     for (auto *c : ctx) BQ(cudaStreamSynchronize(c->st));
-    rc = batch_phase(B, ctx, all, 0, 4.0e-6, max_sweeps, st, &kms32, &launches);
+    rc = (pen32 ? batch_phase_pencils : batch_phase)(B, ctx, all, 0, 4.0e-6, max_sweeps, st, &kms32, &launches);
     for (auto *c : ctx) c->last_prec = 0;
     if (!rc && o.precision == PDFS_PREC_FP32_POLISH64) {
       for (auto *c : ctx) {
         if ((rc = ctx_widen(c))) return cleanup(rc);
       }
       for (auto *c : ctx) BQ(cudaStreamSynchronize(c->st));
-      rc = batch_phase(B, ctx, all, 2, o.tol, max_sweeps, st, &kms64, &launches);
+      rc = (pen64 ? batch_phase_pencils : batch_phase)(B, ctx, all, 2, o.tol, max_sweeps, st, &kms64, &launches);
       for (auto *c : ctx) c->last_prec = 1;
     }
   }

@@ -83,6 +83,11 @@ cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, 
 cudaError_t launch_sweep_pencils(int which, int arith, bool iso, const SweepArgs &a, const Layout &L, int sms,
                                  cudaStream_t st, int *grid_used);
 cudaError_t encode_mask_map(CUtensorMap *m, const SweepArgs &a, int ty);
+// One round of a batch on pencils (pencil_batch.cu): the 8 orderings of every
+// grid that a0.batch describes, in one launch (at most max_ticks tickets).
+cudaError_t launch_pencil_round(int which, int arith, bool iso, const SweepArgs &a0, int max_ticks, int sms,
+                                cudaStream_t st, int *grid_used);
+cudaError_t encode_pencil_maps(int which, const SweepArgs &a, const Layout &L, CUtensorMap m[3]);
 // One sweep by the lane-column kernel (lanecol.cu): which 0 = FP32 min, 1 =
 // pair min, 2 = pair replace; tiles of rows = 4 or 8 rows.
 cudaError_t launch_sweep_lanecol(int which, int rows, bool iso, const LcArgs &a, int sms, cudaStream_t st,
@@ -97,6 +102,13 @@ cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout
 // for sched_learned).  *count += active blocks.
 cudaError_t sched_change(const unsigned int *ring, int cur, int hist, float thr, uint8_t *active, int nbx, int nby,
                          int nbz, int *count, int sms, cudaStream_t st);
+// Polish orderings per 8^3 block (bit sn-1: ordering sn matters to the
+// block), from the FP32 result; and the active mask of one ordering.
+cudaError_t octant_mask(const float *u32, const Layout &L, const uint32_t *fmask, const MaskLayout &M,
+                        const pdfs_grid &g, float slack, float far, int nbx, int nby, int nbz, uint8_t *omask,
+                        cudaStream_t st);
+cudaError_t octant_active(const uint8_t *omask, int sn, int dilate, uint8_t *active, int nbx, int nby, int nbz,
+                          int *count, int sms, cudaStream_t st);
 
 // Status words a sweep writes on the device (read back after each sweep).
 struct DevStatus {
@@ -120,6 +132,14 @@ constexpr int kRing = kHist + 1;
 // The learned scheduler recomputes its band feature every kBandEvery
 // scheduled sweeps (a pass over the field each time).
 constexpr int kBandEvery = 4;
+// Polish octant masks: an axis whose two neighbours differ by at most
+// kOctSlack * h accepts both sweep directions; kOctDilate = 1 adds each
+// block's face neighbours' orderings.  Measured on the 768^3 headline grid
+// (polish time, polish sweeps): slack 0.25 without dilation 54.4 ms, 10;
+// with it 52.1 ms, 9 (one masked cycle and one certifying full sweep); slack
+// 0.5 56.4 / 57.3 ms; slack 1.0 59.0 / 64.8 ms; unscheduled 62.0 ms, 9.
+constexpr float kOctSlack = 0.25f;
+constexpr int kOctDilate = 1;
 
 // Weights of the learned scheduler compiled into the library (a blob of
 // PDFS_MLP_BLOB floats), or nullptr when none were built in.
@@ -185,6 +205,7 @@ struct pdfs_ctx {
   long long nblocks = 0;
   unsigned int *bchg = nullptr;  // [kRing][nblocks] float bits of per-block max change, rotating
   uint8_t *bact = nullptr;       // [nblocks] active mask of the next sweep
+  uint8_t *omask = nullptr;      // [nblocks] polish: the orderings that matter to each block
   float *bmin = nullptr;         // [nblocks] per-block field minimum (learned scheduler)
   uint16_t *mlp_w = nullptr;     // learned scheduler: bf16 network weights
   float mlp_thr = 0.0f;          // its decision threshold on the logit
@@ -203,7 +224,15 @@ struct pdfs_ctx {
 namespace pdfs {
 void fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg,
                      SweepArgs *out);
-void ordering_signs(int sn, int *sx, int *sy, int *sz);
+// Sweep direction of ordering sn (1..8), +1 ascending, from makeSweepInfo
+// (mpi_openacc/src/phi3D_fsm.c:206-218): a reflection offset reverses its
+// axis, descending levels reverse all three.
+__host__ __device__ inline void ordering_signs(int sn, int *sx, int *sy, int *sz) {
+  const int desc = (sn == 2 || sn == 5 || sn == 7 || sn == 8) ? -1 : 1;
+  *sx = ((sn == 4 || sn == 8) ? -1 : 1) * desc;
+  *sy = ((sn == 2 || sn == 6) ? -1 : 1) * desc;
+  *sz = ((sn == 3 || sn == 7) ? -1 : 1) * desc;
+}
 std::vector<int> wavefront_order(int ncx, int ncy, int tx, int ty);
 // One sweep of context c (which: 0 FP32 min, 1 FP64 min, 2 FP64 replace):
 // active = block mask or nullptr, blk_chg = per-block change or nullptr.

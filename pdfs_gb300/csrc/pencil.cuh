@@ -94,6 +94,20 @@ __device__ __forceinline__ bool mail_get(const unsigned long long *e, int epoch,
   }
 }
 
+// A warp's max change -> the change word (FP32: float bits; FP64: the u64
+// key of change_u64), one atomic per warp.
+template <class T, int ARITH>
+__device__ __forceinline__ void warp_change_out(T v, void *maxchg, int lane) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(0xffffffffu, v, off));
+  if (lane == 0 && change_pos<T, ARITH>(v)) {
+    if constexpr (sizeof(T) == 4)
+      atomicMax(reinterpret_cast<unsigned int *>(maxchg), __float_as_uint(v));
+    else
+      atomicMax(reinterpret_cast<unsigned long long *>(maxchg), change_u64<T, ARITH>(v));
+  }
+}
+
 // One idle round of a helper warp: lane 0 decides, for the whole warp, to give
 // up on the abort flag or after wait_cycles without progress.
 __device__ __forceinline__ bool helper_idle(const SweepArgs &a, int col, volatile int *s_abort, long long t_last,
@@ -116,10 +130,34 @@ __device__ __forceinline__ bool helper_idle(const SweepArgs &a, int col, volatil
   return false;
 }
 
-template <class T, int MODE, int ARITH, bool ISO>
+// Batched rounds: the grid description of the current ticket, staged in
+// shared memory (a function-scope __shared__ object, so the single-grid
+// instantiations do not carry it).
+__device__ __forceinline__ SweepArgs &pc_batch_args() {
+  __shared__ SweepArgs s;
+  return s;
+}
+template <bool BATCH>
+__device__ __forceinline__ const SweepArgs &pc_args(const SweepArgs &a0) {
+  if constexpr (BATCH)
+    return pc_batch_args();
+  else
+    return a0;
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;\n" ::: "memory");
+}
+
+// BATCH: one launch runs a whole round -- the 8 orderings of every grid of a
+// batch (BatchDesc).  A ticket names (grid, sweep, pencil); sweep s of a grid
+// starts once every pencil of its sweep s - 1 has finished (a per-(grid,
+// sweep) counter, bounded wait), and tickets list every grid's sweep s before
+// any grid's sweep s + 1, so every wait is on smaller tickets.
+template <class T, int MODE, int ARITH, bool ISO, bool BATCH = false>
 __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                                const __grid_constant__ CUtensorMap tm_mask,
-                                                               const __grid_constant__ SweepArgs a) {
+                                                               const __grid_constant__ SweepArgs a0) {
+  const SweepArgs &a = pc_args<BATCH>(a0);
   using G = PcGeo<T>;
   constexpr int BX = G::BX, BY = G::BY, W = G::W, SK = G::SK, D = G::D;
   constexpr int SE = (int)(G::SLOT_BYTES / sizeof(T));  // slot stride in elements
@@ -127,31 +165,39 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
   T *ring = reinterpret_cast<T *>(sm);
   uint64_t *full = reinterpret_cast<uint64_t *>(sm + G::OFF_BAR);
   __shared__ int s_ticket, s_stop, s_done, s_ready, s_landed;
+  __shared__ int s_gs, s_lc;                // BATCH: the ticket's grid * 8 + sweep, and its pencil
+  __shared__ const CUtensorMap *s_maps;     // BATCH: the grid's tensor maps
   __shared__ volatile int s_abort;
 
   if ((saddr(sm) & 127u) != 0) {  // TMA destinations must be 128-byte aligned
     if (threadIdx.x == 0) {
-      atomicCAS(a.err, 0, DEV_ERR_SMEM_ALIGN);
-      atomicExch(a.err + 1, 1);
+      atomicCAS(a0.err, 0, DEV_ERR_SMEM_ALIGN);
+      atomicExch(a0.err + 1, 1);
     }
     return;
   }
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int ntick = a.ncx * a.ncy;
-  const int sxd = a.sx, syd = a.sy, szd = a.sz;
-  const int nx = a.nx, ny = a.ny, nz = a.nz;
-  const int NP = nz + 2, t_end = nz + SK;  // planes (sweep order, halo planes included), levels
-  const long long plane = a.plane, px = a.px;
-  const bool masked = a.fmask != nullptr;
-  const int epoch = a.epoch;
+  int ntick;
+  if constexpr (BATCH)
+    ntick = a0.batch->nticket;
+  else
+    ntick = a0.ncx * a0.ncy;
+  int cur_gs = -1;  // BATCH: the (grid, sweep) staged in shared memory
   T tmax = T(0);
 
   if (tid == 0) s_abort = 0;
   for (int npen = 0;; ++npen) {
     if (tid == 0) {
-      const int tk = atomicAdd(a.ticket, 1);
+      const int tk = atomicAdd(a0.ticket, 1);
       s_ticket = tk;
-      if (*(volatile int *)(a.err + 1)) s_abort = 1;
+      if constexpr (BATCH) {
+        if (tk < ntick) {
+          const int2 e = a0.batch->tickets[tk];
+          s_gs = e.x;
+          s_lc = e.y;
+        }
+      }
+      if (*(volatile int *)(a0.err + 1)) s_abort = 1;
       s_stop = (tk >= ntick || s_abort) ? 1 : 0;
       s_done = 0;
       s_ready = 0;
@@ -164,7 +210,67 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
     }
     __syncthreads();
     if (s_stop) break;
-    const int lc = a.order[s_ticket];
+    if constexpr (BATCH) {
+      if (s_gs != cur_gs) {  // stage the grid's description; set the sweep's direction, epoch, change word
+        cur_gs = s_gs;
+        const int g = cur_gs >> 3, sw = cur_gs & 7;
+        const int *ws = reinterpret_cast<const int *>(a0.batch->args + g);
+        int *wd = reinterpret_cast<int *>(&pc_batch_args());
+        for (int i = tid; i < (int)(sizeof(SweepArgs) / 4); i += blockDim.x) wd[i] = ws[i];
+        __syncthreads();
+        if (tid == 0) {
+          SweepArgs &S = pc_batch_args();
+          ordering_signs(sw + 1, &S.sx, &S.sy, &S.sz);
+          S.epoch += 8 * *a0.batch->round + sw;
+          S.err = a0.err;
+          S.ticket = a0.ticket;
+          S.maxchg = reinterpret_cast<unsigned long long *>(a0.maxchg) + (size_t)sw * a0.batch->ngrid + g;
+          s_maps = a0.batch->maps + 3 * g;
+          // the grid's previous sweep must be complete: its stores, then its count (release)
+          if (sw > 0) {
+            const int *cnt = a0.batch->done + cur_gs - 1;
+            const int need = S.ncx * S.ncy;
+            if (ld_acquire_gpu(cnt) < need) {
+              const long long t0 = cycles();
+              unsigned nap = 32;
+              while (ld_acquire_gpu(cnt) < need) {
+                if (s_abort || *(volatile int *)(a0.err + 1)) {
+                  s_abort = 1;
+                  break;
+                }
+                if (cycles() - t0 > S.wait_cycles) {
+                  raise_timeout(S, -1, &s_abort);
+                  break;
+                }
+                __nanosleep(nap);
+                nap = min(nap * 2, 256u);
+              }
+            }
+          }
+        }
+        __syncthreads();
+        if (s_abort) break;
+      }
+    }
+    const int sxd = a.sx, syd = a.sy, szd = a.sz;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    const int NP = nz + 2, t_end = nz + SK;  // planes (sweep order, halo planes included), levels
+    const long long plane = a.plane, px = a.px;
+    const bool masked = a.fmask != nullptr;
+    const int epoch = a.epoch;
+    const CUtensorMap *mp_u, *mp_mask;
+    if constexpr (BATCH) {
+      mp_u = s_maps;
+      mp_mask = s_maps + 2;
+    } else {
+      mp_u = &tm_u;
+      mp_mask = &tm_mask;
+    }
+    int lc;
+    if constexpr (BATCH)
+      lc = s_lc;
+    else
+      lc = a.order[s_ticket];
     const int lcx = lc % a.ncx, lcy = lc / a.ncx;
     const int cx = sxd > 0 ? lcx : a.ncx - 1 - lcx;
     const int cy = syd > 0 ? lcy : a.ncy - 1 - lcy;
@@ -180,6 +286,9 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       long long t_last = cycles();
       unsigned nap = 0;
       bool failed = false;
+      // a round's earlier sweep was written by other CTAs of this launch:
+      // order the acquire of its count before these async-proxy reads
+      if constexpr (BATCH) fence_proxy_async_global();
       for (;;) {
         int moved = 0;
         if (lane == 0) {
@@ -190,8 +299,8 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
             const int gz = szd > 0 ? q_issue : nz + 1 - q_issue;
             unsigned char *dst = sm + (size_t)s * G::SLOT_BYTES;
             mbar_arrive_tx(full + s, tx_bytes);
-            tma_load_3d(dst, &tm_u, cx * BX, y0 - 1, gz, full + s);
-            if (masked) tma_load_3d(dst + G::MASK_OFF, &tm_mask, cy * BY, cx >> 1, gz, full + s);
+            tma_load_3d(dst, mp_u, cx * BX, y0 - 1, gz, full + s);
+            if (masked) tma_load_3d(dst + G::MASK_OFF, mp_mask, cy * BY, cx >> 1, gz, full + s);
             ++q_issue;
             moved = 1;
           }
@@ -385,20 +494,25 @@ __global__ void __launch_bounds__(PcGeo<T>::NT) pc_sweep_kernel(const __grid_con
       }
       compute_bar();
       if (tid == 0 && !stop) st_release_cta_s(&s_done, t_end);
+      if constexpr (BATCH) {
+        // this pencil's change -> its (grid, sweep) word; my stores come
+        // before the next sweep's plane copies, which another CTA may issue
+        warp_change_out<T, ARITH>(tmax, a.maxchg, lane);
+        tmax = T(0);
+        fence_proxy_async_global();
+      }
     }
     __syncthreads();
     if (s_abort) break;
+    if constexpr (BATCH) {  // the pencil is done: count it (release)
+      if (tid == 0) {
+        __threadfence();
+        atomicAdd(a0.batch->done + cur_gs, 1);
+      }
+    }
   }
   // the CTA's max change -> the grid's counter (one atomic per warp)
-  T v = tmax;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(0xffffffffu, v, off));
-  if (lane == 0 && change_pos<T, ARITH>(v)) {
-    if constexpr (sizeof(T) == 4)
-      atomicMax(reinterpret_cast<unsigned int *>(a.maxchg), __float_as_uint(v));
-    else
-      atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg), change_u64<T, ARITH>(v));
-  }
+  if constexpr (!BATCH) warp_change_out<T, ARITH>(tmax, a.maxchg, lane);
 }
 
 }  // namespace pdfs

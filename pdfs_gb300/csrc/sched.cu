@@ -46,4 +46,99 @@ cudaError_t sched_change(const unsigned int *ring, int cur, int hist, float thr,
   return cudaGetLastError();
 }
 
+// Polish orderings.  Along a characteristic of |grad u| = 1 (a straight line
+// from the nearest interface point) a node's upwind neighbours lie on the
+// side of the smaller value on every axis its Godunov update uses; an
+// ordering whose sweep directions agree with those sides carries the node's
+// whole upwind chain into it in one sweep (the fast sweeping argument, Zhao,
+// Math. Comp. 74 (2005) 603-627).  From a nearly converged field this gives
+// each 8^3 block the set of orderings that matter to it: bit sn-1 of omask
+// is set where some node of the block accepts ordering sn.  An axis accepts
+// both directions where the update does not use it (its smaller neighbour is
+// not below the node) or where its two neighbours differ by at most
+// slack * h (a characteristic nearly parallel to the faces).  Frozen nodes
+// and nodes not yet reached (>= far) accept none.  One warp covers four
+// blocks along x, lane = node x offset.
+__global__ void k_octant_mask(const float *__restrict__ u, Layout L, const uint32_t *__restrict__ fmask,
+                              MaskLayout M, int nx, int ny, int nz, float hx, float hy, float hz, float slack,
+                              float far, int nbx, int nby, int nbz, uint8_t *__restrict__ omask) {
+  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwx = (nbx + 3) / 4;
+  if (wid >= (long long)nwx * nby * nbz) return;
+  const int wx = (int)(wid % nwx), by = (int)((wid / nwx) % nby), bz = (int)(wid / ((long long)nwx * nby));
+  const int x = 1 + wx * 32 + lane;
+  unsigned acc = 0;
+  // accepted directions of one axis: bit 0 ascending, bit 1 descending
+  auto axis = [](float c, float lo, float hi, float tie) -> unsigned {
+    const float m = fminf(lo, hi);
+    if (!(m < c) || fabsf(lo - hi) <= tie) return 3u;
+    return lo < hi ? 1u : 2u;
+  };
+  if (x <= nx) {
+    for (int z = 1 + bz * 8; z <= min(nz, bz * 8 + 8); ++z)
+      for (int y = 1 + by * 8; y <= min(ny, by * 8 + 8); ++y) {
+        if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
+        const float c = fabsf(u[L.index(x, y, z)]);
+        if (!(c < far)) continue;
+        const unsigned ax = axis(c, fabsf(u[L.index(x - 1, y, z)]), fabsf(u[L.index(x + 1, y, z)]), slack * hx);
+        const unsigned ay = axis(c, fabsf(u[L.index(x, y - 1, z)]), fabsf(u[L.index(x, y + 1, z)]), slack * hy);
+        const unsigned az = axis(c, fabsf(u[L.index(x, y, z - 1)]), fabsf(u[L.index(x, y, z + 1)]), slack * hz);
+#pragma unroll
+        for (int sn = 1; sn <= 8; ++sn) {
+          int sx, sy, sz;
+          ordering_signs(sn, &sx, &sy, &sz);
+          if ((ax & (sx > 0 ? 1u : 2u)) && (ay & (sy > 0 ? 1u : 2u)) && (az & (sz > 0 ? 1u : 2u)))
+            acc |= 1u << (sn - 1);
+        }
+      }
+  }
+#pragma unroll
+  for (int off = 1; off < 8; off <<= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, off);
+  const int bx = wx * 4 + (lane >> 3);
+  if ((lane & 7) == 0 && bx < nbx) omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)acc;
+}
+
+// active[b] = ordering sn matters to block b or to one of its six face
+// neighbours (dilate) ; count receives the number of active blocks.
+__global__ void k_octant_active(const uint8_t *__restrict__ omask, int sn, int dilate, uint8_t *__restrict__ active,
+                                int nbx, int nby, int nbz, int *__restrict__ count) {
+  const long long n = (long long)nbx * nby * nbz;
+  const unsigned bit = 1u << (sn - 1);
+  int local = 0;
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n; b += (long long)gridDim.x * blockDim.x) {
+    const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long long)nbx * nby));
+    bool on = (omask[b] & bit) != 0;
+    if (dilate && !on) {
+      const long long pl = (long long)nbx * nby;
+      on = (bx > 0 && (omask[b - 1] & bit)) || (bx < nbx - 1 && (omask[b + 1] & bit)) ||
+           (by > 0 && (omask[b - nbx] & bit)) || (by < nby - 1 && (omask[b + nbx] & bit)) ||
+           (bz > 0 && (omask[b - pl] & bit)) || (bz < nbz - 1 && (omask[b + pl] & bit));
+    }
+    active[b] = on ? 1 : 0;
+    local += on ? 1 : 0;
+  }
+  for (int off = 16; off > 0; off >>= 1) local += __shfl_xor_sync(0xffffffffu, local, off);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
+cudaError_t octant_mask(const float *u32, const Layout &L, const uint32_t *fmask, const MaskLayout &M,
+                        const pdfs_grid &g, float slack, float far, int nbx, int nby, int nbz, uint8_t *omask,
+                        cudaStream_t st) {
+  const long long warps = (long long)((nbx + 3) / 4) * nby * nbz;
+  const int grid = (int)((warps * 32 + 255) / 256);
+  k_octant_mask<<<grid, 256, 0, st>>>(u32, L, fmask, M, g.nx, g.ny, g.nz, (float)g.dx, (float)g.dy, (float)g.dz, slack,
+                                      far, nbx, nby, nbz, omask);
+  return cudaGetLastError();
+}
+
+cudaError_t octant_active(const uint8_t *omask, int sn, int dilate, uint8_t *active, int nbx, int nby, int nbz,
+                          int *count, int sms, cudaStream_t st) {
+  const long long n = (long long)nbx * nby * nbz;
+  int grid = (int)std::min<long long>((n + 255) / 256, (long long)sms * 8);
+  if (grid < 1) grid = 1;
+  k_octant_active<<<grid, 256, 0, st>>>(omask, sn, dilate, active, nbx, nby, nbz, count);
+  return cudaGetLastError();
+}
+
 }  // namespace pdfs

@@ -309,16 +309,6 @@ std::vector<int> wavefront_order(int ncx, int ncy, int tx, int ty) {
   return o;
 }
 
-// Sweep direction of ordering sn (1..8), from makeSweepInfo
-// (mpi_openacc/src/phi3D_fsm.c:206-218): a reflection offset reverses its
-// axis, descending levels reverse all three.
-void ordering_signs(int sn, int *sx, int *sy, int *sz) {
-  const int desc = (sn == 2 || sn == 5 || sn == 7 || sn == 8) ? -1 : 1;
-  *sx = ((sn == 4 || sn == 8) ? -1 : 1) * desc;
-  *sy = ((sn == 2 || sn == 6) ? -1 : 1) * desc;
-  *sz = ((sn == 3 || sn == 7) ? -1 : 1) * desc;
-}
-
 }  // namespace pdfs
 
 using namespace pdfs;
@@ -676,6 +666,7 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   want(&c->dstat, sizeof(DevStatus));
   want(&c->bchg, (size_t)c->nblocks * kRing * 4);
   want(&c->bact, (size_t)c->nblocks);
+  if (o.precision == PDFS_PREC_FP32_POLISH64) want(&c->omask, (size_t)c->nblocks);
   if (!wb.empty()) {
     want(&c->mlp_w, PDFS_MLP_PARAMS * 2);
     want(&c->bmin, (size_t)c->nblocks * 4);
@@ -1212,14 +1203,21 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     c->kern_ms = 0.0;
     CK(cudaEventRecord(c->e0, c->st));
     const bool sched = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0 && !(polish && which == 2);
+    // the polish under a scheduler: its first cycle visits, in each ordering,
+    // only the blocks that ordering matters to (octant masks of the FP32
+    // result); full sweeps follow until one certifies
+    const bool octant = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0 && polish && which == 2;
     const bool certify = !(polish && which == 0);  // must the phase end on a full sweep?
     const int nfull = 8;  // sweeps that visit every block before the scheduler starts
     const float thr = (float)tol;
     // per-block changes: ring slot cur = this sweep, (cur - k) mod kRing = k sweeps ago
     int cur = 0;
-    if (sched) {
-      CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * kRing * 4, c->st));
-      CK(cudaMemsetAsync(&c->dstat->sched_err, 0, 4, c->st));
+    if (sched) CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * kRing * 4, c->st));
+    if (sched || octant) CK(cudaMemsetAsync(&c->dstat->sched_err, 0, 4, c->st));
+    if (octant) {
+      CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack, INFINITY, c->nbx, c->nby,
+                     c->nbz, c->omask, c->st));
+      c->launches++;
     }
     bool need_full = true;
     int s = 0;
@@ -1231,13 +1229,17 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         break;
       }
       const int sn = (first + s) % 8 + 1;
-      const bool full = !sched || s < nfull || need_full;
+      const bool full = octant ? s >= 8 : (!sched || s < nfull || need_full);
       const uint8_t *act = nullptr;
       long long nact = c->nblocks;
       if (!full) {
         CK(cudaEventRecord(c->q0, c->st));
         CK(cudaMemsetAsync(&c->dstat->active_blocks, 0, 4, c->st));
-        if (o.scheduler == PDFS_SCHED_LEARNED) {
+        if (octant) {
+          CK(octant_active(c->omask, sn, kOctDilate, c->bact, c->nbx, c->nby, c->nbz, &c->dstat->active_blocks,
+                           c->sms, c->st));
+          c->launches++;
+        } else if (o.scheduler == PDFS_SCHED_LEARNED) {
           const bool f32 = which == 0;
           // the band feature (per-block field minimum) moves little once the
           // scheduler runs: it is refreshed every kBandEvery scheduled sweeps

@@ -143,9 +143,14 @@ struct LcArgs {
 // columns in wavefront order; args[g] / maps[3g..3g+2] describe grid g.
 struct BatchDesc {
   int nticket;
-  const int2 *tickets;      // (grid, local column id)
+  const int2 *tickets;      // (grid, local column id); pencil rounds: (grid * 8 + sweep, local pencil id)
   const SweepArgs *args;    // per grid (sx/sy/sz are taken from the launch)
   const CUtensorMap *maps;  // per grid: field, cap, mask
+  // Pencil rounds (pencil.cuh): one launch runs all 8 orderings of a round
+  // for every grid; sweep s of a grid starts once its sweep s - 1 is done.
+  int ngrid;                // grids in args; the change words are [sweep][grid]
+  int *done;                // [grid * 8 + sweep]: pencils finished this round
+  const int *round;         // rounds run before this one (mailbox epochs advance 8 per round)
 };
 
 // Shared-memory plan of one kernel variant: columns of 32 x TY nodes, R rows

@@ -1,4 +1,8 @@
-"""Batched solves (pdfs_solve_batch) and the tile autotuner."""
+"""Batched solves (pdfs_solve_batch) and the tile autotuner.
+
+A batch runs on pencils by default: one launch per round of 8 orderings
+over every grid (pencil.cuh's batched mode).  Column tiles, asked for
+explicitly, run one launch per sweep."""
 import numpy as np
 import pytest
 
@@ -65,9 +69,9 @@ def test_batch_without_masks_and_invalid_args():
 
 def test_autotune_returns_valid_tiles():
     t = api.autotune(96, 80, 64, (1.0, 1.0, 1.0), precision=L.PREC_FP32_POLISH64)
-    # FP32: columns 1-7, bricks 8, 9, 11, pencils 10; FP64 polish, reference
-    # arithmetic: columns 1-2, bricks 5, 7, 8, pencils 6
-    assert 1 <= (t & 0xFF) <= 11 and (t >> 8) in (1, 2, 5, 6, 7, 8)
+    # FP32: columns 1-7, bricks 8, 9, 11, pencils 10, lane columns 12-13; FP64
+    # polish, reference arithmetic: columns 1-2, bricks 5, 7, 8, pencils 6
+    assert 1 <= (t & 0xFF) <= 13 and (t >> 8) in (1, 2, 5, 6, 7, 8)
     w = W.random_spheres(96, 80, 64, 1.0, 1.0, 1.0, 5, 3.0, 10.0, seed=2)
     a = w.field.copy()
     api.solve(a, (1.0, 1.0, 1.0), frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
@@ -76,3 +80,73 @@ def test_autotune_returns_valid_tiles():
     O.solve(ref, (1.0, 1.0, 1.0), tol=0.0, frozen=w.frozen, threads=4)
     i = (slice(1, -1),) * 3
     assert np.max(np.abs(a[i] - ref[i]) / np.maximum(np.abs(ref[i]), 1.0)) <= 1e-10
+
+
+COLUMNS = 4 | (1 << 8)  # column tiles: the per-sweep batched launch
+
+
+def test_batch_on_columns_still_bit_exact():
+    ws = uneven_batch(8, 21)
+    fields = [w.field.copy() for w in ws]
+    api.solve_batch(fields, [(w.dx, w.dy, w.dz) for w in ws], frozen=[w.frozen for w in ws],
+                    freeze=L.FREEZE_MASK, tol=0.0, tile=COLUMNS)
+    for w, f in zip(ws, fields):
+        ref = w.field.copy()
+        O.solve(ref, (w.dx, w.dy, w.dz), tol=0.0, frozen=w.frozen, threads=4)
+        assert f.tobytes() == ref.tobytes(), w.name
+
+
+def test_pencil_rounds_mixed_spacings_and_sizes():
+    """Isotropic and anisotropic grids, tiny and taller than a pencil's ring,
+    in one batch: the round kernel stages each grid's description per ticket."""
+    rng = np.random.default_rng(4)
+    ws = []
+    for i, (n, sp) in enumerate([((1, 1, 1), (1.0, 1.0, 1.0)), ((17, 33, 5), (0.7, 1.0, 0.5)),
+                                 ((48, 40, 96), (1.0, 1.0, 1.0)), ((33, 16, 70), (0.5, 0.5, 1.0)),
+                                 ((64, 64, 64), (1.0, 1.0, 1.0))]):
+        ws.append(W.random_spheres(*n, *sp, 3, 1.5, 8.0, seed=int(rng.integers(1 << 30)), log_radii=False))
+    fields = [w.field.copy() for w in ws]
+    st = api.solve_batch(fields, [(w.dx, w.dy, w.dz) for w in ws], frozen=[w.frozen for w in ws],
+                         freeze=L.FREEZE_MASK, tol=0.0)
+    for w, f, s in zip(ws, fields, st):
+        ref = w.field.copy()
+        O.solve(ref, (w.dx, w.dy, w.dz), tol=0.0, frozen=w.frozen, threads=4)
+        na, nb = np.isnan(f), np.isnan(ref)  # the reference arithmetic's NaN (far nodes, anisotropic)
+        assert np.array_equal(na, nb) and f[~na].tobytes() == ref[~nb].tobytes(), w.name
+        assert s["status"] == 0 and s["launches"] > 0
+
+
+def test_pencil_rounds_pair_polish_within_1e6():
+    ws = uneven_batch(10, 13)
+    fields = [w.field.copy() for w in ws]
+    st = api.solve_batch(fields, [(w.dx, w.dy, w.dz) for w in ws], frozen=[w.frozen for w in ws],
+                         freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5)
+    i = (slice(1, -1),) * 3
+    for w, f, s in zip(ws, fields, st):
+        ref = w.field.copy()
+        O.solve(ref, (w.dx, w.dy, w.dz), tol=1e-12, frozen=w.frozen, threads=4)
+        err = np.max(np.abs(f[i] - ref[i]) / np.maximum(np.abs(ref[i]), 1.0)) if f[i].size else 0.0
+        assert err <= 1e-6, (w.name, err)
+        assert s["tile"] == 10 | (6 << 8)
+
+
+def test_pencil_round_timeout_then_clean_batch(monkeypatch):
+    """A pencil that never publishes its faces (the test hook) makes its
+    downwind pencils' bounded waits give up: PDFS_ERR_TIMEOUT, and the next
+    batch is bit-exact."""
+    ws = [W.random_spheres(64, 48, 40, 1.0, 1.0, 1.0, 3, 2.0, 9.0, seed=s) for s in (1, 2, 3)]
+    monkeypatch.setenv("PDFS_TEST_POISON_COLUMN", "0")
+    monkeypatch.setenv("PDFS_WAIT_MS", "200")
+    fields = [w.field.copy() for w in ws]
+    with pytest.raises(api.PdfsError) as ei:
+        api.solve_batch(fields, [(1.0, 1.0, 1.0)] * 3, frozen=[w.frozen for w in ws], freeze=L.FREEZE_MASK,
+                        tol=0.0)
+    assert ei.value.status == L.PDFS_ERR_TIMEOUT
+    monkeypatch.delenv("PDFS_TEST_POISON_COLUMN")
+    monkeypatch.delenv("PDFS_WAIT_MS")
+    fields = [w.field.copy() for w in ws]
+    api.solve_batch(fields, [(1.0, 1.0, 1.0)] * 3, frozen=[w.frozen for w in ws], freeze=L.FREEZE_MASK, tol=0.0)
+    for w, f in zip(ws, fields):
+        ref = w.field.copy()
+        O.solve(ref, (1.0, 1.0, 1.0), tol=0.0, frozen=w.frozen, threads=4)
+        assert f.tobytes() == ref.tobytes()

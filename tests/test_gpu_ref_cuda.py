@@ -9,7 +9,8 @@ driver API).
     pinned to the reference's phi3D_fsm.c) and this library's FP64 solve in
     the reference arithmetic.
   * Built as the reference's Makefile builds it (nvcc's default contraction),
-    it differs from them only by rounding, bounded here.
+    it reaches the same fixed point to rounding; after the reference
+    program's single round, which is not converged, it differs more.
 
 The cubins travel with the repository's built files; where they were not
 built (no reference tree on the build machine) the tests are skipped."""
@@ -68,19 +69,22 @@ def test_run_fsm_round_c1_equals_oracle_and_library():
     assert ms > 0.0
 
 
-def test_reference_build_within_rounding():
-    """nvcc's default contraction of the expanded quadratic changes only
-    rounding: within 1e-12 relative of the CPU reference after a round."""
+def test_reference_build_converges_to_the_same_fixed_point():
+    """nvcc's default contraction of the expanded quadratic changes rounding,
+    and with it Godunov branch decisions at near-ties: after the reference
+    program's single round (run_fsm(pf, 1), 8 sweeps, far from converged on
+    this grid: the oracle needs 22) the two builds differ at some nodes by
+    more than 10% (measured 0.137 relative).  From two rounds on, and at the
+    fixed point, they agree to rounding (measured 1.3e-14)."""
     need("nvcc")
     w = W.config("C1")
     sp = (w.dx, w.dy, w.dz)
+    ref = w.field.copy()
+    n, _ = O.solve(ref, sp, tol=0.0)
     a = w.field.copy()
-    O.ref_cuda_run(a, sp, first=1, nsweeps=8, variant="nvcc")
-    b = w.field.copy()
-    for sn in range(1, 9):
-        O.sweep(b, sp, sn)
+    O.ref_cuda_run(a, sp, first=1, nsweeps=8 * ((n + 7) // 8 + 1), variant="nvcc")
     i = (slice(1, -1),) * 3
-    err = float(np.max(np.abs(a[i] - b[i]) / np.maximum(np.abs(b[i]), min(sp))))
+    err = float(np.max(np.abs(a[i] - ref[i]) / np.maximum(np.abs(ref[i]), min(sp))))
     assert err <= 1e-12, err
 
 
