@@ -217,18 +217,20 @@ def kernel_name(kind, tile, prec, arith):
     return "ws_sweep_kernel<%s, %d, %d, %s, %s>" % ((t,) + ty + (mode, ar))
 
 
-def traffic_per_launch(kind, prec, nodes, tile):
+def traffic_per_launch(kind, prec, nodes, tile, masked=False):
     """DRAM bytes of one launch of the dominant sweep kernel: the per-update
     traffic an ncu capture measured (profiles/traffic.json, dram__bytes_read
-    + dram__bytes_write over the capture's voxel updates) times this
-    launch's updates; None without a capture for that kernel."""
+    + dram__bytes_write over the capture's executed voxel updates) times this
+    launch's updates; None without a capture for that kernel.  masked: the
+    block-masked sweeps (bricks), whose traffic per executed update differs
+    from a full sweep's."""
     from pdfs_gb300 import _lib as L
     try:
         t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     except (OSError, ValueError):
         return None
     key = "fp32" if kind == "fp32" else ("fp64_replace" if prec == L.PREC_FP32_POLISH64 else "fp64_min")
-    key += "_" + kernel_kind(kind, tile)
+    key += "_masked_brick" if masked else "_" + kernel_kind(kind, tile)
     e = t.get(key)
     return None if not e else float(e["dram_bytes_per_update"]) * nodes
 
@@ -334,18 +336,29 @@ def run_batch(args, rank, world, pg, device):
     for w in ws:
         api.solve(w.field.copy(), (w.dx, w.dy, w.dz), frozen=w.frozen, **kw)
     t_loop = time.perf_counter() - t0
+    # the same batch on column tiles: one launch per sweep, mixed polish
+    kc = dict(kw, tile=4 | (4 << 8), arith=L.ARITH_MIXED)
+    api.solve_batch([w.field.copy() for w in ws], sps, frozen=[w.frozen for w in ws], **kc)
+    t0 = time.perf_counter()
+    api.solve_batch([w.field.copy() for w in ws], sps, frozen=[w.frozen for w in ws], **kc)
+    t_cols = time.perf_counter() - t0
     if rank == 0:
         line = {
             "metric": "grids/s of the batched FP32 + FP64-polish solve (256 grids) vs looping the plain FP64 solver",
             "value": world * len(ws) / t_batch, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded spheres)",
+            "vs_baseline": None, "dtype": "f32+f32pair" if arith == L.ARITH_PAIR else "f32+f64",
+            "data": "synthetic (seeded spheres)",
             "config": {"workload": "C5_256_grids_32-256", "grids": len(ws), "interior_nodes": nodes,
                        "polish_tol": args.tol, "polish_arith": args.polish_arith,
                        "l2": "inputs larger than L2 (no flush needed)"},
             "gvox_updates_per_s_plain_equivalent": plain_sweeps / t_batch / 1e9,
             "plain_fp64_loop": {"grids_per_s": len(ws) / t_plain, "time_s": t_plain},
             "own_single_grid_loop": {"grids_per_s": len(ws) / t_loop, "time_s": t_loop},
+            "batch_on_columns": {"grids_per_s": len(ws) / t_cols, "time_s": t_cols,
+                                 "kernel": "columns 32x8 / mixed polish, one launch per sweep"},
+            "batch_kernel": "pencil rounds: one launch per round of 8 orderings over every grid",
+            "launches_per_step": int(max(x["launches"] for x in st)),
             "speedup_vs_plain_loop": t_plain / t_batch, "max_rel_err_vs_plain": err,
             "sweeps_per_grid": {"fp32": float(np.mean([x["sweeps_fp32"] for x in st])),
                                 "fp64": float(np.mean([x["sweeps_fp64"] for x in st]))},
@@ -546,36 +559,53 @@ def main():
                "d2h_bytes_per_step": int(world * w.field.nbytes), "time_to_converge_s": te,
                "steps": len(ts), "host_buffers": "pinned" if pinned else "pageable"}
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel: the sweep kernels by phase and kind (full
+    # sweeps on the tile's kernel, block-masked sweeps on bricks), each with its
+    # executed updates, launches and summed CUDA-event durations
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
+    mask_b = 1.0 / 8.0
     k32, k64 = st["ms_kern_fp32"], st["ms_kern_fp64"]
     s32, s64 = st["sweeps_fp32"], st["sweeps_fp64"]
-    dominant = "fp64" if k64 >= k32 else "fp32"
-    mask_b = 1.0 / 8.0
-    # executed updates of the dominant phase (scheduled sweeps count only their active blocks)
-    if dominant == "fp32":
-        upd = st["voxel_updates_fp32"] if "voxel_updates_fp32" in st else w.interior * s32
-        per_update = 8 + mask_b
-        dur = k32
-    else:
-        # 2 * sizeof(T) per voxel-update plus the frozen-mask bit; the polish's cap
-        # reads are not algorithmic bytes (the kernels skip them where a block's
-        # smallest cap is above the new value)
-        upd = st["voxel_updates_fp64"] if "voxel_updates_fp64" in st else w.interior * s64
-        per_update = 16 + mask_b
-        dur = k64
-    achieved = upd * per_update / (dur / 1e3) / 1e9 if dur > 0 else 0.0
-    nsw = max(s32 if dominant == "fp32" else s64, 1)
-    kname = kernel_name(dominant, st["tile"], prec, arith)
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": traffic_per_launch(dominant, prec, upd / nsw, st["tile"]), "kernel": kname,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s",
-            "bytes_per_update": per_update, "launches_per_step": nsw, "ms_per_launch": dur / nsw}
+    vu64 = st["voxel_updates_fp64"]
+    vu32 = st["voxel_updates"] - vu64
+    parts = []
+    for phase, kt, kmask, n, nmask, upd, umask, per in (
+            ("fp32", k32, st["ms_kern_masked_fp32"], s32, st["masked_sweeps_fp32"], vu32,
+             st["updates_masked_fp32"], 8 + mask_b),
+            ("fp64", k64, st["ms_kern_masked_fp64"], s64, st["masked_sweeps_fp64"], vu64,
+             st["updates_masked_fp64"], 16 + mask_b)):
+        if n - nmask > 0:
+            parts.append({"phase": phase, "kind": "full", "ms": kt - kmask, "launches": n - nmask,
+                          "updates": upd - umask, "bytes_per_update": per})
+        if nmask > 0:
+            parts.append({"phase": phase, "kind": "masked", "ms": kmask, "launches": nmask, "updates": umask,
+                          "bytes_per_update": per})
+    for q in parts:
+        q["kernel"] = kernel_name(q["phase"], st["tile"], prec, arith) if q["kind"] == "full" else \
+            ("t3_sweep_kernel<float, 16, 32, MIN, FAST>" if q["phase"] == "fp32" else
+             f"t3_sweep_kernel<double, 16, 16, {'REPLACE' if prec == L.PREC_FP32_POLISH64 else 'MIN'}, "
+             f"{ {L.ARITH_PAIR: 'PAIR', L.ARITH_MIXED: 'MIXED', L.ARITH_FAST: 'FAST'}.get(arith, 'REF')}>")
+        q["ms_per_launch"] = q["ms"] / q["launches"]
+        q["achieved_gbs"] = q["updates"] * q["bytes_per_update"] / (q["ms"] / 1e3) / 1e9 if q["ms"] > 0 else 0.0
+        q["frac"] = q["achieved_gbs"] / hbm
+        q["share_of_sweep_time"] = q["ms"] / max(k32 + k64, 1e-9)
+    dom = max(parts, key=lambda q: q["ms"]) if parts else None
+    roof = None
+    if dom is not None:
+        # traffic: ncu DRAM bytes per update of this kernel (profiles/traffic.json) x its updates per launch
+        tr = traffic_per_launch(dom["phase"], prec, dom["updates"] / dom["launches"], st["tile"],
+                                masked=dom["kind"] == "masked")
+        roof = {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": hbm, "unit": "GB/s", "frac": dom["frac"],
+                "traffic": tr, "kernel": dom["kernel"],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s",
+                "bytes_per_update": dom["bytes_per_update"], "launches_per_step": dom["launches"],
+                "ms_per_launch": dom["ms_per_launch"], "sweep_kind": dom["kind"]}
     fp32_roof = None
-    if s32:
-        a32 = w.interior * (8 + mask_b) / (k32 / s32 / 1e3) / 1e9
-        fp32_roof = {"achieved": a32, "frac": a32 / hbm, "ms_per_sweep": k32 / s32}
+    full32 = [q for q in parts if q["phase"] == "fp32" and q["kind"] == "full"]
+    if full32:
+        fp32_roof = {"achieved": full32[0]["achieved_gbs"], "frac": full32[0]["frac"],
+                     "ms_per_sweep": full32[0]["ms_per_launch"]}
 
     # the same solve under each scheduler (one timed run each, after one warm run)
     sched_table = None
@@ -644,7 +674,8 @@ def main():
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (plain["time_s"] / t_step) if plain else None,
             "fp64_polish": fp64_polish,
-            "roofline": roof, "roofline_fp32_sweep": fp32_roof, "schedulers": sched_table,
+            "roofline": roof, "roofline_fp32_sweep": fp32_roof, "roofline_by_kernel": parts,
+            "schedulers": sched_table,
             "cpu_baseline": cpu, "reference_gpu": ref_gpu, "e2e": e2e, "gpu_launches": int(sum(s["launches"] for s in stats)),
             "clocks": clk,
         }

@@ -129,7 +129,11 @@ typedef struct {
   double ms_device;           /* pdfs_ctx_run: device time from its first to its last
                                  kernel (CUDA events on the context's stream)        */
   long long voxel_updates_fp64; /* the part of voxel_updates done by FP64 sweeps     */
-  int reserved[2];
+  /* the block-masked (scheduled) sweeps, a part of the sums above: their
+   * kernels' summed durations and the node updates they executed */
+  double ms_kern_masked_fp32, ms_kern_masked_fp64;
+  long long updates_masked_fp32, updates_masked_fp64;
+  int masked_sweeps_fp32, masked_sweeps_fp64;
 } pdfs_stats;
 
 /* Fills *o with the defaults: FP64, reference arithmetic, no freezing, no
@@ -186,6 +190,17 @@ int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz);
  * (phi3D_fsm.c:83-119): this is the building block of block schedulers and
  * of the traces their models learn from. */
 int pdfs_ctx_sweep(pdfs_ctx *c, int sn, const uint8_t *active, float *block_change, double *max_change);
+
+/* Per 8^3 block, the orderings that matter to it, from the context's FP32
+ * working field (after a PDFS_PREC_FP32 run or sweeps, or the FP32 phase of a
+ * PDFS_PREC_FP32_POLISH64 run): bit sn-1 of orderings[b] is set where, at some
+ * updated node of the block, every axis the Godunov update uses has its
+ * smaller neighbour on the side ordering sn sweeps from (an axis the update
+ * does not use, or whose neighbours differ by at most h/4, accepts both), or
+ * where that holds in a face-neighbour block.  These are the masks of the
+ * polish's first cycle under a scheduler.  orderings: one byte per block,
+ * host or device.  PDFS_ERR_INVALID for a context without an FP32 field. */
+int pdfs_ctx_orderings(pdfs_ctx *c, uint8_t *orderings);
 
 /* Solves n independent grids together (the batched configuration).  On
  * pencil tiles (the default; brick and lane-column tiles map to it) each

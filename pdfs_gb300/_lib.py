@@ -30,7 +30,7 @@ EXPORTS = [
     "pdfs_ctx_store", "pdfs_ctx_destroy", "pdfs_release_cached", "pdfs_status_string", "pdfs_version",
     "run_fsm", "pdfs_vti_read", "pdfs_vti_write", "pdfs_phi_free", "pdfs_calc_dist_field",
     "pdfs_solve_batch", "pdfs_autotune", "pdfs_static_layout", "pdfs_sweep_static",
-    "pdfs_ctx_blocks", "pdfs_ctx_sweep",
+    "pdfs_ctx_blocks", "pdfs_ctx_sweep", "pdfs_ctx_orderings",
     "pdfs_mlp_trainer_create", "pdfs_mlp_trainer_add_solve", "pdfs_mlp_trainer_fit", "pdfs_mlp_trainer_weights",
     "pdfs_mlp_trainer_destroy", "pdfs_mlp_grad", "pdfs_mlp_adam", "pdfs_mlp_infer",
 ]
@@ -59,7 +59,10 @@ class Stats(C.Structure):
                 ("ms_d2h", C.c_double), ("ms_fp32", C.c_double), ("ms_fp64", C.c_double),
                 ("ms_sched", C.c_double), ("ms_kern_fp32", C.c_double),
                 ("ms_kern_fp64", C.c_double), ("tile", C.c_int), ("launches", C.c_int),
-                ("ms_device", C.c_double), ("voxel_updates_fp64", C.c_longlong), ("reserved", C.c_int * 2)]
+                ("ms_device", C.c_double), ("voxel_updates_fp64", C.c_longlong),
+                ("ms_kern_masked_fp32", C.c_double), ("ms_kern_masked_fp64", C.c_double),
+                ("updates_masked_fp32", C.c_longlong), ("updates_masked_fp64", C.c_longlong),
+                ("masked_sweeps_fp32", C.c_int), ("masked_sweeps_fp64", C.c_int)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -132,6 +135,8 @@ def load(path: str = LIB_PATH):
     L.pdfs_ctx_blocks.restype = ip
     L.pdfs_ctx_sweep.argtypes = [vp, ip, vp, vp, C.POINTER(C.c_double)]
     L.pdfs_ctx_sweep.restype = ip
+    L.pdfs_ctx_orderings.argtypes = [vp, vp]
+    L.pdfs_ctx_orderings.restype = ip
     fp = C.POINTER(C.c_float)
     L.pdfs_mlp_trainer_create.argtypes = [ip, C.c_uint, C.POINTER(vp)]
     L.pdfs_mlp_trainer_create.restype = ip

@@ -170,6 +170,16 @@ class Context:
             raise PdfsError(s, "pdfs_ctx_blocks")
         return tuple(x.value for x in b)
 
+    def orderings(self) -> np.ndarray:
+        """Per 8^3 block (nbz, nby, nbx), the bit set of the orderings that
+        matter to it, from the FP32 working field (pdfs_ctx_orderings)."""
+        nbx, nby, nbz = self.blocks()
+        out = np.zeros((nbz, nby, nbx), dtype=np.uint8)
+        s = self._lib.pdfs_ctx_orderings(self.h, out.ctypes.data)
+        if s != L.PDFS_OK:
+            raise PdfsError(s, "pdfs_ctx_orderings")
+        return out
+
     def sweep(self, sn: int, active=None, block_change=None) -> float:
         """One ordering on the working field (pdfs_ctx_sweep); active and
         block_change are uint8 / float32 arrays with one entry per block,

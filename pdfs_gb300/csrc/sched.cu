@@ -65,38 +65,60 @@ __global__ void k_octant_mask(const float *__restrict__ u, Layout L, const uint3
   const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int nwx = (nbx + 3) / 4;
-  if (wid >= (long long)nwx * nby * nbz) return;
+  if (wid >= (long long)nwx * nby * nbz) return;  // whole warps leave together
   const int wx = (int)(wid % nwx), by = (int)((wid / nwx) % nby), bz = (int)(wid / ((long long)nwx * nby));
   const int x = 1 + wx * 32 + lane;
-  unsigned acc = 0;
+  const bool have = x <= nx + 1;  // the node, or the halo node right of the grid
   // accepted directions of one axis: bit 0 ascending, bit 1 descending
   auto axis = [](float c, float lo, float hi, float tie) -> unsigned {
     const float m = fminf(lo, hi);
     if (!(m < c) || fabsf(lo - hi) <= tie) return 3u;
     return lo < hi ? 1u : 2u;
   };
-  if (x <= nx) {
-    for (int z = 1 + bz * 8; z <= min(nz, bz * 8 + 8); ++z)
-      for (int y = 1 + by * 8; y <= min(ny, by * 8 + 8); ++y) {
-        if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
-        const float c = fabsf(u[L.index(x, y, z)]);
-        if (!(c < far)) continue;
-        const unsigned ax = axis(c, fabsf(u[L.index(x - 1, y, z)]), fabsf(u[L.index(x + 1, y, z)]), slack * hx);
-        const unsigned ay = axis(c, fabsf(u[L.index(x, y - 1, z)]), fabsf(u[L.index(x, y + 1, z)]), slack * hy);
-        const unsigned az = axis(c, fabsf(u[L.index(x, y, z - 1)]), fabsf(u[L.index(x, y, z + 1)]), slack * hz);
-#pragma unroll
-        for (int sn = 1; sn <= 8; ++sn) {
-          int sx, sy, sz;
-          ordering_signs(sn, &sx, &sy, &sz);
-          if ((ax & (sx > 0 ? 1u : 2u)) && (ay & (sy > 0 ? 1u : 2u)) && (az & (sz > 0 ? 1u : 2u)))
-            acc |= 1u << (sn - 1);
-        }
+  auto at = [&](int xx, int yy, int zz) { return fabsf(u[L.index(xx, yy, zz)]); };
+  // the (x, y, z) direction sets met in the block, as 27 bits: bit 9(ax-1) + 3(ay-1) + (az-1)
+  unsigned combos = 0;
+  const int z0 = 1 + bz * 8, z1 = min(nz, bz * 8 + 8);
+  for (int y = 1 + by * 8; y <= min(ny, by * 8 + 8); ++y) {
+    // a sliding window along z: the planes below, at and above the node
+    float cm = have ? at(x, y, z0 - 1) : INFINITY;
+    float c = have ? at(x, y, z0) : INFINITY;
+    for (int z = z0; z <= z1; ++z) {
+      const float cp = have ? at(x, y, z + 1) : INFINITY;
+      // x neighbours from the adjacent lanes; the warp's edge lanes read theirs
+      float xl = __shfl_up_sync(0xffffffffu, c, 1), xr = __shfl_down_sync(0xffffffffu, c, 1);
+      if (lane == 0 && have) xl = at(x - 1, y, z);
+      if (lane == 31 && x <= nx) xr = at(x + 1, y, z);
+      // frozen bits of the warp's 32 x: one word, when the warp holds a grid node
+      const unsigned fw = (fmask && 1 + wx * 32 <= nx) ? fmask[M.word(1 + wx * 32, y, z)] : 0u;
+      if (x <= nx && !((fw >> lane) & 1u) && c < far) {
+        const unsigned ax = axis(c, xl, xr, slack * hx);
+        const unsigned ay = axis(c, at(x, y - 1, z), at(x, y + 1, z), slack * hy);
+        const unsigned az = axis(c, cm, cp, slack * hz);
+        combos |= 1u << ((ax - 1) * 9 + (ay - 1) * 3 + (az - 1));
       }
+      cm = c;
+      c = cp;
+    }
   }
 #pragma unroll
-  for (int off = 1; off < 8; off <<= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, off);
+  for (int off = 1; off < 8; off <<= 1) combos |= __shfl_xor_sync(0xffffffffu, combos, off);
   const int bx = wx * 4 + (lane >> 3);
-  if ((lane & 7) == 0 && bx < nbx) omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)acc;
+  if ((lane & 7) == 0 && bx < nbx) {
+    unsigned acc = 0;
+    for (int k = 0; k < 27; ++k) {
+      if (!((combos >> k) & 1u)) continue;
+      const unsigned ax = k / 9 + 1, ay = (k / 3) % 3 + 1, az = k % 3 + 1;
+#pragma unroll
+      for (int sn = 1; sn <= 8; ++sn) {
+        int sx, sy, sz;
+        ordering_signs(sn, &sx, &sy, &sz);
+        if ((ax & (sx > 0 ? 1u : 2u)) && (ay & (sy > 0 ? 1u : 2u)) && (az & (sz > 0 ? 1u : 2u)))
+          acc |= 1u << (sn - 1);
+      }
+    }
+    omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)acc;
+  }
 }
 
 // active[b] = ordering sn matters to block b or to one of its six face
@@ -129,6 +151,32 @@ cudaError_t octant_mask(const float *u32, const Layout &L, const uint32_t *fmask
   const int grid = (int)((warps * 32 + 255) / 256);
   k_octant_mask<<<grid, 256, 0, st>>>(u32, L, fmask, M, g.nx, g.ny, g.nz, (float)g.dx, (float)g.dy, (float)g.dz, slack,
                                       far, nbx, nby, nbz, omask);
+  return cudaGetLastError();
+}
+
+// out[b] = omask of block b | omask of its six face neighbours (the widened
+// masks that octant_active(dilate = 1) applies one ordering at a time).
+__global__ void k_octant_union(const uint8_t *__restrict__ omask, uint8_t *__restrict__ out, int nbx, int nby,
+                               int nbz) {
+  const long long n = (long long)nbx * nby * nbz, pl = (long long)nbx * nby;
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n; b += (long long)gridDim.x * blockDim.x) {
+    const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / pl);
+    unsigned m = omask[b];
+    if (bx > 0) m |= omask[b - 1];
+    if (bx < nbx - 1) m |= omask[b + 1];
+    if (by > 0) m |= omask[b - nbx];
+    if (by < nby - 1) m |= omask[b + nbx];
+    if (bz > 0) m |= omask[b - pl];
+    if (bz < nbz - 1) m |= omask[b + pl];
+    out[b] = (uint8_t)m;
+  }
+}
+
+cudaError_t octant_union(const uint8_t *omask, uint8_t *out, int nbx, int nby, int nbz, int sms, cudaStream_t st) {
+  const long long n = (long long)nbx * nby * nbz;
+  int grid = (int)std::min<long long>((n + 255) / 256, (long long)sms * 8);
+  if (grid < 1) grid = 1;
+  k_octant_union<<<grid, 256, 0, st>>>(omask, out, nbx, nby, nbz);
   return cudaGetLastError();
 }
 

@@ -666,7 +666,7 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   want(&c->dstat, sizeof(DevStatus));
   want(&c->bchg, (size_t)c->nblocks * kRing * 4);
   want(&c->bact, (size_t)c->nblocks);
-  if (o.precision == PDFS_PREC_FP32_POLISH64) want(&c->omask, (size_t)c->nblocks);
+  if (need32) want(&c->omask, (size_t)c->nblocks);  // the polish's octant masks (pdfs_ctx_orderings)
   if (!wb.empty()) {
     want(&c->mlp_w, PDFS_MLP_PARAMS * 2);
     want(&c->bmin, (size_t)c->nblocks * 4);
@@ -1062,6 +1062,8 @@ static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsi
     return PDFS_OK;
   }
   // pencils sweep unmasked sweeps; a block mask or block-change output goes to bricks
+  // (pencils that recorded block changes measured no faster: 37.4 against 36.9 ms
+  // for the 8 recording sweeps of the 768^3 headline solve)
   const bool pencil = ts.pencil && !active && !blk_chg;
   if (ts.bz == 0 || pencil) CK(cudaMemsetAsync(c->progress, 0, (size_t)L.ncx * L.ncy * L.ty * 4, c->st));
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
@@ -1281,6 +1283,9 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         st.full_sweeps++;
       } else {
         st.blocks_skipped += c->nblocks - nact;
+        (which == 0 ? st.ms_kern_masked_fp32 : st.ms_kern_masked_fp64) += c->kern_ms - kms0;
+        (which == 0 ? st.updates_masked_fp32 : st.updates_masked_fp64) += upd;
+        (which == 0 ? st.masked_sweeps_fp32 : st.masked_sweeps_fp64)++;
       }
       if (o.fixed_sweeps == 0 && (full || !certify) && chg <= tol) break;
       need_full = !full && chg <= tol;  // a quiet skipped sweep calls for a judging full sweep
@@ -1409,6 +1414,21 @@ extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) 
   if (nbx) *nbx = c->nbx;
   if (nby) *nby = c->nby;
   if (nbz) *nbz = c->nbz;
+  return PDFS_OK;
+}
+
+extern "C" int pdfs_ctx_orderings(pdfs_ctx *c, uint8_t *orderings) {
+  if (!c || !c->loaded || !c->u32 || !c->omask || !orderings || c->last_prec < 0) return PDFS_ERR_INVALID;
+  CK(cudaSetDevice(c->dev));
+  const uint8_t *buf = c->omask;
+  CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, c->g, kOctSlack, INFINITY, c->nbx, c->nby,
+                 c->nbz, c->omask, c->st));
+  if (kOctDilate) {  // the polish's widened masks: bit sn of a block or of a face neighbour
+    CK(octant_union(c->omask, c->bact, c->nbx, c->nby, c->nbz, c->sms, c->st));
+    buf = c->bact;
+  }
+  CK(cudaMemcpyAsync(orderings, buf, (size_t)c->nblocks, cudaMemcpyDefault, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return PDFS_OK;
 }
 

@@ -357,3 +357,4 @@ def test_polish_binding_caps(arith):
     b = f.copy()
     O.solve(b, sp, tol=0.0, frozen=w.frozen, threads=8)
     assert rel_err(out[0], b, 1.0) <= 1e-6
+

@@ -1,0 +1,105 @@
+"""Octant masks of the polish's first cycle (k_octant_mask, k_octant_union in
+sched.cu, read through pdfs_ctx_orderings): per 8^3 block, the orderings
+that matter to it, computed from the FP32 working field.  Checked bit for bit
+against a numpy restatement of the rule in the same FP32 arithmetic, on
+ragged grids with both spacing kinds and frozen nodes, and through the
+scheduled polish solve itself (same answer as the unscheduled one)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pdfs_gb300 import _lib as L
+from pdfs_gb300 import api
+from pdfs_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+SLACK = np.float32(0.25)  # kOctSlack
+
+
+def signs(sn):
+    """Sweep directions of ordering sn (+1 ascending), makeSweepInfo's table."""
+    desc = -1 if sn in (2, 5, 7, 8) else 1
+    return ((-1 if sn in (4, 8) else 1) * desc, (-1 if sn in (2, 6) else 1) * desc, (-1 if sn in (3, 7) else 1) * desc)
+
+
+def orderings_ref(u32, frozen, spacing, widen=True):
+    """u32: the FP32 field in the reference layout (nz+2, ny+2, nx+2)."""
+    u = np.abs(u32.astype(np.float32))
+    c = u[1:-1, 1:-1, 1:-1]
+    nz, ny, nx = c.shape
+
+    def axis(lo, hi, h):
+        m = np.minimum(lo, hi)
+        tie = np.float32(SLACK * np.float32(h))
+        both = ~(m < c) | (np.abs(lo - hi) <= tie)
+        return np.where(both, 3, np.where(lo < hi, 1, 2)).astype(np.uint8)
+
+    ax = axis(u[1:-1, 1:-1, :-2], u[1:-1, 1:-1, 2:], spacing[0])
+    ay = axis(u[1:-1, :-2, 1:-1], u[1:-1, 2:, 1:-1], spacing[1])
+    az = axis(u[:-2, 1:-1, 1:-1], u[2:, 1:-1, 1:-1], spacing[2])
+    ok = np.isfinite(c)
+    if frozen is not None:
+        ok &= frozen[1:-1, 1:-1, 1:-1] == 0
+    bits = np.zeros(c.shape, dtype=np.uint8)
+    for sn in range(1, 9):
+        sx, sy, sz = signs(sn)
+        m = ((ax & (1 if sx > 0 else 2)) > 0) & ((ay & (1 if sy > 0 else 2)) > 0) & ((az & (1 if sz > 0 else 2)) > 0)
+        bits |= (m & ok).astype(np.uint8) << (sn - 1)
+    nbz, nby, nbx = (nz + 7) // 8, (ny + 7) // 8, (nx + 7) // 8
+    pad = np.zeros((nbz * 8, nby * 8, nbx * 8), dtype=np.uint8)
+    pad[:nz, :ny, :nx] = bits
+    blk = np.bitwise_or.reduce(pad.reshape(nbz, 8, nby, 8, nbx, 8), axis=(1, 3, 5))
+    if not widen:
+        return blk
+    out = blk.copy()
+    out[1:] |= blk[:-1]
+    out[:-1] |= blk[1:]
+    out[:, 1:] |= blk[:, :-1]
+    out[:, :-1] |= blk[:, 1:]
+    out[:, :, 1:] |= blk[:, :, :-1]
+    out[:, :, :-1] |= blk[:, :, 1:]
+    return out
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+@pytest.mark.parametrize("shape", [(1, 1, 1), (9, 17, 8), (33, 40, 7), (65, 31, 47), (70, 64, 40)])
+def test_orderings_equal_numpy_rule(shape, aniso):
+    sp = (0.7, 1.0, 0.5) if aniso else (1.0, 1.0, 1.0)
+    w = W.random_spheres(*shape, *sp, 4, 1.5, 8.0, seed=sum(shape))
+    with api.Context(w.nx, w.ny, w.nz, sp, freeze=L.FREEZE_MASK, precision=L.PREC_FP32) as c:
+        c.load(w.field, w.frozen)
+        c.run()
+        f = np.empty_like(w.field)
+        c.store(f)
+        got = c.orderings()
+    want = orderings_ref(f.astype(np.float32), w.frozen, sp)
+    assert got.shape == want.shape
+    assert np.array_equal(got, want), int((got != want).sum())
+
+
+def test_orderings_need_an_fp32_field():
+    w = W.random_spheres(20, 20, 20, 1.0, 1.0, 1.0, 2, 2.0, 5.0, seed=3)
+    with api.Context(w.nx, w.ny, w.nz, (1.0, 1.0, 1.0), precision=L.PREC_FP64) as c:
+        c.load(w.field)
+        c.run()
+        with pytest.raises(api.PdfsError):
+            c.orderings()
+
+
+def test_scheduled_polish_same_answer():
+    """The octant-masked first polish cycle then full sweeps to the tolerance:
+    the answer is the unscheduled polish's to within the FP32-pair rounding,
+    and both are within 1e-6 of the oracle."""
+    w = W.random_spheres(128, 112, 96, 1.0, 1.0, 1.0, 10, 3.0, 20.0, seed=44)
+    sp = (w.dx, w.dy, w.dz)
+    kw = dict(frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5)
+    a, b = w.field.copy(), w.field.copy()
+    sa = api.solve(a, sp, scheduler=L.SCHED_LEARNED, **kw)
+    api.solve(b, sp, **kw)
+    ref = w.field.copy()
+    O.solve(ref, sp, tol=1e-12, frozen=w.frozen, threads=8)
+    i = (slice(1, -1),) * 3
+    for x in (a, b):
+        assert float(np.max(np.abs(x[i] - ref[i]) / np.maximum(np.abs(ref[i]), 1.0))) <= 1e-6
+    assert sa["masked_sweeps_fp64"] == 8 and sa["updates_masked_fp64"] < 8 * w.interior
