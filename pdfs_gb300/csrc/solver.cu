@@ -667,6 +667,10 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   want(&c->bchg, (size_t)c->nblocks * kRing * 4);
   want(&c->bact, (size_t)c->nblocks);
   if (need32) want(&c->omask, (size_t)c->nblocks);  // the polish's octant masks (pdfs_ctx_orderings)
+  if (o.precision == PDFS_PREC_FP32_POLISH64 && s64.bz == 16 && s64.ty == 16) {  // the octant round
+    want(&c->toct, (8 * bo[1].size() + 17) * 4);
+    want(&c->ochg, 8 * 8);
+  }
   if (!wb.empty()) {
     want(&c->mlp_w, PDFS_MLP_PARAMS * 2);
     want(&c->bmin, (size_t)c->nblocks * 4);
@@ -972,6 +976,7 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
 }
 
 static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg);
+static int octant_round(pdfs_ctx *c, int first, double chg[8], long long *active);
 int pdfs::ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   return run_sweep(c, which, sn, active, blk_chg, chg);
 }
@@ -1225,6 +1230,30 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     int s = 0;
     int band_sweep = -1;  // learned scheduler: the sweep of the last block-minimum pass
     for (;;) {
+      if (octant && s == 0 && c->toct && max_sweeps > 8) {
+        // the first cycle in one launch: the 8 orderings on their octant masks
+        double ch8[8];
+        long long nb_act = 0;
+        const double kms0 = c->kern_ms;
+        int r = octant_round(c, first, ch8, &nb_act);
+        if (r) return r;
+        const long long bnodes = (long long)c->nt64[0] * c->nt64[1] * c->nt64[2];
+        // updates: the visited bricks' nodes, at most the grid's
+        const long long upd = std::min<long long>(nb_act * 4096LL, 8LL * nodes);
+        if (verbose(o))
+          for (int j = 0; j < 8; ++j)
+            fprintf(stderr, "pdfs: phase %d sweep %d sn=%d octant change=%.3e (one launch: %.3f ms for 8 sweeps, "
+                            "%lld of %lld brick visits)\n",
+                    which, j, (first + j) % 8 + 1, ch8[j], c->kern_ms - kms0, nb_act, 8 * bnodes);
+        st.voxel_updates += upd;
+        st.voxel_updates_fp64 += upd;
+        st.ms_kern_masked_fp64 += c->kern_ms - kms0;
+        st.updates_masked_fp64 += upd;
+        st.masked_sweeps_fp64 += 8;
+        chg = ch8[7];
+        s = 8;
+        continue;
+      }
       if (o.fixed_sweeps > 0 && s >= o.fixed_sweeps) break;
       if (o.fixed_sweeps == 0 && s >= max_sweeps) {
         rc = PDFS_ERR_NOT_CONVERGED;
@@ -1414,6 +1443,58 @@ extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) 
   if (nbx) *nbx = c->nbx;
   if (nby) *nby = c->nby;
   if (nbz) *nbz = c->nbz;
+  return PDFS_OK;
+}
+
+// The polish's first cycle as one launch (an octant round on 16 x 16 x 16
+// bricks, tile3d.cuh OCT): orderings (first + j) % 8 + 1, j = 0..7, each over
+// the blocks its octant mask names.  chg: the 8 sweeps' max changes;
+// *active: the blocks visited, summed over the 8 sweeps.
+static int octant_round(pdfs_ctx *c, int first, double chg[8], long long *active) {
+  const pdfs_grid &g = c->g;
+  CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack, INFINITY, c->nbx, c->nby,
+                 c->nbz, c->omask, c->st));
+  const uint8_t *bits = c->omask;
+  if (kOctDilate) {
+    CK(octant_union(c->omask, c->bact, c->nbx, c->nby, c->nbz, c->sms, c->st));
+    bits = c->bact;
+  }
+  SweepArgs a;
+  fill_sweep_args(c, 2, first % 8 + 1, nullptr, nullptr, &a);
+  a.oct_first = first;
+  a.oct_bits = bits;
+  a.oct_tbits = c->tact;
+  a.maxchg = c->ochg;
+  a.epoch = c->epoch + 1;  // sweep j publishes epoch + j
+  c->epoch += 8;
+  const int nb = c->nt64[0] * c->nt64[1] * c->nt64[2];
+  int *cnt_off = c->toct + 8 * (size_t)nb;
+  CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
+  CK(cudaMemsetAsync(c->ochg, 0, 8 * 8, c->st));
+  CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
+  const bool iso = g.dx == g.dy && g.dy == g.dz;
+  const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF
+                    : c->o.arith == PDFS_ARITH_MIXED   ? ARITH_MIXED
+                    : c->o.arith == PDFS_ARITH_PAIR    ? ARITH_PAIR
+                                                       : ARITH_FAST;
+  int grid = 0;
+  CK(cudaEventRecord(c->k0, c->st));
+  CK(launch_octant_round(arith, iso, a, c->L64, c->toct, cnt_off, c->sms, c->st, &grid));
+  CK(cudaEventRecord(c->k1, c->st));
+  unsigned long long h[8];
+  int cnt[8];
+  CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(h, c->ochg, sizeof h, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(cnt, cnt_off, sizeof cnt, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->kern_ms += ms_between(c->k0, c->k1);
+  c->launches += 5 + (kOctDilate ? 1 : 0);
+  if (c->hstat->err[0]) return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
+  *active = 0;
+  for (int j = 0; j < 8; ++j) {
+    std::memcpy(&chg[j], &h[j], 8);  // FP64 change words hold the double's bits (pairs: see change_u64)
+    *active += (long long)cnt[j];
+  }
   return PDFS_OK;
 }
 

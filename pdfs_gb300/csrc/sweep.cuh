@@ -108,6 +108,14 @@ struct SweepArgs {
   // them in wavefront order, *nticket of them)
   const uint8_t *tact;
   const int *nticket;
+  // an octant round on bricks (tile3d.cuh, OCT): the 8 orderings of the
+  // polish's first cycle in one launch, ordering (oct_first + j) % 8 + 1 for
+  // sweep j; oct_bits: per 8^3 block, bit sn-1 = ordering sn visits it;
+  // oct_tbits: the same per brick (the union of its blocks); torder: [8][ntile]
+  // tickets per sweep, nticket: their 9 prefix offsets
+  int oct_first;
+  const uint8_t *oct_bits;
+  const uint8_t *oct_tbits;
 };
 
 // Arguments of the lane-column sweep (lanecol.cuh).

@@ -121,6 +121,120 @@ __global__ void k_brick_compact(const int *__restrict__ torder, int ntx, int nty
   if (tid == nt - 1) *count = s_sum[tid];
 }
 
+// ---- octant rounds (the polish's first cycle in one launch, tile3d.cuh OCT) ----
+
+// Per brick, the union of its 8^3 blocks' ordering bits.
+__global__ void k_brick_bits(int ntx, int nty, int ntz, int bx, int by, int bz, const uint8_t *__restrict__ bits,
+                             int nbx, int nby, int nbz, uint8_t *__restrict__ tbits) {
+  const int n = ntx * nty * ntz;
+  for (int tile = blockIdx.x * blockDim.x + threadIdx.x; tile < n; tile += gridDim.x * blockDim.x) {
+    const int bi = tile % ntx, bj = (tile / ntx) % nty, bk = tile / (ntx * nty);
+    unsigned m = 0;
+    for (int q = 0; q < bz; ++q)
+      for (int p = 0; p < by; ++p)
+        for (int o = 0; o < bx; ++o) {
+          const int X = bi * bx + o, Y = bj * by + p, Z = bk * bz + q;
+          if (X < nbx && Y < nby && Z < nbz) m |= bits[((long long)Z * nby + Y) * nbx + X];
+        }
+    tbits[tile] = (uint8_t)m;
+  }
+}
+
+// Sweep j's tickets (CTA j): the bricks whose bits name ordering
+// (first + j) % 8 + 1, in that ordering's wavefront order, to out[j][...];
+// their count to cnt[j].  The scan keeps the order (as k_brick_compact).
+__global__ void k_oct_tickets(const int *__restrict__ torder, int ntx, int nty, int ntz, int first,
+                              const uint8_t *__restrict__ tbits, int *__restrict__ out, int *__restrict__ cnt) {
+  __shared__ int s_sum[1024];
+  const int j = blockIdx.x, n = ntx * nty * ntz, tid = threadIdx.x, nt = blockDim.x;
+  const int sn = (first + j) % 8 + 1;
+  const unsigned bit = 1u << (sn - 1);
+  int sx, sy, sz;
+  ordering_signs(sn, &sx, &sy, &sz);
+  const int per = (n + nt - 1) / nt, t0 = min(n, tid * per), t1 = min(n, t0 + per);
+  auto active = [&](int tk) {
+    const int lt = torder[tk], li = lt % ntx, lj = (lt / ntx) % nty, lk = lt / (ntx * nty);
+    const int bi = sx > 0 ? li : ntx - 1 - li, bj = sy > 0 ? lj : nty - 1 - lj, bk = sz > 0 ? lk : ntz - 1 - lk;
+    return (tbits[(bk * nty + bj) * ntx + bi] & bit) != 0;
+  };
+  int c = 0;
+  for (int tk = t0; tk < t1; ++tk) c += active(tk) ? 1 : 0;
+  s_sum[tid] = c;
+  __syncthreads();
+  for (int off = 1; off < nt; off <<= 1) {
+    const int v = tid >= off ? s_sum[tid - off] : 0;
+    __syncthreads();
+    s_sum[tid] += v;
+    __syncthreads();
+  }
+  int pos = s_sum[tid] - c;
+  int *o = out + (long long)j * n;
+  for (int tk = t0; tk < t1; ++tk)
+    if (active(tk)) o[pos++] = torder[tk];
+  if (tid == nt - 1) cnt[j] = s_sum[tid];
+}
+
+// off[0..8]: prefix sums of the 8 counts (the round's ticket ranges).
+__global__ void k_oct_offsets(const int *__restrict__ cnt, int *__restrict__ off) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    off[0] = 0;
+    for (int j = 0; j < 8; ++j) off[j + 1] = off[j] + cnt[j];
+  }
+}
+
+template <int ARITH, bool ISO>
+static cudaError_t launch_oct(const SweepArgs &a, const Layout &L, int sms, cudaStream_t st, int *grid_used) {
+  using G = T3Geo<double, 16, 16>;
+  auto kern = t3_sweep_kernel<double, 16, 16, MODE_REPLACE, ARITH, ISO, true>;
+  CUtensorMap m;
+  cudaError_t e = encode_field_map(&m, a.u, 8, L, a.nz + 2, G::W, G::RY, G::RZ);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::BYTES);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, G::NT, G::BYTES);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  // every CTA resident: a ticket waits only on smaller tickets
+  int grid = std::min(per_sm * sms, 8 * a.ntx * a.nty * a.ntz);
+  if (grid < 1) grid = 1;
+  kern<<<grid, G::NT, G::BYTES, st>>>(m, a);
+  if (grid_used) *grid_used = grid;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_octant_round(int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list, int *cnt_off,
+                                int sms, cudaStream_t st, int *g) {
+  if (!a0.tflag || !a0.torder || !a0.oct_bits || !a0.oct_tbits || a0.ntx < 1 || L.ty != 16 || L.tx != 16 ||
+      L.xo != 0 || !a0.bcap64 || !a0.bcap32)
+    return cudaErrorInvalidValue;
+  const int n = a0.ntx * a0.nty * a0.ntz;
+  k_brick_bits<<<std::min((n + 255) / 256, 4 * sms), 256, 0, st>>>(a0.ntx, a0.nty, a0.ntz, 2, 2, 2, a0.oct_bits,
+                                                                  a0.nbx, a0.nby, a0.nbz,
+                                                                  const_cast<uint8_t *>(a0.oct_tbits));
+  k_oct_tickets<<<8, 1024, 0, st>>>(a0.torder, a0.ntx, a0.nty, a0.ntz, a0.oct_first, a0.oct_tbits, list, cnt_off);
+  k_oct_offsets<<<1, 32, 0, st>>>(cnt_off, cnt_off + 8);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  SweepArgs a = a0;
+  a.torder = list;
+  a.nticket = cnt_off + 8;
+  a.blk_active = nullptr;
+  a.tact = nullptr;
+  switch (arith) {
+    case ARITH_PAIR:
+      return iso ? launch_oct<ARITH_PAIR, true>(a, L, sms, st, g) : launch_oct<ARITH_PAIR, false>(a, L, sms, st, g);
+    case ARITH_MIXED:
+      return iso ? launch_oct<ARITH_MIXED, true>(a, L, sms, st, g) : launch_oct<ARITH_MIXED, false>(a, L, sms, st, g);
+    case ARITH_FAST:
+      return launch_oct<ARITH_FAST, false>(a, L, sms, st, g);
+    case ARITH_REF:
+      return launch_oct<ARITH_REF, false>(a, L, sms, st, g);
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_sweep_bricks(int which, int by, int bz, int arith, bool iso, const SweepArgs &a0, const Layout &L,
                                 int sms, cudaStream_t st, int *g) {
   if (!a0.tflag || !a0.torder || a0.ntx < 1 || a0.nty < 1 || a0.ntz < 1 || L.ty != by || L.tx != 16 ||

@@ -63,7 +63,16 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
-template <class T, int BY_, int BZ, int MODE, int ARITH, bool ISO>
+// OCT: an octant round -- the 8 orderings of the polish's first cycle in one
+// launch.  A ticket names (sweep j, brick); ordering (oct_first + j) % 8 + 1
+// visits the bricks and blocks whose bits name it.  Before its box is read, a
+// brick waits until it and its six face neighbours have finished their latest
+// earlier sweep of the round (their values are this sweep's old values), then
+// for its upwind bricks in this sweep as usual.  Flags carry epoch + j, so
+// "finished sweep j" is a flag >= epoch + j; tickets list sweep j's bricks
+// (wavefront order) before sweep j + 1's, so every wait is on a smaller
+// ticket.  The result is the sequential sweeps', bit for bit.
+template <class T, int BY_, int BZ, int MODE, int ARITH, bool ISO, bool OCT = false>
 __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                             const __grid_constant__ SweepArgs a) {
   using G = T3Geo<T, BY_, BZ>;
@@ -84,13 +93,13 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
   }
   const int tid = threadIdx.x, lane = tid & 31;
   const int lx = tid & (BX - 1), ly = tid / BX;  // brick-local x, y in sweep order
-  const int sxd = a.sx, syd = a.sy, szd = a.sz;
-  const int gxl = sxd > 0 ? lx : BX - 1 - lx;    // brick-local x, y in grid order
-  const int gyl = syd > 0 ? ly : BY - 1 - ly;
+  int sxd = a.sx, syd = a.sy, szd = a.sz;  // OCT: set per ticket
+  int gxl = sxd > 0 ? lx : BX - 1 - lx;      // brick-local x, y in grid order
+  int gyl = syd > 0 ? ly : BY - 1 - ly;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int ntx = a.ntx, nty = a.nty, ntz = a.ntz;
   // a block-masked sweep takes tickets only for the bricks with an active block
-  const int ntile = a.nticket ? *a.nticket : ntx * nty * ntz;
+  const int ntile = OCT ? a.nticket[8] : (a.nticket ? *a.nticket : ntx * nty * ntz);
   const uint8_t *__restrict__ tact = a.tact;
   const long long plane = a.plane, px = a.px;
   const float hmin = a.hmin;
@@ -101,7 +110,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
   const bool masked = a.fmask != nullptr;
   T *__restrict__ u = reinterpret_cast<T *>(a.u);
   const T *__restrict__ capg = reinterpret_cast<const T *>(a.cap);
-  const int epoch = a.epoch;
+  int epoch = a.epoch;  // OCT: epoch + the ticket's sweep
   T tmax = T(0);
 
   if (tid == 0) {
@@ -121,7 +130,20 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     // a uniform decision (s_abort may change under the reads); the barrier
     // also orders every read of s_next before its next write
     if (__syncthreads_or(tk >= ntile || s_abort)) break;
-    const int lt = a.torder[tk];  // local brick id in sweep order: (lk * nty + lj) * ntx + li
+    int lt, osw = 0;
+    unsigned obit = 0;  // OCT: the ticket's ordering bit
+    if constexpr (OCT) {
+      while (osw < 7 && tk >= a.nticket[osw + 1]) ++osw;
+      lt = a.torder[(long long)osw * ntx * nty * ntz + (tk - a.nticket[osw])];
+      const int sn = (a.oct_first + osw) % 8 + 1;
+      obit = 1u << (sn - 1);
+      ordering_signs(sn, &sxd, &syd, &szd);
+      gxl = sxd > 0 ? lx : BX - 1 - lx;
+      gyl = syd > 0 ? ly : BY - 1 - ly;
+      epoch = a.epoch + osw;
+    } else {
+      lt = a.torder[tk];  // local brick id in sweep order: (lk * nty + lj) * ntx + li
+    }
     const int li = lt % ntx, lj = (lt / ntx) % nty, lk = lt / (ntx * nty);
     const int bi = sxd > 0 ? li : ntx - 1 - li;
     const int bj = syd > 0 ? lj : nty - 1 - lj;
@@ -134,14 +156,15 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     // otherwise only the levels that reach its active planes run
     bool run = true;
     int lev0 = 0, lev1 = NL;  // levels [lev0, lev1) of this brick
-    if (blk_active) {
+    if (OCT || blk_active) {
       bool act = false;
       if (tid < G::NBX * G::NBY * NZB) {
         const int q = tid / (G::NBX * G::NBY);
         const int bx = G::NBX * bi + tid % G::NBX, by = G::NBY * bj + (tid / G::NBX) % G::NBY;
         const int bz = bk * NZB + q;
         if (bx < a.nbx && by < a.nby && bz < a.nbz)
-          act = __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0;
+          act = OCT ? (__ldg(a.oct_bits + ((long long)bz * a.nby + by) * a.nbx + bx) & obit) != 0
+                    : __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0;
         if (act) {  // the block's planes 8q .. 8q+7 (grid order) in sweep order
           const int lo = szd > 0 ? 8 * q : BZ - 8 * q - 8;
           atomicMin(&s_lo, lo);
@@ -159,6 +182,46 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       continue;
     }
 
+    if constexpr (OCT) {
+      // the round's earlier sweeps: this brick and its six face neighbours
+      // (lanes 0..6 of warp 0, one each) finish their latest earlier sweep first
+      bool okp = true;
+      if (tid < 7) {
+        int n = -1;
+        if (tid == 0) n = tile;
+        if (tid == 1 && bi > 0) n = tile - 1;
+        if (tid == 2 && bi < ntx - 1) n = tile + 1;
+        if (tid == 3 && bj > 0) n = tile - ntx;
+        if (tid == 4 && bj < nty - 1) n = tile + ntx;
+        if (tid == 5 && bk > 0) n = tile - ntx * nty;
+        if (tid == 6 && bk < ntz - 1) n = tile + ntx * nty;
+        int need = -1;
+        if (n >= 0) {
+          const unsigned tb = __ldg(a.oct_tbits + n);
+          for (int j = osw - 1; j >= 0 && need < 0; --j)
+            if ((tb >> ((a.oct_first + j) % 8)) & 1u) need = j;
+        }
+        if (need >= 0 && ld_acquire_gpu(a.tflag + n) < a.epoch + need) {
+          const long long t0 = cycles();
+          unsigned nap = 32;
+          while (ld_acquire_gpu(a.tflag + n) < a.epoch + need) {
+            if (s_abort || *(volatile int *)(a.err + 1)) {
+              s_abort = 1;
+              okp = false;
+              break;
+            }
+            if (cycles() - t0 > a.wait_cycles) {
+              raise_timeout(a, tile, &s_abort);
+              okp = false;
+              break;
+            }
+            __nanosleep(nap);
+            nap = min(nap * 2, 256u);
+          }
+        }
+      }
+      if (!__syncthreads_and(okp)) break;
+    }
     // the box: TMA from (x0 - 1, y0 - 1, z0 - 1); out-of-range rows and planes read 0 (never used)
     fence_proxy_async();  // this CTA's generic accesses to the box come before the copy's writes
     __syncthreads();
@@ -182,13 +245,15 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     const int mshift = 16 * (bi & 1) + gxl;
     // active 8^3 blocks of my (x, y) column, one bit per z block of the brick
     unsigned actz = (1u << NZB) - 1u;
-    if (blk_active && vxy) {
+    if ((OCT || blk_active) && vxy) {
       actz = 0;
       const int bx = (x0 - 1 + gxl) >> 3, by = (y0 - 1 + gyl) >> 3;
 #pragma unroll
       for (int q = 0; q < NZB; ++q) {
         const int bz = bk * NZB + q;
-        if (bz < a.nbz && __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx)) actz |= 1u << q;
+        if (bz < a.nbz && (OCT ? (__ldg(a.oct_bits + ((long long)bz * a.nby + by) * a.nbx + bx) & obit) != 0
+                                : __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0))
+          actz |= 1u << q;
       }
     }
     const long long gbase = (long long)z0 * plane + (long long)(y0 + gyl) * px + (x0 + gxl);
@@ -210,7 +275,11 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       if (tid == 1 && lj > 0) up = tile - syd * ntx;
       if (tid == 2 && lk > 0) up = tile - szd * ntx * nty;
       // an upwind brick without an active block keeps its values: nothing to wait for
-      if (up >= 0 && tact && !tact[up]) up = -1;
+      if constexpr (OCT) {
+        if (up >= 0 && !(__ldg(a.oct_tbits + up) & obit)) up = -1;
+      } else {
+        if (up >= 0 && tact && !tact[up]) up = -1;
+      }
       if (up >= 0 && ld_acquire_gpu(a.tflag + up) < epoch) {
         const long long t0 = cycles();
         unsigned nap = 32;
@@ -343,6 +412,14 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
           atomicMax(blk_chg + ((long long)bz * a.nby + by) * a.nbx + bx, __float_as_uint(change_f<T, ARITH>(v)));
         }
       }
+    }
+    if constexpr (OCT) {  // this sweep's change word (one per sweep of the round)
+      T v = tmax;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(0xffffffffu, v, off));
+      if (lane == 0 && change_pos<T, ARITH>(v))
+        atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg) + osw, change_u64<T, ARITH>(v));
+      tmax = T(0);
     }
     // publish: the barrier orders every thread's stores before thread 0's
     // GPU-scope fence, which orders them before the flag

@@ -103,3 +103,22 @@ def test_scheduled_polish_same_answer():
     for x in (a, b):
         assert float(np.max(np.abs(x[i] - ref[i]) / np.maximum(np.abs(ref[i]), 1.0))) <= 1e-6
     assert sa["masked_sweeps_fp64"] == 8 and sa["updates_masked_fp64"] < 8 * w.interior
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_octant_round_equals_sequential_masked_sweeps(aniso):
+    """The polish's first cycle as one launch (16 x 16 x 16 bricks, the
+    octant round: a brick of sweep j starts once it and its face neighbours
+    finished their latest earlier sweep) against the same 8 masked sweeps
+    run one launch each (16 x 16 x 32 bricks, which have no round): the
+    same bits, the same sweep counts."""
+    sp = (0.8, 1.0, 0.6) if aniso else (1.0, 1.0, 1.0)
+    w = W.random_spheres(112, 96, 120, *sp, 12, 3.0, 18.0, seed=45)
+    kw = dict(frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5,
+              scheduler=L.SCHED_LEARNED)
+    a, b = w.field.copy(), w.field.copy()
+    sa = api.solve(a, sp, tile=10 | (6 << 8), **kw)
+    sb = api.solve(b, sp, tile=10 | (7 << 8), **kw)
+    assert (sa["sweeps_fp32"], sa["sweeps_fp64"]) == (sb["sweeps_fp32"], sb["sweeps_fp64"])
+    assert sa["masked_sweeps_fp64"] == sb["masked_sweeps_fp64"] == 8
+    assert a.tobytes() == b.tobytes()
