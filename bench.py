@@ -1,9 +1,10 @@
 """Benchmark of the GB300 FSM distance-field solve.
 
 Metric (the reference's headline, printed identically by both arms):
-time-to-converge and Gvoxel-updates/s of the learned-scheduler FP32-bulk +
+time-to-converge and Gvoxel-updates/s of the block-scheduled FP32-bulk +
 FP64-precision-polish solve against the plain FP64 FSM, at <= 1e-6
-relative error.  Gvox-updates/s are plain-equivalent: the plain FP64 FSM's
+relative error (the octant scheduler by default; the none, history-rule and
+learned schedulers are timed beside it).  Gvox-updates/s are plain-equivalent: the plain FP64 FSM's
 node updates on the same input (interior nodes x its sweep count) divided by
 the time to converge.  The reference arm runs the plain FP64 FSM itself, so
 its rate is its own per-ordering rate.
@@ -38,7 +39,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 
-METRIC = "time-to-converge & Gvox-updates/s: learned+FP32 vs plain FP64 FSM at 1e-6 err"
+METRIC = "time-to-converge & Gvox-updates/s: scheduled FP32+polish vs plain FP64 FSM at 1e-6 err"
 UNIT = "Gvox-updates/s"
 
 
@@ -50,7 +51,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="C4")
     p.add_argument("--mode", default="polish", choices=["polish", "fp32", "fp64", "fp64ref"])
-    p.add_argument("--scheduler", default="learned", choices=["none", "change", "learned"])
+    p.add_argument("--scheduler", default="octant", choices=["none", "change", "learned", "octant"])
     p.add_argument("--tol", type=float, default=1e-5, help="FP64 polish tolerance (max change)")
     p.add_argument("--polish-arith", default="pair", choices=["mixed", "pair", "fast"],
                    help="polish arithmetic: FP32 increments over an FP64 field (mixed) or an FP32-pair "
@@ -406,6 +407,8 @@ def run_configs(args, device):
                  ("fp32_polish_pair", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5 * h)),
                  ("fp32_polish_pair_learned", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR,
                                                    tol=1e-5 * h, scheduler=L.SCHED_LEARNED)),
+                 ("fp32_polish_pair_octant", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR,
+                                                  tol=1e-5 * h, scheduler=L.SCHED_OCTANT)),
                  ("fp32_polish_fp64", dict(precision=L.PREC_FP32_POLISH64, arith=L.ARITH_FAST, tol=1e-5 * h)),
                  ("fp32_only", dict(precision=L.PREC_FP32))]
         if name in ("C1", "C2"):
@@ -464,7 +467,8 @@ def main():
     arith = L.ARITH_REFERENCE if args.mode == "fp64ref" else L.ARITH_FAST
     if args.mode == "polish" and args.polish_arith in ("mixed", "pair"):
         arith = L.ARITH_MIXED if args.polish_arith == "mixed" else L.ARITH_PAIR
-    sched = {"none": L.SCHED_NONE, "change": L.SCHED_CHANGE, "learned": L.SCHED_LEARNED}[args.scheduler]
+    sched = {"none": L.SCHED_NONE, "change": L.SCHED_CHANGE, "learned": L.SCHED_LEARNED,
+             "octant": L.SCHED_OCTANT}[args.scheduler]
     if args.mode in ("fp64", "fp64ref"):
         sched = L.SCHED_NONE
     opts = dict(precision=prec, arith=arith, freeze=freeze, scheduler=sched, tol=args.tol, tile=args.tile,
@@ -611,7 +615,8 @@ def main():
     sched_table = None
     if not args.no_sched_table and args.fixed_sweeps == 0 and args.mode in ("polish", "fp32"):
         sched_table = {}
-        for name, sv in (("none", L.SCHED_NONE), ("change", L.SCHED_CHANGE), ("learned", L.SCHED_LEARNED)):
+        for name, sv in (("none", L.SCHED_NONE), ("change", L.SCHED_CHANGE), ("learned", L.SCHED_LEARNED),
+                         ("octant", L.SCHED_OCTANT)):
             o2 = dict(opts, scheduler=sv)
             try:
                 with api.Context(w.nx, w.ny, w.nz, sp, **o2) as c2:

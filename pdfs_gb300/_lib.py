@@ -22,7 +22,7 @@ STATIC_SCRATCH_BYTES = 32 << 20
 PREC_FP64, PREC_FP32, PREC_FP32_POLISH64 = 0, 1, 2
 ARITH_REFERENCE, ARITH_FAST, ARITH_MIXED, ARITH_PAIR = 0, 1, 2, 3
 FREEZE_NONE, FREEZE_MASK = 0, 1
-SCHED_NONE, SCHED_CHANGE, SCHED_LEARNED = 0, 1, 2
+SCHED_NONE, SCHED_CHANGE, SCHED_LEARNED, SCHED_OCTANT = 0, 1, 2, 3
 
 # Every function declared in include/pdfs.h (the CPU tests check the exports).
 EXPORTS = [

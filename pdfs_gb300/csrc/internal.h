@@ -92,12 +92,13 @@ cudaError_t encode_pencil_maps(int which, const SweepArgs &a, const Layout &L, C
 // pair min, 2 = pair replace; tiles of rows = 4 or 8 rows.
 cudaError_t launch_sweep_lanecol(int which, int rows, bool iso, const LcArgs &a, int sms, cudaStream_t st,
                                  int *grid_used);
-// The polish's first cycle as one launch on 16 x 16 x 16 FP64 bricks (tile3d.cu):
-// a0 as for a replace-update sweep, with oct_first, oct_bits (per block) and
-// oct_tbits (per brick, filled here) set, a0.epoch the first of 8 epochs and
-// a0.maxchg 8 change words; list: 8 x bricks ints, cnt_off: 17 ints.
-cudaError_t launch_octant_round(int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list, int *cnt_off,
-                                int sms, cudaStream_t st, int *grid_used);
+// A cycle of 8 orderings as one launch on bricks over octant masks (tile3d.cu):
+// which 0 = FP32 min-update (16 x 16 x 32 bricks), 2 = the polish's replace-
+// update (16 x 16 x 16).  a0 as for such a sweep, with oct_first, oct_bits
+// (per block) and oct_tbits (per brick, filled here) set, a0.epoch the first of
+// 8 epochs and a0.maxchg 8 change words; list: 8 x bricks ints, cnt_off: 17 ints.
+cudaError_t launch_octant_round(int which, int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list,
+                                int *cnt_off, int sms, cudaStream_t st, int *grid_used);
 // Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
 std::vector<int> brick_order(int ntx, int nty, int ntz);
 cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by,
@@ -213,7 +214,8 @@ struct pdfs_ctx {
   unsigned int *bchg = nullptr;  // [kRing][nblocks] float bits of per-block max change, rotating
   uint8_t *bact = nullptr;       // [nblocks] active mask of the next sweep
   uint8_t *omask = nullptr;      // [nblocks] polish: the orderings that matter to each block
-  int *toct = nullptr;           // polish octant round: [8][FP64 bricks] tickets, then 17 counts / offsets
+  int *toct = nullptr;           // octant rounds: [8][bricks] tickets, then 17 counts / offsets
+  bool oct32_ok = false, oct64_ok = false;  // octant rounds available (FP32 / polish brick shapes)
   unsigned long long *ochg = nullptr;  // its 8 change words
   float *bmin = nullptr;         // [nblocks] per-block field minimum (learned scheduler)
   uint16_t *mlp_w = nullptr;     // learned scheduler: bf16 network weights

@@ -495,7 +495,7 @@ static int validate(const pdfs_grid *g, const pdfs_opts *o) {
       !std::isfinite(g->dz))
     return PDFS_ERR_INVALID;
   if (o->precision < 0 || o->precision > 2 || o->arith < 0 || o->arith > 3 || o->freeze < 0 || o->freeze > 1 ||
-      o->scheduler < 0 || o->scheduler > 2 || o->tol < 0 || !std::isfinite(o->tol) || o->fixed_sweeps < 0 ||
+      o->scheduler < 0 || o->scheduler > 3 || o->tol < 0 || !std::isfinite(o->tol) || o->fixed_sweeps < 0 ||
       o->max_sweeps < 0 || o->first_ordering < 0 || o->first_ordering > 8)
     return PDFS_ERR_INVALID;
   const int t32 = o->tile & 0xff, t64 = (o->tile >> 8) & 0xff;
@@ -667,8 +667,11 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   want(&c->bchg, (size_t)c->nblocks * kRing * 4);
   want(&c->bact, (size_t)c->nblocks);
   if (need32) want(&c->omask, (size_t)c->nblocks);  // the polish's octant masks (pdfs_ctx_orderings)
-  if (o.precision == PDFS_PREC_FP32_POLISH64 && s64.bz == 16 && s64.ty == 16) {  // the octant round
-    want(&c->toct, (8 * bo[1].size() + 17) * 4);
+  // octant rounds: FP32 on 16 x 16 x 32 bricks, the polish on 16 x 16 x 16 ones
+  c->oct32_ok = o.precision != PDFS_PREC_FP64 && s32.bz == 32 && s32.ty == 16 && s32.tx == 16;
+  c->oct64_ok = o.precision == PDFS_PREC_FP32_POLISH64 && s64.bz == 16 && s64.ty == 16 && s64.tx == 16;
+  if (c->oct32_ok || c->oct64_ok) {
+    want(&c->toct, (8 * std::max(bo[0].size(), bo[1].size()) + 17) * 4);
     want(&c->ochg, 8 * 8);
   }
   if (!wb.empty()) {
@@ -976,7 +979,7 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
 }
 
 static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg);
-static int octant_round(pdfs_ctx *c, int first, double chg[8], long long *active);
+static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active);
 int pdfs::ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   return run_sweep(c, which, sn, active, blk_chg, chg);
 }
@@ -1209,7 +1212,12 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   auto phase = [&](int which, double tol, int *count, double *ms, double *kms) -> int {
     c->kern_ms = 0.0;
     CK(cudaEventRecord(c->e0, c->st));
-    const bool sched = o.scheduler != PDFS_SCHED_NONE && o.fixed_sweeps == 0 && !(polish && which == 2);
+    // PDFS_SCHED_OCTANT, FP32 phase: a full first cycle, then cycles as octant
+    // rounds over masks from the field (at most three, until a round's last
+    // two sweeps change by at most 16 x the phase tolerance)
+    const bool oct32 = o.scheduler == PDFS_SCHED_OCTANT && which == 0 && o.fixed_sweeps == 0 && c->oct32_ok;
+    const bool sched = o.scheduler != PDFS_SCHED_NONE && o.scheduler != PDFS_SCHED_OCTANT && o.fixed_sweeps == 0 &&
+                       !(polish && which == 2);
     // the polish under a scheduler: its first cycle visits, in each ordering,
     // only the blocks that ordering matters to (octant masks of the FP32
     // result); full sweeps follow until one certifies
@@ -1221,37 +1229,50 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     int cur = 0;
     if (sched) CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * kRing * 4, c->st));
     if (sched || octant) CK(cudaMemsetAsync(&c->dstat->sched_err, 0, 4, c->st));
-    if (octant) {
+    if (octant && !c->oct64_ok) {  // the masks of the one-launch-per-sweep path (the round computes its own)
       CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack, INFINITY, c->nbx, c->nby,
                      c->nbz, c->omask, c->st));
       c->launches++;
     }
     bool need_full = true;
     int s = 0;
+    int oct_rounds = 0;
+    bool oct_done = false;
     int band_sweep = -1;  // learned scheduler: the sweep of the last block-minimum pass
     for (;;) {
-      if (octant && s == 0 && c->toct && max_sweeps > 8) {
-        // the first cycle in one launch: the 8 orderings on their octant masks
+      const bool round64 = octant && s == 0 && c->oct64_ok && max_sweeps > 8;
+      const bool round32 = oct32 && s >= 8 && !oct_done && s + 8 < max_sweeps;
+      if (round64 || round32) {
+        // a cycle of 8 orderings in one launch, each on its octant mask
         double ch8[8];
         long long nb_act = 0;
         const double kms0 = c->kern_ms;
-        int r = octant_round(c, first, ch8, &nb_act);
+        int r = octant_round(c, which, (first + s) % 8, ch8, &nb_act);
         if (r) return r;
-        const long long bnodes = (long long)c->nt64[0] * c->nt64[1] * c->nt64[2];
+        const int *nt = which == 0 ? c->nt32 : c->nt64;
+        const long long bnodes = (long long)nt[0] * nt[1] * nt[2];
         // updates: the visited bricks' nodes, at most the grid's
-        const long long upd = std::min<long long>(nb_act * 4096LL, 8LL * nodes);
+        const long long upd = std::min<long long>(nb_act * (which == 0 ? 8192LL : 4096LL), 8LL * nodes);
         if (verbose(o))
           for (int j = 0; j < 8; ++j)
             fprintf(stderr, "pdfs: phase %d sweep %d sn=%d octant change=%.3e (one launch: %.3f ms for 8 sweeps, "
                             "%lld of %lld brick visits)\n",
-                    which, j, (first + j) % 8 + 1, ch8[j], c->kern_ms - kms0, nb_act, 8 * bnodes);
+                    which, s + j, (first + s + j) % 8 + 1, ch8[j], c->kern_ms - kms0, nb_act, 8 * bnodes);
         st.voxel_updates += upd;
-        st.voxel_updates_fp64 += upd;
-        st.ms_kern_masked_fp64 += c->kern_ms - kms0;
-        st.updates_masked_fp64 += upd;
-        st.masked_sweeps_fp64 += 8;
+        if (which != 0) st.voxel_updates_fp64 += upd;
+        (which == 0 ? st.ms_kern_masked_fp32 : st.ms_kern_masked_fp64) += c->kern_ms - kms0;
+        (which == 0 ? st.updates_masked_fp32 : st.updates_masked_fp64) += upd;
+        (which == 0 ? st.masked_sweeps_fp32 : st.masked_sweeps_fp64) += 8;
         chg = ch8[7];
-        s = 8;
+        s += 8;
+        if (round32) {
+          ++oct_rounds;
+          const bool quiet = std::max(ch8[6], ch8[7]) <= 16.0 * tol;
+          if (quiet || oct_rounds == 3) {
+            if (!certify) break;  // the polish's full sweeps certify the fixed point
+            oct_done = true;      // full sweeps follow until one is within tol
+          }
+        }
         continue;
       }
       if (o.fixed_sweeps > 0 && s >= o.fixed_sweeps) break;
@@ -1260,7 +1281,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         break;
       }
       const int sn = (first + s) % 8 + 1;
-      const bool full = octant ? s >= 8 : (!sched || s < nfull || need_full);
+      const bool full = octant ? s >= 8 : (!sched || s < nfull || need_full);  // oct32: its full sweeps
       const uint8_t *act = nullptr;
       long long nact = c->nblocks;
       if (!full) {
@@ -1446,12 +1467,14 @@ extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) 
   return PDFS_OK;
 }
 
-// The polish's first cycle as one launch (an octant round on 16 x 16 x 16
-// bricks, tile3d.cuh OCT): orderings (first + j) % 8 + 1, j = 0..7, each over
-// the blocks its octant mask names.  chg: the 8 sweeps' max changes;
-// *active: the blocks visited, summed over the 8 sweeps.
-static int octant_round(pdfs_ctx *c, int first, double chg[8], long long *active) {
+// A cycle of 8 orderings as one launch (an octant round on bricks,
+// tile3d.cuh OCT): orderings (first + j) % 8 + 1, j = 0..7, each over the
+// blocks its octant mask (from the FP32 field) names.  which: 0 = FP32
+// min-update (16 x 16 x 32 bricks), 2 = the polish (16 x 16 x 16).  chg: the 8
+// sweeps' max changes; *active: the bricks visited, summed over the 8 sweeps.
+static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active) {
   const pdfs_grid &g = c->g;
+  const bool f32 = which == 0;
   CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack, INFINITY, c->nbx, c->nby,
                  c->nbz, c->omask, c->st));
   const uint8_t *bits = c->omask;
@@ -1460,14 +1483,15 @@ static int octant_round(pdfs_ctx *c, int first, double chg[8], long long *active
     bits = c->bact;
   }
   SweepArgs a;
-  fill_sweep_args(c, 2, first % 8 + 1, nullptr, nullptr, &a);
-  a.oct_first = first;
+  fill_sweep_args(c, which, first % 8 + 1, nullptr, nullptr, &a);
+  a.oct_first = first % 8;
   a.oct_bits = bits;
   a.oct_tbits = c->tact;
   a.maxchg = c->ochg;
   a.epoch = c->epoch + 1;  // sweep j publishes epoch + j
   c->epoch += 8;
-  const int nb = c->nt64[0] * c->nt64[1] * c->nt64[2];
+  const int *nt = f32 ? c->nt32 : c->nt64;
+  const int nb = nt[0] * nt[1] * nt[2];
   int *cnt_off = c->toct + 8 * (size_t)nb;
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
   CK(cudaMemsetAsync(c->ochg, 0, 8 * 8, c->st));
@@ -1479,7 +1503,7 @@ static int octant_round(pdfs_ctx *c, int first, double chg[8], long long *active
                                                        : ARITH_FAST;
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
-  CK(launch_octant_round(arith, iso, a, c->L64, c->toct, cnt_off, c->sms, c->st, &grid));
+  CK(launch_octant_round(which, arith, iso, a, f32 ? c->L32 : c->L64, c->toct, cnt_off, c->sms, c->st, &grid));
   CK(cudaEventRecord(c->k1, c->st));
   unsigned long long h[8];
   int cnt[8];
@@ -1492,7 +1516,14 @@ static int octant_round(pdfs_ctx *c, int first, double chg[8], long long *active
   if (c->hstat->err[0]) return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
   *active = 0;
   for (int j = 0; j < 8; ++j) {
-    std::memcpy(&chg[j], &h[j], 8);  // FP64 change words hold the double's bits (pairs: see change_u64)
+    if (f32) {  // float bits in the slot's low word
+      const unsigned b32 = (unsigned)h[j];
+      float f;
+      std::memcpy(&f, &b32, 4);
+      chg[j] = f;
+    } else {  // the double's bits (pairs: their hi word as a double)
+      std::memcpy(&chg[j], &h[j], 8);
+    }
     *active += (long long)cnt[j];
   }
   return PDFS_OK;

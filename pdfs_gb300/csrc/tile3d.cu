@@ -182,12 +182,12 @@ __global__ void k_oct_offsets(const int *__restrict__ cnt, int *__restrict__ off
   }
 }
 
-template <int ARITH, bool ISO>
+template <class T, int BZ, int MODE, int ARITH, bool ISO>
 static cudaError_t launch_oct(const SweepArgs &a, const Layout &L, int sms, cudaStream_t st, int *grid_used) {
-  using G = T3Geo<double, 16, 16>;
-  auto kern = t3_sweep_kernel<double, 16, 16, MODE_REPLACE, ARITH, ISO, true>;
+  using G = T3Geo<T, 16, BZ>;
+  auto kern = t3_sweep_kernel<T, 16, BZ, MODE, ARITH, ISO, true>;
   CUtensorMap m;
-  cudaError_t e = encode_field_map(&m, a.u, 8, L, a.nz + 2, G::W, G::RY, G::RZ);
+  cudaError_t e = encode_field_map(&m, a.u, sizeof(T), L, a.nz + 2, G::W, G::RY, G::RZ);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::BYTES);
   if (e != cudaSuccess) return e;
@@ -203,13 +203,16 @@ static cudaError_t launch_oct(const SweepArgs &a, const Layout &L, int sms, cuda
   return cudaGetLastError();
 }
 
-cudaError_t launch_octant_round(int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list, int *cnt_off,
-                                int sms, cudaStream_t st, int *g) {
+cudaError_t launch_octant_round(int which, int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list,
+                                int *cnt_off, int sms, cudaStream_t st, int *g) {
+  // FP32 min-update rounds on the FP32 masked bricks (16 x 16 x 32), FP64
+  // replace-update (polish) rounds on the FP64 ones (16 x 16 x 16)
+  const int bz = which == 0 ? 32 : 16;
   if (!a0.tflag || !a0.torder || !a0.oct_bits || !a0.oct_tbits || a0.ntx < 1 || L.ty != 16 || L.tx != 16 ||
-      L.xo != 0 || !a0.bcap64 || !a0.bcap32)
+      L.xo != 0 || which == 1 || (which == 2 && (!a0.bcap64 || !a0.bcap32)) || a0.ntz != (a0.nz + bz - 1) / bz)
     return cudaErrorInvalidValue;
   const int n = a0.ntx * a0.nty * a0.ntz;
-  k_brick_bits<<<std::min((n + 255) / 256, 4 * sms), 256, 0, st>>>(a0.ntx, a0.nty, a0.ntz, 2, 2, 2, a0.oct_bits,
+  k_brick_bits<<<std::min((n + 255) / 256, 4 * sms), 256, 0, st>>>(a0.ntx, a0.nty, a0.ntz, 2, 2, bz / 8, a0.oct_bits,
                                                                   a0.nbx, a0.nby, a0.nbz,
                                                                   const_cast<uint8_t *>(a0.oct_tbits));
   k_oct_tickets<<<8, 1024, 0, st>>>(a0.torder, a0.ntx, a0.nty, a0.ntz, a0.oct_first, a0.oct_tbits, list, cnt_off);
@@ -221,15 +224,20 @@ cudaError_t launch_octant_round(int arith, bool iso, const SweepArgs &a0, const 
   a.nticket = cnt_off + 8;
   a.blk_active = nullptr;
   a.tact = nullptr;
+  if (which == 0)
+    return iso ? launch_oct<float, 32, MODE_MIN, ARITH_FAST, true>(a, L, sms, st, g)
+               : launch_oct<float, 32, MODE_MIN, ARITH_FAST, false>(a, L, sms, st, g);
   switch (arith) {
     case ARITH_PAIR:
-      return iso ? launch_oct<ARITH_PAIR, true>(a, L, sms, st, g) : launch_oct<ARITH_PAIR, false>(a, L, sms, st, g);
+      return iso ? launch_oct<double, 16, MODE_REPLACE, ARITH_PAIR, true>(a, L, sms, st, g)
+                 : launch_oct<double, 16, MODE_REPLACE, ARITH_PAIR, false>(a, L, sms, st, g);
     case ARITH_MIXED:
-      return iso ? launch_oct<ARITH_MIXED, true>(a, L, sms, st, g) : launch_oct<ARITH_MIXED, false>(a, L, sms, st, g);
+      return iso ? launch_oct<double, 16, MODE_REPLACE, ARITH_MIXED, true>(a, L, sms, st, g)
+                 : launch_oct<double, 16, MODE_REPLACE, ARITH_MIXED, false>(a, L, sms, st, g);
     case ARITH_FAST:
-      return launch_oct<ARITH_FAST, false>(a, L, sms, st, g);
+      return launch_oct<double, 16, MODE_REPLACE, ARITH_FAST, false>(a, L, sms, st, g);
     case ARITH_REF:
-      return launch_oct<ARITH_REF, false>(a, L, sms, st, g);
+      return launch_oct<double, 16, MODE_REPLACE, ARITH_REF, false>(a, L, sms, st, g);
     default:
       return cudaErrorInvalidValue;
   }

@@ -417,8 +417,13 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       T v = tmax;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v = vmax_nonneg<T, ARITH>(v, __shfl_xor_sync(0xffffffffu, v, off));
-      if (lane == 0 && change_pos<T, ARITH>(v))
-        atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg) + osw, change_u64<T, ARITH>(v));
+      if (lane == 0 && change_pos<T, ARITH>(v)) {
+        if constexpr (sizeof(T) == 4)  // the low word of the sweep's 64-bit slot
+          atomicMax(reinterpret_cast<unsigned int *>(reinterpret_cast<unsigned long long *>(a.maxchg) + osw),
+                    __float_as_uint(v));
+        else
+          atomicMax(reinterpret_cast<unsigned long long *>(a.maxchg) + osw, change_u64<T, ARITH>(v));
+      }
       tmax = T(0);
     }
     // publish: the barrier orders every thread's stores before thread 0's

@@ -122,3 +122,58 @@ def test_octant_round_equals_sequential_masked_sweeps(aniso):
     assert (sa["sweeps_fp32"], sa["sweeps_fp64"]) == (sb["sweeps_fp32"], sb["sweeps_fp64"])
     assert sa["masked_sweeps_fp64"] == sb["masked_sweeps_fp64"] == 8
     assert a.tobytes() == b.tobytes()
+
+
+def test_fp32_octant_rounds_equal_sweep_by_sweep():
+    """PDFS_SCHED_OCTANT on an FP32 solve: a full first cycle, then cycles as
+    one-launch octant rounds (16 x 16 x 32 bricks) until a round's last two
+    sweeps change by at most 16 x 4e-6, then full sweeps to the tolerance.
+    Replayed here sweep by sweep through pdfs_ctx_sweep with the masks of
+    pdfs_ctx_orderings: the same bits."""
+    w = W.random_spheres(96, 80, 112, 1.0, 1.0, 1.0, 12, 3.0, 16.0, seed=46)
+    sp = (w.dx, w.dy, w.dz)
+    a = w.field.copy()
+    st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32, scheduler=L.SCHED_OCTANT)
+    assert st["masked_sweeps_fp32"] >= 8
+    with api.Context(w.nx, w.ny, w.nz, sp, freeze=L.FREEZE_MASK, precision=L.PREC_FP32) as c:
+        c.load(w.field, w.frozen)
+        s = 0
+        for _ in range(8):
+            c.sweep(s % 8 + 1)
+            s += 1
+        for _ in range(3):
+            bits = c.orderings()
+            ch = []
+            for _ in range(8):
+                sn = s % 8 + 1
+                ch.append(c.sweep(sn, active=((bits >> (sn - 1)) & 1).astype(np.uint8)))
+                s += 1
+            if max(ch[6], ch[7]) <= 16 * np.float32(4e-6):
+                break
+        while True:
+            chg = c.sweep(s % 8 + 1)
+            s += 1
+            if chg <= np.float32(4e-6):
+                break
+        b = np.empty_like(w.field)
+        c.store(b)
+    assert st["sweeps_fp32"] == s
+    assert a.tobytes() == b.tobytes()
+
+
+def test_octant_scheduler_headline_accuracy():
+    """The FP32 + pair polish solve under PDFS_SCHED_OCTANT: within 1e-6 of the
+    oracle's FP64 fixed point, fewer node updates than the unscheduled solve."""
+    w = W.random_spheres(128, 112, 96, 1.0, 1.0, 1.0, 10, 3.0, 20.0, seed=44)
+    sp = (w.dx, w.dy, w.dz)
+    kw = dict(frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-5)
+    a, b = w.field.copy(), w.field.copy()
+    sa = api.solve(a, sp, scheduler=L.SCHED_OCTANT, **kw)
+    sb = api.solve(b, sp, **kw)
+    ref = w.field.copy()
+    O.solve(ref, sp, tol=1e-12, frozen=w.frozen, threads=8)
+    i = (slice(1, -1),) * 3
+    err = float(np.max(np.abs(a[i] - ref[i]) / np.maximum(np.abs(ref[i]), 1.0)))
+    assert err <= 1e-6, err
+    assert sa["masked_sweeps_fp32"] >= 8 and sa["masked_sweeps_fp64"] == 8
+    assert sa["voxel_updates"] < sb["voxel_updates"]
