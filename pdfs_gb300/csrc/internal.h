@@ -117,6 +117,9 @@ cudaError_t octant_mask(const float *u32, const Layout &L, const uint32_t *fmask
 cudaError_t octant_active(const uint8_t *omask, int sn, int dilate, uint8_t *active, int nbx, int nby, int nbz,
                           int *count, int sms, cudaStream_t st);
 cudaError_t octant_union(const uint8_t *omask, uint8_t *out, int nbx, int nby, int nbz, int sms, cudaStream_t st);
+// nodes[j] += grid nodes of the blocks with bit j (ordering j + 1) set.
+cudaError_t octant_nodes(const uint8_t *bits, int nbx, int nby, int nbz, int nx, int ny, int nz,
+                         unsigned long long *nodes, int sms, cudaStream_t st);
 
 // Status words a sweep writes on the device (read back after each sweep).
 struct DevStatus {

@@ -172,6 +172,37 @@ __global__ void k_octant_union(const uint8_t *__restrict__ omask, uint8_t *__res
   }
 }
 
+// nodes[j] += the grid nodes of the blocks whose bit j is set (the node
+// updates a masked sweep of ordering j + 1 executes).
+__global__ void k_octant_nodes(const uint8_t *__restrict__ bits, int nbx, int nby, int nbz, int nx, int ny, int nz,
+                               unsigned long long *__restrict__ nodes) {
+  const long long n = (long long)nbx * nby * nbz;
+  unsigned long long local[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n; b += (long long)gridDim.x * blockDim.x) {
+    const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((long long)nbx * nby));
+    const unsigned long long v = (unsigned long long)min(8, nx - 8 * bx) * min(8, ny - 8 * by) * min(8, nz - 8 * bz);
+    const unsigned m = bits[b];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if ((m >> j) & 1u) local[j] += v;
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    unsigned long long v = local[j];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(nodes + j, v);
+  }
+}
+
+cudaError_t octant_nodes(const uint8_t *bits, int nbx, int nby, int nbz, int nx, int ny, int nz,
+                         unsigned long long *nodes, int sms, cudaStream_t st) {
+  const long long n = (long long)nbx * nby * nbz;
+  int grid = (int)std::min<long long>((n + 255) / 256, (long long)sms * 8);
+  if (grid < 1) grid = 1;
+  k_octant_nodes<<<grid, 256, 0, st>>>(bits, nbx, nby, nbz, nx, ny, nz, nodes);
+  return cudaGetLastError();
+}
+
 cudaError_t octant_union(const uint8_t *omask, uint8_t *out, int nbx, int nby, int nbz, int sms, cudaStream_t st) {
   const long long n = (long long)nbx * nby * nbz;
   int grid = (int)std::min<long long>((n + 255) / 256, (long long)sms * 8);

@@ -672,7 +672,7 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   c->oct64_ok = o.precision == PDFS_PREC_FP32_POLISH64 && s64.bz == 16 && s64.ty == 16 && s64.tx == 16;
   if (c->oct32_ok || c->oct64_ok) {
     want(&c->toct, (8 * std::max(bo[0].size(), bo[1].size()) + 17) * 4);
-    want(&c->ochg, 8 * 8);
+    want(&c->ochg, 16 * 8);
   }
   if (!wb.empty()) {
     want(&c->mlp_w, PDFS_MLP_PARAMS * 2);
@@ -979,7 +979,7 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
 }
 
 static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg);
-static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active);
+static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates);
 int pdfs::ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   return run_sweep(c, which, sn, active, blk_chg, chg);
 }
@@ -1245,14 +1245,12 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
       if (round64 || round32) {
         // a cycle of 8 orderings in one launch, each on its octant mask
         double ch8[8];
-        long long nb_act = 0;
+        long long nb_act = 0, upd = 0;
         const double kms0 = c->kern_ms;
-        int r = octant_round(c, which, (first + s) % 8, ch8, &nb_act);
+        int r = octant_round(c, which, (first + s) % 8, ch8, &nb_act, &upd);
         if (r) return r;
         const int *nt = which == 0 ? c->nt32 : c->nt64;
         const long long bnodes = (long long)nt[0] * nt[1] * nt[2];
-        // updates: the visited bricks' nodes, at most the grid's
-        const long long upd = std::min<long long>(nb_act * (which == 0 ? 8192LL : 4096LL), 8LL * nodes);
         if (verbose(o))
           for (int j = 0; j < 8; ++j)
             fprintf(stderr, "pdfs: phase %d sweep %d sn=%d octant change=%.3e (one launch: %.3f ms for 8 sweeps, "
@@ -1471,8 +1469,9 @@ extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) 
 // tile3d.cuh OCT): orderings (first + j) % 8 + 1, j = 0..7, each over the
 // blocks its octant mask (from the FP32 field) names.  which: 0 = FP32
 // min-update (16 x 16 x 32 bricks), 2 = the polish (16 x 16 x 16).  chg: the 8
-// sweeps' max changes; *active: the bricks visited, summed over the 8 sweeps.
-static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active) {
+// sweeps' max changes; *active: the bricks visited, summed over the 8 sweeps;
+// *updates: the node updates of the active blocks, summed alike.
+static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
   CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack, INFINITY, c->nbx, c->nby,
@@ -1494,8 +1493,9 @@ static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long l
   const int nb = nt[0] * nt[1] * nt[2];
   int *cnt_off = c->toct + 8 * (size_t)nb;
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
-  CK(cudaMemsetAsync(c->ochg, 0, 8 * 8, c->st));
+  CK(cudaMemsetAsync(c->ochg, 0, 16 * 8, c->st));  // 8 change words, 8 node counts
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
+  CK(octant_nodes(bits, c->nbx, c->nby, c->nbz, g.nx, g.ny, g.nz, c->ochg + 8, c->sms, c->st));
   const bool iso = g.dx == g.dy && g.dy == g.dz;
   const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF
                     : c->o.arith == PDFS_ARITH_MIXED   ? ARITH_MIXED
@@ -1505,16 +1505,18 @@ static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long l
   CK(cudaEventRecord(c->k0, c->st));
   CK(launch_octant_round(which, arith, iso, a, f32 ? c->L32 : c->L64, c->toct, cnt_off, c->sms, c->st, &grid));
   CK(cudaEventRecord(c->k1, c->st));
-  unsigned long long h[8];
+  unsigned long long h[16];
   int cnt[8];
   CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(h, c->ochg, sizeof h, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(cnt, cnt_off, sizeof cnt, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   c->kern_ms += ms_between(c->k0, c->k1);
-  c->launches += 5 + (kOctDilate ? 1 : 0);
+  c->launches += 6 + (kOctDilate ? 1 : 0);
   if (c->hstat->err[0]) return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
   *active = 0;
+  *updates = 0;
+  for (int j = 0; j < 8; ++j) *updates += (long long)h[8 + (first + j) % 8];  // sweep j runs ordering first + j + 1
   for (int j = 0; j < 8; ++j) {
     if (f32) {  // float bits in the slot's low word
       const unsigned b32 = (unsigned)h[j];

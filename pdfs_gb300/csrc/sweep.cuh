@@ -240,6 +240,12 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
       "l"(map), "r"(x), "r"(y), "r"(z), "r"(saddr(bar))
       : "memory");
 }
+// An L2 prefetch of a tensor-map box (no shared memory, no completion).
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap *map, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];\n" ::"l"(map), "r"(x), "r"(y),
+               "r"(z)
+               : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 __device__ __forceinline__ int ld_acquire_gpu(const int *p) {
   int v;
