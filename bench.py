@@ -574,22 +574,29 @@ def main():
     vu64 = st["voxel_updates_fp64"]
     vu32 = st["voxel_updates"] - vu64
     parts = []
+    # octant rounds run a masked cycle of 8 sweeps as one launch
+    per_round = 8 if args.scheduler == "octant" or (args.scheduler in ("change", "learned") and
+                                                    prec == L.PREC_FP32_POLISH64) else 1
     for phase, kt, kmask, n, nmask, upd, umask, per in (
             ("fp32", k32, st["ms_kern_masked_fp32"], s32, st["masked_sweeps_fp32"], vu32,
              st["updates_masked_fp32"], 8 + mask_b),
             ("fp64", k64, st["ms_kern_masked_fp64"], s64, st["masked_sweeps_fp64"], vu64,
              st["updates_masked_fp64"], 16 + mask_b)):
         if n - nmask > 0:
-            parts.append({"phase": phase, "kind": "full", "ms": kt - kmask, "launches": n - nmask,
-                          "updates": upd - umask, "bytes_per_update": per})
+            parts.append({"phase": phase, "kind": "full", "ms": kt - kmask, "sweeps": n - nmask,
+                          "launches": n - nmask, "updates": upd - umask, "bytes_per_update": per})
         if nmask > 0:
-            parts.append({"phase": phase, "kind": "masked", "ms": kmask, "launches": nmask, "updates": umask,
-                          "bytes_per_update": per})
+            rounds = (phase == "fp64" and per_round == 8) or (phase == "fp32" and args.scheduler == "octant")
+            parts.append({"phase": phase, "kind": "masked", "ms": kmask, "sweeps": nmask,
+                          "launches": max(1, nmask // 8) if rounds else nmask, "updates": umask,
+                          "bytes_per_update": per, "one_launch_per_8_sweeps": rounds})
     for q in parts:
         q["kernel"] = kernel_name(q["phase"], st["tile"], prec, arith) if q["kind"] == "full" else \
             ("t3_sweep_kernel<float, 16, 32, MIN, FAST>" if q["phase"] == "fp32" else
              f"t3_sweep_kernel<double, 16, 16, {'REPLACE' if prec == L.PREC_FP32_POLISH64 else 'MIN'}, "
              f"{ {L.ARITH_PAIR: 'PAIR', L.ARITH_MIXED: 'MIXED', L.ARITH_FAST: 'FAST'}.get(arith, 'REF')}>")
+        if q.get("one_launch_per_8_sweeps"):
+            q["kernel"] = q["kernel"][:-1] + ", octant round>"
         q["ms_per_launch"] = q["ms"] / q["launches"]
         q["achieved_gbs"] = q["updates"] * q["bytes_per_update"] / (q["ms"] / 1e3) / 1e9 if q["ms"] > 0 else 0.0
         q["frac"] = q["achieved_gbs"] / hbm
