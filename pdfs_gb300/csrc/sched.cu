@@ -57,18 +57,21 @@ cudaError_t sched_change(const unsigned int *ring, int cur, int hist, float thr,
 // both directions where the update does not use it (its smaller neighbour is
 // not below the node) or where its two neighbours differ by at most
 // slack * h (a characteristic nearly parallel to the faces).  Frozen nodes
-// and nodes not yet reached (>= far) accept none.  One warp covers four
-// blocks along x, lane = node x offset.
-__global__ void k_octant_mask(const float *__restrict__ u, Layout L, const uint32_t *__restrict__ fmask,
-                              MaskLayout M, int nx, int ny, int nz, float hx, float hy, float hz, float slack,
-                              float far, int nbx, int nby, int nbz, uint8_t *__restrict__ omask) {
-  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+// and nodes not yet reached (>= far) accept none.
+__global__ void __launch_bounds__(256) k_octant_mask(const float *__restrict__ u, Layout L,
+                                                     const uint32_t *__restrict__ fmask, MaskLayout M, int nx, int ny,
+                                                     int nz, float hx, float hy, float hz, float slack, float far,
+                                                     int nbx, int nby, int nbz, uint8_t *__restrict__ omask) {
+  // one CTA per 4 x 1 x 1 blocks (32 x of one block row and plane): warp w
+  // takes row y = 8 by + w + 1, lane = x offset, and walks the block's 8 planes
+  // with a window along z held in registers
+  __shared__ unsigned s_c[8][4];
   const int nwx = (nbx + 3) / 4;
-  if (wid >= (long long)nwx * nby * nbz) return;  // whole warps leave together
-  const int wx = (int)(wid % nwx), by = (int)((wid / nwx) % nby), bz = (int)(wid / ((long long)nwx * nby));
-  const int x = 1 + wx * 32 + lane;
-  const bool have = x <= nx + 1;  // the node, or the halo node right of the grid
+  const int wx = (int)(blockIdx.x % nwx), by = (int)((blockIdx.x / nwx) % nby), bz = (int)(blockIdx.x / ((long long)nwx * nby));
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int x = 1 + wx * 32 + lane, y = 1 + by * 8 + w;
+  const bool row = y <= ny;
+  const bool have = row && x <= nx + 1;  // the node, or the halo node right of the grid
   // accepted directions of one axis: bit 0 ascending, bit 1 descending
   auto axis = [](float c, float lo, float hi, float tie) -> unsigned {
     const float m = fminf(lo, hi);
@@ -79,35 +82,41 @@ __global__ void k_octant_mask(const float *__restrict__ u, Layout L, const uint3
   // the (x, y, z) direction sets met in the block, as 27 bits: bit 9(ax-1) + 3(ay-1) + (az-1)
   unsigned combos = 0;
   const int z0 = 1 + bz * 8, z1 = min(nz, bz * 8 + 8);
-  for (int y = 1 + by * 8; y <= min(ny, by * 8 + 8); ++y) {
-    // a sliding window along z: the planes below, at and above the node
-    float cm = have ? at(x, y, z0 - 1) : INFINITY;
-    float c = have ? at(x, y, z0) : INFINITY;
-    for (int z = z0; z <= z1; ++z) {
-      const float cp = have ? at(x, y, z + 1) : INFINITY;
-      // x neighbours from the adjacent lanes; the warp's edge lanes read theirs
-      float xl = __shfl_up_sync(0xffffffffu, c, 1), xr = __shfl_down_sync(0xffffffffu, c, 1);
-      if (lane == 0 && have) xl = at(x - 1, y, z);
-      if (lane == 31 && x <= nx) xr = at(x + 1, y, z);
-      // frozen bits of the warp's 32 x: one word, when the warp holds a grid node
-      const unsigned fw = (fmask && 1 + wx * 32 <= nx) ? fmask[M.word(1 + wx * 32, y, z)] : 0u;
-      if (x <= nx && !((fw >> lane) & 1u) && c < far) {
-        const unsigned ax = axis(c, xl, xr, slack * hx);
-        const unsigned ay = axis(c, at(x, y - 1, z), at(x, y + 1, z), slack * hy);
-        const unsigned az = axis(c, cm, cp, slack * hz);
-        combos |= 1u << ((ax - 1) * 9 + (ay - 1) * 3 + (az - 1));
-      }
-      cm = c;
-      c = cp;
+  const bool wgrid = row && 1 + wx * 32 <= nx;  // the warp holds grid nodes (its frozen word exists)
+  float cm = have ? at(x, y, z0 - 1) : INFINITY;
+  float c = have ? at(x, y, z0) : INFINITY;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int z = z0 + k;
+    const bool zin = z <= z1;
+    const float cp = (have && zin) ? at(x, y, z + 1) : INFINITY;
+    // x neighbours from the adjacent lanes; the warp's edge lanes read theirs
+    float xl = __shfl_up_sync(0xffffffffu, c, 1), xr = __shfl_down_sync(0xffffffffu, c, 1);
+    if (lane == 0 && have && zin) xl = at(x - 1, y, z);
+    if (lane == 31 && x <= nx && row && zin) xr = at(x + 1, y, z);
+    // frozen bits of the warp's 32 x: one word
+    const unsigned fw = (fmask && wgrid && zin) ? fmask[M.word(1 + wx * 32, y, z)] : 0u;
+    if (zin && row && x <= nx && !((fw >> lane) & 1u) && c < far) {
+      const unsigned ax = axis(c, xl, xr, slack * hx);
+      const unsigned ay = axis(c, at(x, y - 1, z), at(x, y + 1, z), slack * hy);
+      const unsigned az = axis(c, cm, cp, slack * hz);
+      combos |= 1u << ((ax - 1) * 9 + (ay - 1) * 3 + (az - 1));
     }
+    cm = c;
+    c = cp;
   }
 #pragma unroll
   for (int off = 1; off < 8; off <<= 1) combos |= __shfl_xor_sync(0xffffffffu, combos, off);
-  const int bx = wx * 4 + (lane >> 3);
-  if ((lane & 7) == 0 && bx < nbx) {
+  if ((lane & 7) == 0) s_c[w][lane >> 3] = combos;
+  __syncthreads();
+  const int bx = wx * 4 + threadIdx.x;
+  if (threadIdx.x < 4 && bx < nbx) {
+    unsigned all = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) all |= s_c[k][threadIdx.x];
     unsigned acc = 0;
     for (int k = 0; k < 27; ++k) {
-      if (!((combos >> k) & 1u)) continue;
+      if (!((all >> k) & 1u)) continue;
       const unsigned ax = k / 9 + 1, ay = (k / 3) % 3 + 1, az = k % 3 + 1;
 #pragma unroll
       for (int sn = 1; sn <= 8; ++sn) {
@@ -118,6 +127,83 @@ __global__ void k_octant_mask(const float *__restrict__ u, Layout L, const uint3
       }
     }
     omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)acc;
+  }
+}
+
+// The same masks from a shared-memory copy of the field: one CTA per
+// 16 x 16 x 8 region (2 x 2 blocks), its box with a one-node halo fetched by
+// one TMA copy, thread (lx, ly) walking its column's 8 planes.  For the
+// layouts whose interior x starts 16-byte aligned (pencils, bricks).
+constexpr int kOmW = 20, kOmRY = 18, kOmRZ = 10;  // box: x0-1 .. x0+16 rounded to 16 bytes, y0-1 .. y0+16, z0-1 .. z0+8
+__global__ void __launch_bounds__(256) k_octant_mask_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict__ fmask,
+                                                         MaskLayout M, int nx, int ny, int nz, float hx, float hy,
+                                                         float hz, float slack, float far, int nbx, int nby, int nbz,
+                                                         uint8_t *__restrict__ omask) {
+  __shared__ __align__(128) float box[kOmRZ][kOmRY][kOmW];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ unsigned s_c[4];
+  const int nrx = (nbx + 1) / 2, nry = (nby + 1) / 2;
+  const int rx = (int)(blockIdx.x % nrx), ry = (int)((blockIdx.x / nrx) % nry), bz = (int)(blockIdx.x / ((long long)nrx * nry));
+  const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
+  const int x0 = 1 + 16 * rx, y0 = 1 + 16 * ry, z0 = 1 + 8 * bz;
+  if (tid < 4) s_c[tid] = 0u;
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_arrive_tx(&bar, (unsigned)sizeof(box));
+    tma_load_3d(&box[0][0][0], &tm, x0 - 1, y0 - 1, z0 - 1, &bar);
+  }
+  // bounded wait for the copy; on expiry every ordering is kept (always safe)
+  bool landed = mbar_try(&bar, 0);
+  if (!landed) {
+    const long long t0 = clock64();
+    while (!(landed = mbar_try(&bar, 0)) && clock64() - t0 < 4000000000ll) {
+    }
+  }
+  auto axis = [](float c, float lo, float hi, float tie) -> unsigned {
+    const float m = fminf(lo, hi);
+    if (!(m < c) || fabsf(lo - hi) <= tie) return 3u;
+    return lo < hi ? 1u : 2u;
+  };
+  unsigned combos = 0;
+  const int x = x0 + lx, y = y0 + ly;
+  if (landed && x <= nx && y <= ny) {
+    const int z1 = min(nz, z0 + 7);
+    for (int z = z0; z <= z1; ++z) {
+      const int k = z - z0 + 1;
+      if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
+      const float c = fabsf(box[k][ly + 1][lx + 1]);
+      if (!(c < far)) continue;
+      const unsigned ax = axis(c, fabsf(box[k][ly + 1][lx]), fabsf(box[k][ly + 1][lx + 2]), slack * hx);
+      const unsigned ay = axis(c, fabsf(box[k][ly][lx + 1]), fabsf(box[k][ly + 2][lx + 1]), slack * hy);
+      const unsigned az = axis(c, fabsf(box[k - 1][ly + 1][lx + 1]), fabsf(box[k + 1][ly + 1][lx + 1]), slack * hz);
+      combos |= 1u << ((ax - 1) * 9 + (ay - 1) * 3 + (az - 1));
+    }
+  }
+  // the 4 blocks' direction sets: lanes of a warp share a block row of 8 x
+  if (combos) atomicOr(&s_c[((ly >> 3) << 1) | (lx >> 3)], combos);
+  __syncthreads();
+  if (tid < 4) {
+    const int bx = 2 * rx + (tid & 1), by = 2 * ry + (tid >> 1);
+    if (bx < nbx && by < nby) {
+      const unsigned all = landed ? s_c[tid] : 0x7ffffffu;
+      unsigned acc = 0;
+      for (int k = 0; k < 27; ++k) {
+        if (!((all >> k) & 1u)) continue;
+        const unsigned ax = k / 9 + 1, ay = (k / 3) % 3 + 1, az = k % 3 + 1;
+#pragma unroll
+        for (int sn = 1; sn <= 8; ++sn) {
+          int sx, sy, sz;
+          ordering_signs(sn, &sx, &sy, &sz);
+          if ((ax & (sx > 0 ? 1u : 2u)) && (ay & (sy > 0 ? 1u : 2u)) && (az & (sz > 0 ? 1u : 2u)))
+            acc |= 1u << (sn - 1);
+        }
+      }
+      omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)acc;
+    }
   }
 }
 
@@ -147,10 +233,18 @@ __global__ void k_octant_active(const uint8_t *__restrict__ omask, int sn, int d
 cudaError_t octant_mask(const float *u32, const Layout &L, const uint32_t *fmask, const MaskLayout &M,
                         const pdfs_grid &g, float slack, float far, int nbx, int nby, int nbz, uint8_t *omask,
                         cudaStream_t st) {
-  const long long warps = (long long)((nbx + 3) / 4) * nby * nbz;
-  const int grid = (int)((warps * 32 + 255) / 256);
-  k_octant_mask<<<grid, 256, 0, st>>>(u32, L, fmask, M, g.nx, g.ny, g.nz, (float)g.dx, (float)g.dy, (float)g.dz, slack,
-                                      far, nbx, nby, nbz, omask);
+  if (L.xo == 0 && !L.zc && L.tx % 16 == 0) {  // the box's x start is 16-byte aligned: the TMA kernel
+    CUtensorMap m;
+    cudaError_t e = encode_field_map(&m, (void *)u32, 4, L, g.nz + 2, kOmW, kOmRY, kOmRZ);
+    if (e != cudaSuccess) return e;
+    const long long ctas = (long long)((nbx + 1) / 2) * ((nby + 1) / 2) * nbz;
+    k_octant_mask_tma<<<(unsigned)ctas, 256, 0, st>>>(m, fmask, M, g.nx, g.ny, g.nz, (float)g.dx, (float)g.dy,
+                                                      (float)g.dz, slack, far, nbx, nby, nbz, omask);
+    return cudaGetLastError();
+  }
+  const long long ctas = (long long)((nbx + 3) / 4) * nby * nbz;
+  k_octant_mask<<<(unsigned)ctas, 256, 0, st>>>(u32, L, fmask, M, g.nx, g.ny, g.nz, (float)g.dx, (float)g.dy,
+                                                (float)g.dz, slack, far, nbx, nby, nbz, omask);
   return cudaGetLastError();
 }
 
