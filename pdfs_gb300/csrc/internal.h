@@ -143,13 +143,19 @@ constexpr int kRing = kHist + 1;
 // The learned scheduler recomputes its band feature every kBandEvery
 // scheduled sweeps (a pass over the field each time).
 constexpr int kBandEvery = 4;
-// Polish octant masks: an axis whose two neighbours differ by at most
-// kOctSlack * h accepts both sweep directions; kOctDilate = 1 adds each
-// block's face neighbours' orderings.  Measured on the 768^3 headline grid
-// (polish time, polish sweeps): slack 0.25 without dilation 54.4 ms, 10;
-// with it 52.1 ms, 9 (one masked cycle and one certifying full sweep); slack
-// 0.5 56.4 / 57.3 ms; slack 1.0 59.0 / 64.8 ms; unscheduled 62.0 ms, 9.
-constexpr float kOctSlack = 0.25f;
+// Octant masks: an axis whose two neighbours differ by at most kOctSlack * h
+// accepts both sweep directions (FP32 rounds / the polish); kOctDilate = 1
+// adds each block's face neighbours' orderings.  Measured on the 768^3
+// headline grid under the octant scheduler (solve time; always 16 FP32 and 9
+// polish sweeps): FP32 slack 0.25 with polish slack 0.25 102.0 ms, 0.15 100.4,
+// 0.1 99.9, 0.05 99.5, 0 99.1 ms (0.05 keeps a margin for the characteristics
+// nearly parallel to a face); FP32 slack 0.2 / 0.3 within 0.3 ms of 0.25, 0.1
+// needs a second FP32 round (122.6 ms), 0.5 103.0 ms; without the
+// widening the FP32 phase needs a second round (127 ms).  Earlier, for the
+// polish alone run one masked sweep at a time: slack 0.25 widened 52.1 ms and
+// 9 sweeps, not widened 54.4 ms and 10; slack 0.5 56.4 / 57.3 ms.
+constexpr float kOctSlack32 = 0.25f;
+constexpr float kOctSlack64 = 0.05f;
 constexpr int kOctDilate = 1;
 
 // Weights of the learned scheduler compiled into the library (a blob of

@@ -1230,8 +1230,8 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     if (sched) CK(cudaMemsetAsync(c->bchg, 0, (size_t)c->nblocks * kRing * 4, c->st));
     if (sched || octant) CK(cudaMemsetAsync(&c->dstat->sched_err, 0, 4, c->st));
     if (octant && !c->oct64_ok) {  // the masks of the one-launch-per-sweep path (the round computes its own)
-      CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack, INFINITY, c->nbx, c->nby,
-                     c->nbz, c->omask, c->st));
+      CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack64, INFINITY, c->nbx,
+                     c->nby, c->nbz, c->omask, c->st));
       c->launches++;
     }
     bool need_full = true;
@@ -1474,8 +1474,8 @@ extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) 
 static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
-  CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, kOctSlack, INFINITY, c->nbx, c->nby,
-                 c->nbz, c->omask, c->st));
+  CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, f32 ? kOctSlack32 : kOctSlack64, INFINITY,
+                 c->nbx, c->nby, c->nbz, c->omask, c->st));
   const uint8_t *bits = c->omask;
   if (kOctDilate) {
     CK(octant_union(c->omask, c->bact, c->nbx, c->nby, c->nbz, c->sms, c->st));
@@ -1535,8 +1535,8 @@ extern "C" int pdfs_ctx_orderings(pdfs_ctx *c, uint8_t *orderings) {
   if (!c || !c->loaded || !c->u32 || !c->omask || !orderings || c->last_prec < 0) return PDFS_ERR_INVALID;
   CK(cudaSetDevice(c->dev));
   const uint8_t *buf = c->omask;
-  CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, c->g, kOctSlack, INFINITY, c->nbx, c->nby,
-                 c->nbz, c->omask, c->st));
+  CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, c->g, kOctSlack32, INFINITY, c->nbx,
+                 c->nby, c->nbz, c->omask, c->st));
   if (kOctDilate) {  // the polish's widened masks: bit sn of a block or of a face neighbour
     CK(octant_union(c->omask, c->bact, c->nbx, c->nby, c->nbz, c->sms, c->st));
     buf = c->bact;
