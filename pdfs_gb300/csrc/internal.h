@@ -97,6 +97,8 @@ cudaError_t launch_sweep_lanecol(int which, int rows, bool iso, const LcArgs &a,
 // update (16 x 16 x 16).  a0 as for such a sweep, with oct_first, oct_bits
 // (per block) and oct_tbits (per brick, filled here) set, a0.epoch the first of
 // 8 epochs and a0.maxchg 8 change words; list: 8 x bricks ints, cnt_off: 17 ints.
+// ints of an octant round's ticket scratch (pdfs_ctx::toct) for ntx x nty x ntz bricks
+int octant_scratch_ints(int ntx, int nty, int ntz);
 cudaError_t launch_octant_round(int which, int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list,
                                 int *cnt_off, int sms, cudaStream_t st, int *grid_used);
 // Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
@@ -223,7 +225,8 @@ struct pdfs_ctx {
   unsigned int *bchg = nullptr;  // [kRing][nblocks] float bits of per-block max change, rotating
   uint8_t *bact = nullptr;       // [nblocks] active mask of the next sweep
   uint8_t *omask = nullptr;      // [nblocks] polish: the orderings that matter to each block
-  int *toct = nullptr;           // octant rounds: [8][bricks] tickets, then 17 counts / offsets
+  int *toct = nullptr;           // octant rounds: [8][bricks] tickets, 17 counts / offsets, the merged
+                                 // ticket list and its plan (octant_scratch_ints)
   bool oct32_ok = false, oct64_ok = false;  // octant rounds available (FP32 / polish brick shapes)
   unsigned long long *ochg = nullptr;  // its 8 change words
   float *bmin = nullptr;         // [nblocks] per-block field minimum (learned scheduler)

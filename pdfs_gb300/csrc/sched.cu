@@ -58,6 +58,38 @@ cudaError_t sched_change(const unsigned int *ring, int cur, int hist, float thr,
 // not below the node) or where its two neighbours differ by at most
 // slack * h (a characteristic nearly parallel to the faces).  Frozen nodes
 // and nodes not yet reached (>= far) accept none.
+
+// The orderings that sweep axis `axis` (0 x, 1 y, 2 z) in direction `sign`,
+// one bit per ordering (bit sn-1), from ordering_signs' table.
+__host__ __device__ constexpr unsigned orderings_along(int axis, int sign) {
+  unsigned m = 0;
+  for (int sn = 1; sn <= 8; ++sn) {
+    const int desc = (sn == 2 || sn == 5 || sn == 7 || sn == 8) ? -1 : 1;
+    const int s = axis == 0 ? ((sn == 4 || sn == 8) ? -1 : 1) * desc
+                  : axis == 1 ? ((sn == 2 || sn == 6) ? -1 : 1) * desc
+                              : ((sn == 3 || sn == 7) ? -1 : 1) * desc;
+    if (s == sign) m |= 1u << (sn - 1);
+  }
+  return m;
+}
+
+// accepted directions of one axis: bit 0 ascending, bit 1 descending
+__device__ __forceinline__ unsigned octant_axis(float c, float lo, float hi, float tie) {
+  const float m = fminf(lo, hi);
+  if (!(m < c) || fabsf(lo - hi) <= tie) return 3u;
+  return lo < hi ? 1u : 2u;
+}
+
+// the orderings a node with direction sets (ax, ay, az) accepts
+__device__ __forceinline__ unsigned octant_orderings(unsigned ax, unsigned ay, unsigned az) {
+  constexpr unsigned XP = orderings_along(0, 1), XM = orderings_along(0, -1);
+  constexpr unsigned YP = orderings_along(1, 1), YM = orderings_along(1, -1);
+  constexpr unsigned ZP = orderings_along(2, 1), ZM = orderings_along(2, -1);
+  static_assert((XP | XM) == 0xffu && (XP & XM) == 0u && (YP & ZP & XP) == 1u, "ordering table");
+  return (((ax & 1u) ? XP : 0u) | ((ax & 2u) ? XM : 0u)) & (((ay & 1u) ? YP : 0u) | ((ay & 2u) ? YM : 0u)) &
+         (((az & 1u) ? ZP : 0u) | ((az & 2u) ? ZM : 0u));
+}
+
 __global__ void __launch_bounds__(256) k_octant_mask(const float *__restrict__ u, Layout L,
                                                      const uint32_t *__restrict__ fmask, MaskLayout M, int nx, int ny,
                                                      int nz, float hx, float hy, float hz, float slack, float far,
@@ -72,15 +104,8 @@ __global__ void __launch_bounds__(256) k_octant_mask(const float *__restrict__ u
   const int x = 1 + wx * 32 + lane, y = 1 + by * 8 + w;
   const bool row = y <= ny;
   const bool have = row && x <= nx + 1;  // the node, or the halo node right of the grid
-  // accepted directions of one axis: bit 0 ascending, bit 1 descending
-  auto axis = [](float c, float lo, float hi, float tie) -> unsigned {
-    const float m = fminf(lo, hi);
-    if (!(m < c) || fabsf(lo - hi) <= tie) return 3u;
-    return lo < hi ? 1u : 2u;
-  };
   auto at = [&](int xx, int yy, int zz) { return fabsf(u[L.index(xx, yy, zz)]); };
-  // the (x, y, z) direction sets met in the block, as 27 bits: bit 9(ax-1) + 3(ay-1) + (az-1)
-  unsigned combos = 0;
+  unsigned acc = 0;  // the orderings my nodes accept
   const int z0 = 1 + bz * 8, z1 = min(nz, bz * 8 + 8);
   const bool wgrid = row && 1 + wx * 32 <= nx;  // the warp holds grid nodes (its frozen word exists)
   float cm = have ? at(x, y, z0 - 1) : INFINITY;
@@ -96,37 +121,23 @@ __global__ void __launch_bounds__(256) k_octant_mask(const float *__restrict__ u
     if (lane == 31 && x <= nx && row && zin) xr = at(x + 1, y, z);
     // frozen bits of the warp's 32 x: one word
     const unsigned fw = (fmask && wgrid && zin) ? fmask[M.word(1 + wx * 32, y, z)] : 0u;
-    if (zin && row && x <= nx && !((fw >> lane) & 1u) && c < far) {
-      const unsigned ax = axis(c, xl, xr, slack * hx);
-      const unsigned ay = axis(c, at(x, y - 1, z), at(x, y + 1, z), slack * hy);
-      const unsigned az = axis(c, cm, cp, slack * hz);
-      combos |= 1u << ((ax - 1) * 9 + (ay - 1) * 3 + (az - 1));
-    }
+    if (zin && row && x <= nx && !((fw >> lane) & 1u) && c < far)
+      acc |= octant_orderings(octant_axis(c, xl, xr, slack * hx),
+                              octant_axis(c, at(x, y - 1, z), at(x, y + 1, z), slack * hy),
+                              octant_axis(c, cm, cp, slack * hz));
     cm = c;
     c = cp;
   }
 #pragma unroll
-  for (int off = 1; off < 8; off <<= 1) combos |= __shfl_xor_sync(0xffffffffu, combos, off);
-  if ((lane & 7) == 0) s_c[w][lane >> 3] = combos;
+  for (int off = 1; off < 8; off <<= 1) acc |= __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((lane & 7) == 0) s_c[w][lane >> 3] = acc;
   __syncthreads();
   const int bx = wx * 4 + threadIdx.x;
   if (threadIdx.x < 4 && bx < nbx) {
     unsigned all = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) all |= s_c[k][threadIdx.x];
-    unsigned acc = 0;
-    for (int k = 0; k < 27; ++k) {
-      if (!((all >> k) & 1u)) continue;
-      const unsigned ax = k / 9 + 1, ay = (k / 3) % 3 + 1, az = k % 3 + 1;
-#pragma unroll
-      for (int sn = 1; sn <= 8; ++sn) {
-        int sx, sy, sz;
-        ordering_signs(sn, &sx, &sy, &sz);
-        if ((ax & (sx > 0 ? 1u : 2u)) && (ay & (sy > 0 ? 1u : 2u)) && (az & (sz > 0 ? 1u : 2u)))
-          acc |= 1u << (sn - 1);
-      }
-    }
-    omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)acc;
+    omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)all;
   }
 }
 
@@ -144,7 +155,7 @@ __global__ void __launch_bounds__(256) k_octant_mask_tma(const __grid_constant__
   __shared__ unsigned s_c[4];
   const int nrx = (nbx + 1) / 2, nry = (nby + 1) / 2;
   const int rx = (int)(blockIdx.x % nrx), ry = (int)((blockIdx.x / nrx) % nry), bz = (int)(blockIdx.x / ((long long)nrx * nry));
-  const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4;
+  const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4, lane = tid & 31;
   const int x0 = 1 + 16 * rx, y0 = 1 + 16 * ry, z0 = 1 + 8 * bz;
   if (tid < 4) s_c[tid] = 0u;
   if (tid == 0) {
@@ -163,13 +174,8 @@ __global__ void __launch_bounds__(256) k_octant_mask_tma(const __grid_constant__
     while (!(landed = mbar_try(&bar, 0)) && clock64() - t0 < 4000000000ll) {
     }
   }
-  auto axis = [](float c, float lo, float hi, float tie) -> unsigned {
-    const float m = fminf(lo, hi);
-    if (!(m < c) || fabsf(lo - hi) <= tie) return 3u;
-    return lo < hi ? 1u : 2u;
-  };
-  unsigned combos = 0;
   const int x = x0 + lx, y = y0 + ly;
+  unsigned acc = 0;  // the orderings my nodes accept
   if (landed && x <= nx && y <= ny) {
     const int z1 = min(nz, z0 + 7);
     for (int z = z0; z <= z1; ++z) {
@@ -177,33 +183,22 @@ __global__ void __launch_bounds__(256) k_octant_mask_tma(const __grid_constant__
       if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
       const float c = fabsf(box[k][ly + 1][lx + 1]);
       if (!(c < far)) continue;
-      const unsigned ax = axis(c, fabsf(box[k][ly + 1][lx]), fabsf(box[k][ly + 1][lx + 2]), slack * hx);
-      const unsigned ay = axis(c, fabsf(box[k][ly][lx + 1]), fabsf(box[k][ly + 2][lx + 1]), slack * hy);
-      const unsigned az = axis(c, fabsf(box[k - 1][ly + 1][lx + 1]), fabsf(box[k + 1][ly + 1][lx + 1]), slack * hz);
-      combos |= 1u << ((ax - 1) * 9 + (ay - 1) * 3 + (az - 1));
+      acc |= octant_orderings(
+          octant_axis(c, fabsf(box[k][ly + 1][lx]), fabsf(box[k][ly + 1][lx + 2]), slack * hx),
+          octant_axis(c, fabsf(box[k][ly][lx + 1]), fabsf(box[k][ly + 2][lx + 1]), slack * hy),
+          octant_axis(c, fabsf(box[k - 1][ly + 1][lx + 1]), fabsf(box[k + 1][ly + 1][lx + 1]), slack * hz));
     }
   }
-  // the 4 blocks' direction sets: lanes of a warp share a block row of 8 x
-  if (combos) atomicOr(&s_c[((ly >> 3) << 1) | (lx >> 3)], combos);
+  // the 4 blocks: lanes 0-7 and 16-23 of a warp (rows 2w, 2w + 1) hold x block
+  // 2 rx, lanes 8-15 and 24-31 x block 2 rx + 1; both rows are in y block ly / 8
+#pragma unroll
+  for (int off = 1; off <= 16; off <<= 1)
+    if (off != 8) acc |= __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((lane & 23) == 0 && acc) atomicOr(&s_c[((ly >> 3) << 1) | (lane >> 3)], acc);
   __syncthreads();
   if (tid < 4) {
     const int bx = 2 * rx + (tid & 1), by = 2 * ry + (tid >> 1);
-    if (bx < nbx && by < nby) {
-      const unsigned all = landed ? s_c[tid] : 0x7ffffffu;
-      unsigned acc = 0;
-      for (int k = 0; k < 27; ++k) {
-        if (!((all >> k) & 1u)) continue;
-        const unsigned ax = k / 9 + 1, ay = (k / 3) % 3 + 1, az = k % 3 + 1;
-#pragma unroll
-        for (int sn = 1; sn <= 8; ++sn) {
-          int sx, sy, sz;
-          ordering_signs(sn, &sx, &sy, &sz);
-          if ((ax & (sx > 0 ? 1u : 2u)) && (ay & (sy > 0 ? 1u : 2u)) && (az & (sz > 0 ? 1u : 2u)))
-            acc |= 1u << (sn - 1);
-        }
-      }
-      omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)acc;
-    }
+    if (bx < nbx && by < nby) omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)(landed ? s_c[tid] : 0xffu);
   }
 }
 

@@ -128,10 +128,22 @@ __global__ void k_unpack(const T *__restrict__ src, Layout L, const double *__re
 }
 
 // internal layout of S -> internal layout of D, every halo-padded node
+// (one warp per halo-padded row: row r = blockIdx.x * 8 + warp is (y, z) =
+// (r % (ny + 2), r / (ny + 2)))
+constexpr int kRowWarps = 8;
 template <class S, class D>
-__global__ void k_convert(const S *__restrict__ src, Layout Ls, D *__restrict__ dst, Layout Ld, int nx) {
-  const int y = blockIdx.x, z = blockIdx.y;
-  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) dst[Ld.index(x, y, z)] = (D)src[Ls.index(x, y, z)];
+__global__ void __launch_bounds__(32 * kRowWarps) k_convert(const S *__restrict__ src, Layout Ls, D *__restrict__ dst,
+                                                            Layout Ld, int nx, int ny, int nz) {
+  const long long r = (long long)blockIdx.x * kRowWarps + (threadIdx.x >> 5);
+  if (r >= (long long)(ny + 2) * (nz + 2)) return;
+  const int y = (int)(r % (ny + 2)), z = (int)(r / (ny + 2));
+  const long long is = Ls.index(0, y, z), id = Ld.index(0, y, z);
+#pragma unroll 4
+  for (int x = threadIdx.x & 31; x < nx + 2; x += 32) dst[id + x] = (D)src[is + x];
+}
+
+inline unsigned row_blocks(const pdfs_grid &g) {
+  return (unsigned)(((long long)(g.ny + 2) * (g.nz + 2) + kRowWarps - 1) / kRowWarps);
 }
 
 // Every element of a z-column (ZC) working field, in column order: the
@@ -176,19 +188,22 @@ __global__ void k_zc_fill(T *__restrict__ dst, Layout Ld, const double *__restri
 
 // FP32 working field -> FP64 working field (polish start): frozen nodes and
 // the halo keep the exact FP64 input.
-__global__ void k_widen(const float *__restrict__ u32, Layout L32, const double *__restrict__ in64,
-                        double *__restrict__ u64, Layout L64, const uint32_t *__restrict__ fmask, MaskLayout M,
-                        int nx, int ny, int nz) {
-  const int y = blockIdx.x, z = blockIdx.y;
-  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
-    const long long i64 = L64.index(x, y, z);
-    const bool interior = x >= 1 && x <= nx && y >= 1 && y <= ny && z >= 1 && z <= nz;
+__global__ void __launch_bounds__(32 * kRowWarps) k_widen(const float *__restrict__ u32, Layout L32,
+                                                          const double *__restrict__ in64, double *__restrict__ u64,
+                                                          Layout L64, const uint32_t *__restrict__ fmask, MaskLayout M,
+                                                          int nx, int ny, int nz) {
+  const long long r = (long long)blockIdx.x * kRowWarps + (threadIdx.x >> 5);
+  if (r >= (long long)(ny + 2) * (nz + 2)) return;
+  const int y = (int)(r % (ny + 2)), z = (int)(r / (ny + 2));
+  const bool irow = y >= 1 && y <= ny && z >= 1 && z <= nz;
+  const long long i32 = L32.index(0, y, z), i64 = L64.index(0, y, z);
+#pragma unroll 4
+  for (int x = threadIdx.x & 31; x < nx + 2; x += 32) {
+    const float v = u32[i32 + x];
+    const bool interior = irow && x >= 1 && x <= nx;
     bool frz = !interior;
-    if (interior && fmask) {
-      const uint32_t w = fmask[M.word(x, y, z)];
-      frz = (w >> ((x - 1) & 31)) & 1u;
-    }
-    u64[i64] = frz ? in64[i64] : (double)u32[L32.index(x, y, z)];
+    if (interior && fmask) frz = (__ldg(fmask + M.word(x, y, z)) >> ((x - 1) & 31)) & 1u;
+    u64[i64 + x] = frz ? in64[i64 + x] : (double)v;
   }
 }
 
@@ -203,19 +218,23 @@ __global__ void k_to_pair(const double *__restrict__ src, double *__restrict__ d
 
 // FP32 working field -> pair working field (polish start): (u32, 0) for the
 // nodes the sweeps update, the input's nearest pair for frozen nodes and the halo
-__global__ void k_widen_pair(const float *__restrict__ u32, Layout L32, const double *__restrict__ in64,
-                             double *__restrict__ u64, Layout L64, const uint32_t *__restrict__ fmask, MaskLayout M,
-                             int nx, int ny, int nz) {
-  const int y = blockIdx.x, z = blockIdx.y;
-  for (int x = threadIdx.x; x < nx + 2; x += blockDim.x) {
-    const long long i64 = L64.index(x, y, z);
-    const bool interior = x >= 1 && x <= nx && y >= 1 && y <= ny && z >= 1 && z <= nz;
+__global__ void __launch_bounds__(32 * kRowWarps) k_widen_pair(const float *__restrict__ u32, Layout L32,
+                                                               const double *__restrict__ in64,
+                                                               double *__restrict__ u64, Layout L64,
+                                                               const uint32_t *__restrict__ fmask, MaskLayout M,
+                                                               int nx, int ny, int nz) {
+  const long long r = (long long)blockIdx.x * kRowWarps + (threadIdx.x >> 5);
+  if (r >= (long long)(ny + 2) * (nz + 2)) return;
+  const int y = (int)(r % (ny + 2)), z = (int)(r / (ny + 2));
+  const bool irow = y >= 1 && y <= ny && z >= 1 && z <= nz;
+  const long long i32 = L32.index(0, y, z), i64 = L64.index(0, y, z);
+#pragma unroll 4
+  for (int x = threadIdx.x & 31; x < nx + 2; x += 32) {
+    const float v = u32[i32 + x];
+    const bool interior = irow && x >= 1 && x <= nx;
     bool frz = !interior;
-    if (interior && fmask) {
-      const uint32_t w = fmask[M.word(x, y, z)];
-      frz = (w >> ((x - 1) & 31)) & 1u;
-    }
-    u64[i64] = frz ? to_pair(in64[i64]) : p_make(u32[L32.index(x, y, z)], 0.0f);
+    if (interior && fmask) frz = (__ldg(fmask + M.word(x, y, z)) >> ((x - 1) & 31)) & 1u;
+    u64[i64 + x] = frz ? to_pair(in64[i64 + x]) : p_make(v, 0.0f);
   }
 }
 
@@ -671,7 +690,8 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   c->oct32_ok = o.precision != PDFS_PREC_FP64 && s32.bz == 32 && s32.ty == 16 && s32.tx == 16;
   c->oct64_ok = o.precision == PDFS_PREC_FP32_POLISH64 && s64.bz == 16 && s64.ty == 16 && s64.tx == 16;
   if (c->oct32_ok || c->oct64_ok) {
-    want(&c->toct, (8 * std::max(bo[0].size(), bo[1].size()) + 17) * 4);
+    want(&c->toct, (size_t)std::max(octant_scratch_ints(c->nt32[0], c->nt32[1], c->nt32[2]),
+                                    octant_scratch_ints(c->nt64[0], c->nt64[1], c->nt64[2])) * 4);
     want(&c->ochg, 16 * 8);
   }
   if (!wb.empty()) {
@@ -1156,15 +1176,15 @@ int pdfs::ctx_fp64_start(pdfs_ctx *c) {  // FP64 working field <- the input
 int pdfs::ctx_widen(pdfs_ctx *c) {
   const pdfs_grid &g = c->g;
   if (c->L64.zc) return zc_fill<double>(c, c->u64, c->L64, true);
-  dim3 grid(g.ny + 2, g.nz + 2);
+  const unsigned grid = row_blocks(g);
   if (c->o.arith == PDFS_ARITH_PAIR) {
-    k_widen_pair<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64,
+    k_widen_pair<<<grid, 32 * kRowWarps, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64,
                                           c->has_mask ? c->fmask : nullptr, c->M, g.nx, g.ny, g.nz);
     c->launches++;
     CK(cudaGetLastError());
     return PDFS_OK;
   }
-  k_widen<<<grid, 128, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64, c->has_mask ? c->fmask : nullptr, c->M,
+  k_widen<<<grid, 32 * kRowWarps, 0, c->st>>>(c->u32, c->L32, c->in64, c->u64, c->L64, c->has_mask ? c->fmask : nullptr, c->M,
                                    g.nx, g.ny, g.nz);
   c->launches++;
   CK(cudaGetLastError());
@@ -1174,8 +1194,8 @@ int pdfs::ctx_widen(pdfs_ctx *c) {
 int pdfs::ctx_narrow(pdfs_ctx *c) {  // FP64 input -> FP32 working field
   const pdfs_grid &g = c->g;
   if (c->L32.zc) return zc_fill<float>(c, c->u32, c->L32, false);
-  dim3 grid(g.ny + 2, g.nz + 2);
-  k_convert<double, float><<<grid, 128, 0, c->st>>>(c->in64, c->L64, c->u32, c->L32, g.nx);
+  k_convert<double, float><<<row_blocks(g), 32 * kRowWarps, 0, c->st>>>(c->in64, c->L64, c->u32, c->L32, g.nx, g.ny,
+                                                                         g.nz);
   c->launches++;
   CK(cudaGetLastError());
   return PDFS_OK;
@@ -1512,7 +1532,7 @@ static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long l
   CK(cudaMemcpyAsync(cnt, cnt_off, sizeof cnt, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   c->kern_ms += ms_between(c->k0, c->k1);
-  c->launches += 6 + (kOctDilate ? 1 : 0);
+  c->launches += 7 + (kOctDilate ? 1 : 0);  // mask, union, nodes, brick bits, tickets, plan, merge, round
   if (c->hstat->err[0]) return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
   *active = 0;
   *updates = 0;

@@ -174,12 +174,90 @@ __global__ void k_oct_tickets(const int *__restrict__ torder, int ntx, int nty, 
   if (tid == nt - 1) cnt[j] = s_sum[tid];
 }
 
-// off[0..8]: prefix sums of the 8 counts (the round's ticket ranges).
-__global__ void k_oct_offsets(const int *__restrict__ cnt, int *__restrict__ off) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
+// The round's ticket order.  Sweep j's brick at wavefront level w (its
+// local x + y + z) gets key T[j] + w; tickets are listed by key, then by
+// sweep, so sweep j + 1 starts at its first corner while sweep j is still
+// finishing elsewhere instead of after all of sweep j.  The host picks T so
+// that every wait is on a smaller key: a brick of sweep j waits for its
+// upwind bricks (key - 1) and for itself and its face neighbours in an
+// earlier sweep j', whose keys are at most T[j'] + w + 1 + the summed extents
+// (bricks - 1) of the axes j' and j sweep in opposite directions.
+struct OctKeys {
+  int T[8];
+};
+
+__device__ __forceinline__ int oct_level(int lt, int ntx, int nty) {
+  return lt % ntx + (lt / ntx) % nty + lt / (ntx * nty);
+}
+
+// One CTA: off[0..8] (prefix sums of the 8 counts), start[j][w] (the first of
+// sweep j's listed tickets at level >= w; the lists are in level order) and
+// base[j][w] (where sweep j's level-w tickets begin in the merged order).
+__global__ void __launch_bounds__(1024) k_oct_plan(const int *__restrict__ lists, const int *__restrict__ cnt,
+                                                   int *__restrict__ off, int ntx, int nty, int ntz, OctKeys K,
+                                                   int *__restrict__ start, int *__restrict__ base) {
+  __shared__ int s_sum[1024];
+  const int n = ntx * nty * ntz, WL = ntx + nty + ntz - 2, tid = threadIdx.x;
+  if (tid == 0) {
     off[0] = 0;
     for (int j = 0; j < 8; ++j) off[j + 1] = off[j] + cnt[j];
   }
+  for (int idx = tid; idx < 8 * (WL + 1); idx += blockDim.x) {
+    const int j = idx / (WL + 1), w = idx % (WL + 1);
+    const int *l = lists + (long long)j * n;
+    int lo = 0, hi = cnt[j];  // first listed ticket with level >= w
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (oct_level(l[mid], ntx, nty) < w)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    start[idx] = lo;
+  }
+  __syncthreads();
+  // cells (key k, sweep j) in order; cell size = sweep j's tickets at level k - T[j]
+  const int ncell = (K.T[7] + WL) * 8;
+  const int per = (ncell + blockDim.x - 1) / blockDim.x, c0 = min(ncell, tid * per), c1 = min(ncell, c0 + per);
+  auto size = [&](int c) {
+    const int j = c & 7, w = (c >> 3) - K.T[j];
+    return (w >= 0 && w < WL) ? start[j * (WL + 1) + w + 1] - start[j * (WL + 1) + w] : 0;
+  };
+  int sum = 0;
+  for (int c = c0; c < c1; ++c) sum += size(c);
+  s_sum[tid] = sum;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+    const int v = tid >= o ? s_sum[tid - o] : 0;
+    __syncthreads();
+    s_sum[tid] += v;
+    __syncthreads();
+  }
+  int pos = s_sum[tid] - sum;
+  for (int c = c0; c < c1; ++c) {
+    const int j = c & 7, w = (c >> 3) - K.T[j];
+    if (w >= 0 && w < WL) base[j * WL + w] = pos;
+    pos += size(c);
+  }
+}
+
+// merged[base[j][w] + i - start[j][w]] = (j << 28) | brick, for sweep j's
+// i-th listed ticket (level w)
+__global__ void k_oct_merge(const int *__restrict__ lists, const int *__restrict__ cnt, int ntx, int nty, int ntz,
+                            const int *__restrict__ start, const int *__restrict__ base, int *__restrict__ merged) {
+  const int n = ntx * nty * ntz, WL = ntx + nty + ntz - 2;
+  for (int j = 0; j < 8; ++j) {
+    const int m = cnt[j];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+      const int lt = lists[(long long)j * n + i], w = oct_level(lt, ntx, nty);
+      merged[base[j * WL + w] + i - start[j * (WL + 1) + w]] = (j << 28) | lt;
+    }
+  }
+}
+
+int octant_scratch_ints(int ntx, int nty, int ntz) {
+  const int n = ntx * nty * ntz, WL = ntx + nty + ntz - 2;
+  return 16 * n + 17 + 8 * (WL + 1) + 8 * WL;
 }
 
 template <class T, int BZ, int MODE, int ARITH, bool ISO>
@@ -216,11 +294,30 @@ cudaError_t launch_octant_round(int which, int arith, bool iso, const SweepArgs 
                                                                   a0.nbx, a0.nby, a0.nbz,
                                                                   const_cast<uint8_t *>(a0.oct_tbits));
   k_oct_tickets<<<8, 1024, 0, st>>>(a0.torder, a0.ntx, a0.nty, a0.ntz, a0.oct_first, a0.oct_tbits, list, cnt_off);
-  k_oct_offsets<<<1, 32, 0, st>>>(cnt_off, cnt_off + 8);
+  // the keys' sweep offsets: T[j] >= T[j'] + 2 + the extents of the axes
+  // sweeps j' and j run in opposite directions, for every j' < j
+  OctKeys K;
+  const int ext[3] = {a0.ntx - 1, a0.nty - 1, a0.ntz - 1};
+  int sg[8][3];
+  for (int j = 0; j < 8; ++j) ordering_signs((a0.oct_first + j) % 8 + 1, &sg[j][0], &sg[j][1], &sg[j][2]);
+  for (int j = 0; j < 8; ++j) {
+    K.T[j] = 0;
+    for (int q = 0; q < j; ++q) {
+      int d = 2;
+      for (int ax = 0; ax < 3; ++ax)
+        if (sg[q][ax] != sg[j][ax]) d += ext[ax];
+      K.T[j] = std::max(K.T[j], K.T[q] + d);
+    }
+  }
+  const int WL = a0.ntx + a0.nty + a0.ntz - 2;
+  int *merged = cnt_off + 17, *start = merged + 8 * (size_t)n, *base = start + 8 * (WL + 1);
+  k_oct_plan<<<1, 1024, 0, st>>>(list, cnt_off, cnt_off + 8, a0.ntx, a0.nty, a0.ntz, K, start, base);
+  k_oct_merge<<<std::max(1, std::min((n + 255) / 256, 4 * sms)), 256, 0, st>>>(list, cnt_off, a0.ntx, a0.nty, a0.ntz,
+                                                                               start, base, merged);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   SweepArgs a = a0;
-  a.torder = list;
+  a.torder = merged;
   a.nticket = cnt_off + 8;
   a.blk_active = nullptr;
   a.tact = nullptr;

@@ -63,15 +63,34 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
+// Column of thread tid when the brick's 16 x BY columns are listed by
+// diagonal d = lx + ly (then by ly).  Column (lx, ly) holds a node of level L
+// for L - lx - ly in [0, BZ), so a warp whose 32 columns span diagonals
+// d0 .. d1 runs the level body on BZ + d1 - d0 levels: BZ + 2 to BZ + 7 for
+// 16 x 16 columns listed by diagonal, BZ + 16 for the row-major warp of two
+// rows (158 against 256 warp-level bodies per 16^3 brick).
+template <int BX, int BY>
+__device__ __forceinline__ int2 diag_column(int tid) {
+  int base = 0;
+#pragma unroll 1
+  for (int d = 0; d <= BX + BY - 2; ++d) {
+    const int lo = d - (BX - 1) > 0 ? d - (BX - 1) : 0, hi = d < BY - 1 ? d : BY - 1;  // ly on diagonal d
+    if (tid < base + hi - lo + 1) return make_int2(d - (lo + tid - base), lo + tid - base);
+    base += hi - lo + 1;
+  }
+  return make_int2(0, 0);
+}
+
 // OCT: an octant round -- the 8 orderings of the polish's first cycle in one
 // launch.  A ticket names (sweep j, brick); ordering (oct_first + j) % 8 + 1
 // visits the bricks and blocks whose bits name it.  Before its box is read, a
 // brick waits until it and its six face neighbours have finished their latest
 // earlier sweep of the round (their values are this sweep's old values), then
 // for its upwind bricks in this sweep as usual.  Flags carry epoch + j, so
-// "finished sweep j" is a flag >= epoch + j; tickets list sweep j's bricks
-// (wavefront order) before sweep j + 1's, so every wait is on a smaller
-// ticket.  The result is the sequential sweeps', bit for bit.
+// "finished sweep j" is a flag >= epoch + j; the ticket list (k_oct_plan,
+// k_oct_merge) interleaves the sweeps by wavefront level with every brick
+// after the ones it waits on, so every wait is on a smaller ticket.  The
+// result is the sequential sweeps', bit for bit.
 template <class T, int BY_, int BZ, int MODE, int ARITH, bool ISO, bool OCT = false>
 __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                             const __grid_constant__ SweepArgs a) {
@@ -92,7 +111,9 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     return;
   }
   const int tid = threadIdx.x, lane = tid & 31;
-  const int lx = tid & (BX - 1), ly = tid / BX;  // brick-local x, y in sweep order
+  // brick-local x, y in sweep order; an octant round orders them by diagonal
+  const int lx = OCT ? diag_column<BX, BY>(tid).x : tid & (BX - 1);
+  const int ly = OCT ? diag_column<BX, BY>(tid).y : tid / BX;
   int sxd = a.sx, syd = a.sy, szd = a.sz;  // OCT: set per ticket
   int gxl = sxd > 0 ? lx : BX - 1 - lx;      // brick-local x, y in grid order
   int gyl = syd > 0 ? ly : BY - 1 - ly;
@@ -132,9 +153,10 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     if (__syncthreads_or(tk >= ntile || s_abort)) break;
     int lt, osw = 0;
     unsigned obit = 0;  // OCT: the ticket's ordering bit
-    if constexpr (OCT) {
-      while (osw < 7 && tk >= a.nticket[osw + 1]) ++osw;
-      lt = a.torder[(long long)osw * ntx * nty * ntz + (tk - a.nticket[osw])];
+    if constexpr (OCT) {  // (sweep << 28) | brick in sweep order
+      const int e = a.torder[tk];
+      osw = e >> 28;
+      lt = e & 0x0fffffff;
       const int sn = (a.oct_first + osw) % 8 + 1;
       obit = 1u << (sn - 1);
       ordering_signs(sn, &sxd, &syd, &szd);
@@ -381,7 +403,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
               u[gbase + (long long)gz * plane] = nv;
               const T d = node_change<T, ARITH>(cv, nv, hmin);
               tmax = vmax_nonneg<T, ARITH>(tmax, d);
-              if (blk_chg) {
+              if (!OCT && blk_chg) {
 #pragma unroll
                 for (int q = 0; q < NZB; ++q)
                   if ((gz >> 3) == q) accb[q] = vmax_nonneg<T, ARITH>(accb[q], d);
@@ -394,8 +416,8 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       __syncthreads();
     }
     // per-block change: lanes of one warp with the same 8^3 block are lx in
-    // [0, 8) or [8, 16) of the warp's two rows
-    if (blk_chg) {
+    // [0, 8) or [8, 16) of the warp's two rows (rounds record none)
+    if (!OCT && blk_chg) {
 #pragma unroll
       for (int q = 0; q < NZB; ++q) {
         T v = accb[q];
