@@ -999,7 +999,8 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
 }
 
 static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg);
-static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates);
+static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates,
+                        bool full);
 int pdfs::ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   return run_sweep(c, which, sn, active, blk_chg, chg);
 }
@@ -1232,9 +1233,10 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
   auto phase = [&](int which, double tol, int *count, double *ms, double *kms) -> int {
     c->kern_ms = 0.0;
     CK(cudaEventRecord(c->e0, c->st));
-    // PDFS_SCHED_OCTANT, FP32 phase: a full first cycle, then cycles as octant
-    // rounds over masks from the field (at most three, until a round's last
-    // two sweeps change by at most 16 x the phase tolerance)
+    // PDFS_SCHED_OCTANT, FP32 phase: the first cycle as one unmasked round (8
+    // full sweeps in one launch), then cycles as octant rounds over masks from
+    // the field (at most three, until a round's last two sweeps change by at
+    // most 16 x the phase tolerance)
     const bool oct32 = o.scheduler == PDFS_SCHED_OCTANT && which == 0 && o.fixed_sweeps == 0 && c->oct32_ok;
     const bool sched = o.scheduler != PDFS_SCHED_NONE && o.scheduler != PDFS_SCHED_OCTANT && o.fixed_sweeps == 0 &&
                        !(polish && which == 2);
@@ -1261,28 +1263,39 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
     int band_sweep = -1;  // learned scheduler: the sweep of the last block-minimum pass
     for (;;) {
       const bool round64 = octant && s == 0 && c->oct64_ok && max_sweeps > 8;
+      const bool full32 = oct32 && s == 0 && max_sweeps >= 8;
       const bool round32 = oct32 && s >= 8 && !oct_done && s + 8 < max_sweeps;
-      if (round64 || round32) {
-        // a cycle of 8 orderings in one launch, each on its octant mask
+      if (round64 || round32 || full32) {
+        // a cycle of 8 orderings in one launch, each on its octant mask (or on
+        // every block)
         double ch8[8];
         long long nb_act = 0, upd = 0;
         const double kms0 = c->kern_ms;
-        int r = octant_round(c, which, (first + s) % 8, ch8, &nb_act, &upd);
+        int r = octant_round(c, which, (first + s) % 8, ch8, &nb_act, &upd, full32);
         if (r) return r;
         const int *nt = which == 0 ? c->nt32 : c->nt64;
         const long long bnodes = (long long)nt[0] * nt[1] * nt[2];
         if (verbose(o))
           for (int j = 0; j < 8; ++j)
-            fprintf(stderr, "pdfs: phase %d sweep %d sn=%d octant change=%.3e (one launch: %.3f ms for 8 sweeps, "
+            fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e (one launch: %.3f ms for 8 sweeps, "
                             "%lld of %lld brick visits)\n",
-                    which, s + j, (first + s + j) % 8 + 1, ch8[j], c->kern_ms - kms0, nb_act, 8 * bnodes);
+                    which, s + j, (first + s + j) % 8 + 1, full32 ? "full round" : "octant", ch8[j],
+                    c->kern_ms - kms0, nb_act, 8 * bnodes);
         st.voxel_updates += upd;
         if (which != 0) st.voxel_updates_fp64 += upd;
+        chg = ch8[7];
+        s += 8;
+        if (full32) {
+          st.full_sweeps += 8;
+          // the sweep-by-sweep phase would have ended at its first sweep within tol
+          bool quiet = false;
+          for (int j = 0; j < 8; ++j) quiet = quiet || ch8[j] <= tol;
+          if (quiet) break;
+          continue;
+        }
         (which == 0 ? st.ms_kern_masked_fp32 : st.ms_kern_masked_fp64) += c->kern_ms - kms0;
         (which == 0 ? st.updates_masked_fp32 : st.updates_masked_fp64) += upd;
         (which == 0 ? st.masked_sweeps_fp32 : st.masked_sweeps_fp64) += 8;
-        chg = ch8[7];
-        s += 8;
         if (round32) {
           ++oct_rounds;
           const bool quiet = std::max(ch8[6], ch8[7]) <= 16.0 * tol;
@@ -1491,15 +1504,24 @@ extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) 
 // min-update (16 x 16 x 32 bricks), 2 = the polish (16 x 16 x 16).  chg: the 8
 // sweeps' max changes; *active: the bricks visited, summed over the 8 sweeps;
 // *updates: the node updates of the active blocks, summed alike.
-static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates) {
+static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates,
+                        bool full) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
-  CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, f32 ? kOctSlack32 : kOctSlack64, INFINITY,
-                 c->nbx, c->nby, c->nbz, c->omask, c->st));
   const uint8_t *bits = c->omask;
-  if (kOctDilate) {
-    CK(octant_union(c->omask, c->bact, c->nbx, c->nby, c->nbz, c->sms, c->st));
+  int kernels = 6;  // nodes, brick bits, tickets, plan, merge, round
+  if (full) {  // every ordering on every block: 8 full sweeps
+    CK(cudaMemsetAsync(c->bact, 0xff, (size_t)c->nblocks, c->st));
     bits = c->bact;
+  } else {
+    CK(octant_mask(c->u32, c->L32, c->has_mask ? c->fmask : nullptr, c->M, g, f32 ? kOctSlack32 : kOctSlack64,
+                   INFINITY, c->nbx, c->nby, c->nbz, c->omask, c->st));
+    ++kernels;
+    if (kOctDilate) {
+      CK(octant_union(c->omask, c->bact, c->nbx, c->nby, c->nbz, c->sms, c->st));
+      bits = c->bact;
+      ++kernels;
+    }
   }
   SweepArgs a;
   fill_sweep_args(c, which, first % 8 + 1, nullptr, nullptr, &a);
@@ -1532,7 +1554,7 @@ static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long l
   CK(cudaMemcpyAsync(cnt, cnt_off, sizeof cnt, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   c->kern_ms += ms_between(c->k0, c->k1);
-  c->launches += 7 + (kOctDilate ? 1 : 0);  // mask, union, nodes, brick bits, tickets, plan, merge, round
+  c->launches += kernels;
   if (c->hstat->err[0]) return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
   *active = 0;
   *updates = 0;
