@@ -80,10 +80,11 @@ enum {
                              last sweep                                                   */
   PDFS_SCHED_LEARNED = 2, /* of the blocks PDFS_SCHED_CHANGE would visit, those the MLP
                              predicts will change                                         */
-  PDFS_SCHED_OCTANT = 3,  /* FP32 and polish phases: after a full first FP32 cycle, each
-                             cycle of 8 orderings runs as one launch over the blocks whose
-                             characteristic directions (from the FP32 field) agree with
-                             each ordering; FP64-only solves sweep every block         */
+  PDFS_SCHED_OCTANT = 3,  /* FP32 and polish phases: the first FP32 cycle runs as one
+                             launch of 8 full sweeps, each later cycle of 8 orderings as
+                             one launch over the blocks whose characteristic directions
+                             (from the FP32 field) agree with each ordering; FP64-only
+                             solves sweep every block                                 */
 };
 /* Whatever the scheduler, a solve only terminates after a sweep that visits
  * every block and changes by at most the phase's tolerance (FP32: the

@@ -92,15 +92,20 @@ cudaError_t encode_pencil_maps(int which, const SweepArgs &a, const Layout &L, C
 // pair min, 2 = pair replace; tiles of rows = 4 or 8 rows.
 cudaError_t launch_sweep_lanecol(int which, int rows, bool iso, const LcArgs &a, int sms, cudaStream_t st,
                                  int *grid_used);
-// A cycle of 8 orderings as one launch on bricks over octant masks (tile3d.cu):
-// which 0 = FP32 min-update (16 x 16 x 32 bricks), 2 = the polish's replace-
-// update (16 x 16 x 16).  a0 as for such a sweep, with oct_first, oct_bits
-// (per block) and oct_tbits (per brick, filled here) set, a0.epoch the first of
-// 8 epochs and a0.maxchg 8 change words; list: 8 x bricks ints, cnt_off: 17 ints.
+// nsw <= kOctMax sweeps (orderings oct_first + 1, ..) as one launch on bricks
+// over octant masks (tile3d.cu): which 0 = FP32 min-update (16 x 16 x 32
+// bricks), 2 = the polish's replace-update (16 x 16 x 16).  a0 as for such a
+// sweep, with oct_first, oct_full (the unmasked sweeps), oct_bits (per block)
+// and oct_tbits (per brick, filled here) set, a0.epoch the first of nsw epochs
+// and a0.maxchg nsw change words; list: the start of the scratch
+// (octant_scratch_ints), cnt_off: list + kOctMax x bricks.
+constexpr int kOctMax = 8;
+// pdfs_ctx::ochg: kOctMax change words, then the node counts of the 8 orderings
+constexpr int kOctWords = kOctMax + 8;
 // ints of an octant round's ticket scratch (pdfs_ctx::toct) for ntx x nty x ntz bricks
 int octant_scratch_ints(int ntx, int nty, int ntz);
-cudaError_t launch_octant_round(int which, int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list,
-                                int *cnt_off, int sms, cudaStream_t st, int *grid_used);
+cudaError_t launch_octant_round(int which, int arith, bool iso, int nsw, const SweepArgs &a0, const Layout &L,
+                                int *list, int *cnt_off, int sms, cudaStream_t st, int *grid_used);
 // Ticket order of bricks: local brick ids (lk * nty + lj) * ntx + li by level li + lj + lk.
 std::vector<int> brick_order(int ntx, int nty, int ntz);
 cudaError_t encode_field_map(CUtensorMap *m, void *base, int esize, const Layout &L, int nplanes, int bx, int by,

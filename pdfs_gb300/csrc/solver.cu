@@ -692,7 +692,7 @@ extern "C" int pdfs_ctx_create(const pdfs_grid *g, const pdfs_opts *o_in, pdfs_c
   if (c->oct32_ok || c->oct64_ok) {
     want(&c->toct, (size_t)std::max(octant_scratch_ints(c->nt32[0], c->nt32[1], c->nt32[2]),
                                     octant_scratch_ints(c->nt64[0], c->nt64[1], c->nt64[2])) * 4);
-    want(&c->ochg, 16 * 8);
+    want(&c->ochg, kOctWords * 8);
   }
   if (!wb.empty()) {
     want(&c->mlp_w, PDFS_MLP_PARAMS * 2);
@@ -999,8 +999,8 @@ void pdfs::fill_sweep_args(const pdfs_ctx *c, int which, int sn, const uint8_t *
 }
 
 static int run_sweep(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg);
-static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates,
-                        bool full);
+static int octant_round(pdfs_ctx *c, int which, int first, int nsw, unsigned full, double *chg, long long *active,
+                        long long *updates);
 int pdfs::ctx_sweep_once(pdfs_ctx *c, int which, int sn, const uint8_t *active, unsigned int *blk_chg, double *chg) {
   return run_sweep(c, which, sn, active, blk_chg, chg);
 }
@@ -1267,24 +1267,28 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
       const bool round32 = oct32 && s >= 8 && !oct_done && s + 8 < max_sweeps;
       if (round64 || round32 || full32) {
         // a cycle of 8 orderings in one launch, each on its octant mask (or on
-        // every block)
-        double ch8[8];
+        // every block).  (The polish's first certifying full sweep run as a
+        // ninth sweep of its round was measured: the round grew by the 6.1 ms
+        // of a full pencil sweep, 72.9 ms either way on the 768^3 grid.)
+        const int nsw = 8;
+        const unsigned full = full32 ? 0xffu : 0u;
+        double ch8[kOctMax];
         long long nb_act = 0, upd = 0;
         const double kms0 = c->kern_ms;
-        int r = octant_round(c, which, (first + s) % 8, ch8, &nb_act, &upd, full32);
+        int r = octant_round(c, which, (first + s) % 8, nsw, full, ch8, &nb_act, &upd);
         if (r) return r;
         const int *nt = which == 0 ? c->nt32 : c->nt64;
         const long long bnodes = (long long)nt[0] * nt[1] * nt[2];
         if (verbose(o))
-          for (int j = 0; j < 8; ++j)
-            fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e (one launch: %.3f ms for 8 sweeps, "
+          for (int j = 0; j < nsw; ++j)
+            fprintf(stderr, "pdfs: phase %d sweep %d sn=%d %s change=%.3e (one launch: %.3f ms for %d sweeps, "
                             "%lld of %lld brick visits)\n",
-                    which, s + j, (first + s + j) % 8 + 1, full32 ? "full round" : "octant", ch8[j],
-                    c->kern_ms - kms0, nb_act, 8 * bnodes);
+                    which, s + j, (first + s + j) % 8 + 1, ((full >> j) & 1u) ? "full, in round" : "octant",
+                    ch8[j], c->kern_ms - kms0, nsw, nb_act, nsw * bnodes);
         st.voxel_updates += upd;
         if (which != 0) st.voxel_updates_fp64 += upd;
-        chg = ch8[7];
-        s += 8;
+        chg = ch8[nsw - 1];
+        s += nsw;
         if (full32) {
           st.full_sweeps += 8;
           // the sweep-by-sweep phase would have ended at its first sweep within tol
@@ -1295,7 +1299,7 @@ extern "C" int pdfs_ctx_run(pdfs_ctx *c, pdfs_stats *stats) {
         }
         (which == 0 ? st.ms_kern_masked_fp32 : st.ms_kern_masked_fp64) += c->kern_ms - kms0;
         (which == 0 ? st.updates_masked_fp32 : st.updates_masked_fp64) += upd;
-        (which == 0 ? st.masked_sweeps_fp32 : st.masked_sweeps_fp64) += 8;
+        (which == 0 ? st.masked_sweeps_fp32 : st.masked_sweeps_fp64) += nsw;
         if (round32) {
           ++oct_rounds;
           const bool quiet = std::max(ch8[6], ch8[7]) <= 16.0 * tol;
@@ -1504,13 +1508,18 @@ extern "C" int pdfs_ctx_blocks(const pdfs_ctx *c, int *nbx, int *nby, int *nbz) 
 // min-update (16 x 16 x 32 bricks), 2 = the polish (16 x 16 x 16).  chg: the 8
 // sweeps' max changes; *active: the bricks visited, summed over the 8 sweeps;
 // *updates: the node updates of the active blocks, summed alike.
-static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long long *active, long long *updates,
-                        bool full) {
+// nsw sweeps (orderings first + 1, first + 2, ..) in one launch: sweep j
+// visits every block when bit j of full is set, else the blocks whose octant
+// masks (computed here from the FP32 field) name its ordering.  chg[j]: sweep
+// j's change; active: tickets run; updates: node updates.
+static int octant_round(pdfs_ctx *c, int which, int first, int nsw, unsigned full, double *chg, long long *active,
+                        long long *updates) {
   const pdfs_grid &g = c->g;
   const bool f32 = which == 0;
   const uint8_t *bits = c->omask;
+  const unsigned every = (1u << nsw) - 1u;
   int kernels = 6;  // nodes, brick bits, tickets, plan, merge, round
-  if (full) {  // every ordering on every block: 8 full sweeps
+  if ((full & every) == every) {  // no sweep reads the masks
     CK(cudaMemsetAsync(c->bact, 0xff, (size_t)c->nblocks, c->st));
     bits = c->bact;
   } else {
@@ -1526,18 +1535,19 @@ static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long l
   SweepArgs a;
   fill_sweep_args(c, which, first % 8 + 1, nullptr, nullptr, &a);
   a.oct_first = first % 8;
+  a.oct_full = full & every;
   a.oct_bits = bits;
   a.oct_tbits = c->tact;
   a.maxchg = c->ochg;
   a.epoch = c->epoch + 1;  // sweep j publishes epoch + j
-  c->epoch += 8;
+  c->epoch += kOctMax;
   const int *nt = f32 ? c->nt32 : c->nt64;
   const int nb = nt[0] * nt[1] * nt[2];
-  int *cnt_off = c->toct + 8 * (size_t)nb;
+  int *cnt_off = c->toct + kOctMax * (size_t)nb;
   CK(cudaMemsetAsync(c->dstat, 0, offsetof(DevStatus, active_blocks), c->st));
-  CK(cudaMemsetAsync(c->ochg, 0, 16 * 8, c->st));  // 8 change words, 8 node counts
+  CK(cudaMemsetAsync(c->ochg, 0, kOctWords * 8, c->st));  // change words, then 8 node counts
   CK(cudaMemsetAsync(c->ticket, 0, 4, c->st));
-  CK(octant_nodes(bits, c->nbx, c->nby, c->nbz, g.nx, g.ny, g.nz, c->ochg + 8, c->sms, c->st));
+  CK(octant_nodes(bits, c->nbx, c->nby, c->nbz, g.nx, g.ny, g.nz, c->ochg + kOctMax, c->sms, c->st));
   const bool iso = g.dx == g.dy && g.dy == g.dz;
   const int arith = c->o.arith == PDFS_ARITH_REFERENCE ? ARITH_REF
                     : c->o.arith == PDFS_ARITH_MIXED   ? ARITH_MIXED
@@ -1545,10 +1555,11 @@ static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long l
                                                        : ARITH_FAST;
   int grid = 0;
   CK(cudaEventRecord(c->k0, c->st));
-  CK(launch_octant_round(which, arith, iso, a, f32 ? c->L32 : c->L64, c->toct, cnt_off, c->sms, c->st, &grid));
+  CK(launch_octant_round(which, arith, iso, nsw, a, f32 ? c->L32 : c->L64, c->toct, cnt_off, c->sms, c->st,
+                         &grid));
   CK(cudaEventRecord(c->k1, c->st));
-  unsigned long long h[16];
-  int cnt[8];
+  unsigned long long h[kOctWords];
+  int cnt[kOctMax];
   CK(cudaMemcpyAsync(c->hstat, c->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(h, c->ochg, sizeof h, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(cnt, cnt_off, sizeof cnt, cudaMemcpyDeviceToHost, c->st));
@@ -1558,8 +1569,10 @@ static int octant_round(pdfs_ctx *c, int which, int first, double chg[8], long l
   if (c->hstat->err[0]) return c->hstat->err[0] == DEV_ERR_TIMEOUT ? PDFS_ERR_TIMEOUT : PDFS_ERR_CUDA;
   *active = 0;
   *updates = 0;
-  for (int j = 0; j < 8; ++j) *updates += (long long)h[8 + (first + j) % 8];  // sweep j runs ordering first + j + 1
-  for (int j = 0; j < 8; ++j) {
+  const long long nodes = (long long)g.nx * g.ny * g.nz;
+  for (int j = 0; j < nsw; ++j)  // sweep j runs ordering first + j + 1
+    *updates += ((full >> j) & 1u) ? nodes : (long long)h[kOctMax + (first + j) % 8];
+  for (int j = 0; j < nsw; ++j) {
     if (f32) {  // float bits in the slot's low word
       const unsigned b32 = (unsigned)h[j];
       float f;

@@ -108,12 +108,13 @@ struct SweepArgs {
   // them in wavefront order, *nticket of them)
   const uint8_t *tact;
   const int *nticket;
-  // an octant round on bricks (tile3d.cuh, OCT): the 8 orderings of the
-  // polish's first cycle in one launch, ordering (oct_first + j) % 8 + 1 for
-  // sweep j; oct_bits: per 8^3 block, bit sn-1 = ordering sn visits it;
-  // oct_tbits: the same per brick (the union of its blocks); torder: [8][ntile]
-  // tickets per sweep, nticket: their 9 prefix offsets
+  // an octant round on bricks (tile3d.cuh, OCT): up to kOctMax sweeps in one
+  // launch, ordering (oct_first + j) % 8 + 1 for sweep j; oct_bits: per 8^3
+  // block, bit sn-1 = ordering sn visits it; oct_tbits: the same per brick
+  // (the union of its blocks); oct_full: bit j = sweep j visits every block;
+  // torder: the merged ticket list ((j << 27) | brick), *nticket of them
   int oct_first;
+  unsigned oct_full;
   const uint8_t *oct_bits;
   const uint8_t *oct_tbits;
 };

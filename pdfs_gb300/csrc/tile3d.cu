@@ -141,18 +141,21 @@ __global__ void k_brick_bits(int ntx, int nty, int ntz, int bx, int by, int bz, 
 }
 
 // Sweep j's tickets (CTA j): the bricks whose bits name ordering
-// (first + j) % 8 + 1, in that ordering's wavefront order, to out[j][...];
-// their count to cnt[j].  The scan keeps the order (as k_brick_compact).
-__global__ void k_oct_tickets(const int *__restrict__ torder, int ntx, int nty, int ntz, int first,
+// (first + j) % 8 + 1 (every brick when bit j of full is set), in that
+// ordering's wavefront order, to out[j][...]; their count to cnt[j].  The
+// scan keeps the order (as k_brick_compact).
+__global__ void k_oct_tickets(const int *__restrict__ torder, int ntx, int nty, int ntz, int first, unsigned full,
                               const uint8_t *__restrict__ tbits, int *__restrict__ out, int *__restrict__ cnt) {
   __shared__ int s_sum[1024];
   const int j = blockIdx.x, n = ntx * nty * ntz, tid = threadIdx.x, nt = blockDim.x;
   const int sn = (first + j) % 8 + 1;
   const unsigned bit = 1u << (sn - 1);
+  const bool all = (full >> j) & 1u;
   int sx, sy, sz;
   ordering_signs(sn, &sx, &sy, &sz);
   const int per = (n + nt - 1) / nt, t0 = min(n, tid * per), t1 = min(n, t0 + per);
   auto active = [&](int tk) {
+    if (all) return true;
     const int lt = torder[tk], li = lt % ntx, lj = (lt / ntx) % nty, lk = lt / (ntx * nty);
     const int bi = sx > 0 ? li : ntx - 1 - li, bj = sy > 0 ? lj : nty - 1 - lj, bk = sz > 0 ? lk : ntz - 1 - lk;
     return (tbits[(bk * nty + bj) * ntx + bi] & bit) != 0;
@@ -183,26 +186,27 @@ __global__ void k_oct_tickets(const int *__restrict__ torder, int ntx, int nty, 
 // earlier sweep j', whose keys are at most T[j'] + w + 1 + the summed extents
 // (bricks - 1) of the axes j' and j sweep in opposite directions.
 struct OctKeys {
-  int T[8];
+  int T[kOctMax];
 };
 
 __device__ __forceinline__ int oct_level(int lt, int ntx, int nty) {
   return lt % ntx + (lt / ntx) % nty + lt / (ntx * nty);
 }
 
-// One CTA: off[0..8] (prefix sums of the 8 counts), start[j][w] (the first of
-// sweep j's listed tickets at level >= w; the lists are in level order) and
-// base[j][w] (where sweep j's level-w tickets begin in the merged order).
+// One CTA: off[0..nsw] (prefix sums of the nsw counts), start[j][w] (the
+// first of sweep j's listed tickets at level >= w; the lists are in level
+// order) and base[j][w] (where sweep j's level-w tickets begin in the merged
+// order).
 __global__ void __launch_bounds__(1024) k_oct_plan(const int *__restrict__ lists, const int *__restrict__ cnt,
-                                                   int *__restrict__ off, int ntx, int nty, int ntz, OctKeys K,
-                                                   int *__restrict__ start, int *__restrict__ base) {
+                                                   int *__restrict__ off, int nsw, int ntx, int nty, int ntz,
+                                                   OctKeys K, int *__restrict__ start, int *__restrict__ base) {
   __shared__ int s_sum[1024];
   const int n = ntx * nty * ntz, WL = ntx + nty + ntz - 2, tid = threadIdx.x;
   if (tid == 0) {
     off[0] = 0;
-    for (int j = 0; j < 8; ++j) off[j + 1] = off[j] + cnt[j];
+    for (int j = 0; j < nsw; ++j) off[j + 1] = off[j] + cnt[j];
   }
-  for (int idx = tid; idx < 8 * (WL + 1); idx += blockDim.x) {
+  for (int idx = tid; idx < nsw * (WL + 1); idx += blockDim.x) {
     const int j = idx / (WL + 1), w = idx % (WL + 1);
     const int *l = lists + (long long)j * n;
     int lo = 0, hi = cnt[j];  // first listed ticket with level >= w
@@ -217,10 +221,10 @@ __global__ void __launch_bounds__(1024) k_oct_plan(const int *__restrict__ lists
   }
   __syncthreads();
   // cells (key k, sweep j) in order; cell size = sweep j's tickets at level k - T[j]
-  const int ncell = (K.T[7] + WL) * 8;
+  const int ncell = (K.T[nsw - 1] + WL) * nsw;
   const int per = (ncell + blockDim.x - 1) / blockDim.x, c0 = min(ncell, tid * per), c1 = min(ncell, c0 + per);
   auto size = [&](int c) {
-    const int j = c & 7, w = (c >> 3) - K.T[j];
+    const int j = c % nsw, w = c / nsw - K.T[j];
     return (w >= 0 && w < WL) ? start[j * (WL + 1) + w + 1] - start[j * (WL + 1) + w] : 0;
   };
   int sum = 0;
@@ -235,29 +239,32 @@ __global__ void __launch_bounds__(1024) k_oct_plan(const int *__restrict__ lists
   }
   int pos = s_sum[tid] - sum;
   for (int c = c0; c < c1; ++c) {
-    const int j = c & 7, w = (c >> 3) - K.T[j];
+    const int j = c % nsw, w = c / nsw - K.T[j];
     if (w >= 0 && w < WL) base[j * WL + w] = pos;
     pos += size(c);
   }
 }
 
-// merged[base[j][w] + i - start[j][w]] = (j << 28) | brick, for sweep j's
+// merged[base[j][w] + i - start[j][w]] = (j << 27) | brick, for sweep j's
 // i-th listed ticket (level w)
-__global__ void k_oct_merge(const int *__restrict__ lists, const int *__restrict__ cnt, int ntx, int nty, int ntz,
-                            const int *__restrict__ start, const int *__restrict__ base, int *__restrict__ merged) {
+__global__ void k_oct_merge(const int *__restrict__ lists, const int *__restrict__ cnt, int nsw, int ntx, int nty,
+                            int ntz, const int *__restrict__ start, const int *__restrict__ base,
+                            int *__restrict__ merged) {
   const int n = ntx * nty * ntz, WL = ntx + nty + ntz - 2;
-  for (int j = 0; j < 8; ++j) {
+  for (int j = 0; j < nsw; ++j) {
     const int m = cnt[j];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
       const int lt = lists[(long long)j * n + i], w = oct_level(lt, ntx, nty);
-      merged[base[j * WL + w] + i - start[j * (WL + 1) + w]] = (j << 28) | lt;
+      merged[base[j * WL + w] + i - start[j * (WL + 1) + w]] = (j << 27) | lt;
     }
   }
 }
 
+// [kOctMax][n] per-sweep lists, kOctMax counts, kOctMax + 1 offsets, the
+// merged list, start [kOctMax][WL + 1], base [kOctMax][WL]
 int octant_scratch_ints(int ntx, int nty, int ntz) {
   const int n = ntx * nty * ntz, WL = ntx + nty + ntz - 2;
-  return 16 * n + 17 + 8 * (WL + 1) + 8 * WL;
+  return 2 * kOctMax * n + 2 * kOctMax + 1 + kOctMax * (WL + 1) + kOctMax * WL;
 }
 
 template <class T, int BZ, int MODE, int ARITH, bool ISO>
@@ -274,33 +281,35 @@ static cudaError_t launch_oct(const SweepArgs &a, const Layout &L, int sms, cuda
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   // every CTA resident: a ticket waits only on smaller tickets
-  int grid = std::min(per_sm * sms, 8 * a.ntx * a.nty * a.ntz);
+  int grid = std::min(per_sm * sms, kOctMax * a.ntx * a.nty * a.ntz);
   if (grid < 1) grid = 1;
   kern<<<grid, G::NT, G::BYTES, st>>>(m, a);
   if (grid_used) *grid_used = grid;
   return cudaGetLastError();
 }
 
-cudaError_t launch_octant_round(int which, int arith, bool iso, const SweepArgs &a0, const Layout &L, int *list,
-                                int *cnt_off, int sms, cudaStream_t st, int *g) {
+cudaError_t launch_octant_round(int which, int arith, bool iso, int nsw, const SweepArgs &a0, const Layout &L,
+                                int *list, int *cnt_off, int sms, cudaStream_t st, int *g) {
   // FP32 min-update rounds on the FP32 masked bricks (16 x 16 x 32), FP64
   // replace-update (polish) rounds on the FP64 ones (16 x 16 x 16)
   const int bz = which == 0 ? 32 : 16;
   if (!a0.tflag || !a0.torder || !a0.oct_bits || !a0.oct_tbits || a0.ntx < 1 || L.ty != 16 || L.tx != 16 ||
-      L.xo != 0 || which == 1 || (which == 2 && (!a0.bcap64 || !a0.bcap32)) || a0.ntz != (a0.nz + bz - 1) / bz)
+      L.xo != 0 || which == 1 || (which == 2 && (!a0.bcap64 || !a0.bcap32)) || a0.ntz != (a0.nz + bz - 1) / bz ||
+      nsw < 1 || nsw > kOctMax || (long long)a0.ntx * a0.nty * a0.ntz >= (1ll << 27))
     return cudaErrorInvalidValue;
   const int n = a0.ntx * a0.nty * a0.ntz;
   k_brick_bits<<<std::min((n + 255) / 256, 4 * sms), 256, 0, st>>>(a0.ntx, a0.nty, a0.ntz, 2, 2, bz / 8, a0.oct_bits,
                                                                   a0.nbx, a0.nby, a0.nbz,
                                                                   const_cast<uint8_t *>(a0.oct_tbits));
-  k_oct_tickets<<<8, 1024, 0, st>>>(a0.torder, a0.ntx, a0.nty, a0.ntz, a0.oct_first, a0.oct_tbits, list, cnt_off);
+  k_oct_tickets<<<nsw, 1024, 0, st>>>(a0.torder, a0.ntx, a0.nty, a0.ntz, a0.oct_first, a0.oct_full, a0.oct_tbits,
+                                      list, cnt_off);
   // the keys' sweep offsets: T[j] >= T[j'] + 2 + the extents of the axes
   // sweeps j' and j run in opposite directions, for every j' < j
   OctKeys K;
   const int ext[3] = {a0.ntx - 1, a0.nty - 1, a0.ntz - 1};
-  int sg[8][3];
-  for (int j = 0; j < 8; ++j) ordering_signs((a0.oct_first + j) % 8 + 1, &sg[j][0], &sg[j][1], &sg[j][2]);
-  for (int j = 0; j < 8; ++j) {
+  int sg[kOctMax][3];
+  for (int j = 0; j < nsw; ++j) ordering_signs((a0.oct_first + j) % 8 + 1, &sg[j][0], &sg[j][1], &sg[j][2]);
+  for (int j = 0; j < nsw; ++j) {
     K.T[j] = 0;
     for (int q = 0; q < j; ++q) {
       int d = 2;
@@ -310,15 +319,16 @@ cudaError_t launch_octant_round(int which, int arith, bool iso, const SweepArgs 
     }
   }
   const int WL = a0.ntx + a0.nty + a0.ntz - 2;
-  int *merged = cnt_off + 17, *start = merged + 8 * (size_t)n, *base = start + 8 * (WL + 1);
-  k_oct_plan<<<1, 1024, 0, st>>>(list, cnt_off, cnt_off + 8, a0.ntx, a0.nty, a0.ntz, K, start, base);
-  k_oct_merge<<<std::max(1, std::min((n + 255) / 256, 4 * sms)), 256, 0, st>>>(list, cnt_off, a0.ntx, a0.nty, a0.ntz,
-                                                                               start, base, merged);
+  int *off = cnt_off + kOctMax, *merged = off + kOctMax + 1;
+  int *start = merged + kOctMax * (size_t)n, *base = start + kOctMax * (WL + 1);
+  k_oct_plan<<<1, 1024, 0, st>>>(list, cnt_off, off, nsw, a0.ntx, a0.nty, a0.ntz, K, start, base);
+  k_oct_merge<<<std::max(1, std::min((n + 255) / 256, 4 * sms)), 256, 0, st>>>(list, cnt_off, nsw, a0.ntx, a0.nty,
+                                                                               a0.ntz, start, base, merged);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   SweepArgs a = a0;
   a.torder = merged;
-  a.nticket = cnt_off + 8;
+  a.nticket = off + nsw;  // the round's ticket count
   a.blk_active = nullptr;
   a.tact = nullptr;
   if (which == 0)

@@ -81,9 +81,11 @@ __device__ __forceinline__ int2 diag_column(int tid) {
   return make_int2(0, 0);
 }
 
-// OCT: an octant round -- the 8 orderings of the polish's first cycle in one
-// launch.  A ticket names (sweep j, brick); ordering (oct_first + j) % 8 + 1
-// visits the bricks and blocks whose bits name it.  Before its box is read, a
+// OCT: an octant round -- up to kOctMax sweeps in one launch (a cycle of the
+// 8 orderings).  A ticket
+// names (sweep j, brick); ordering (oct_first + j) % 8 + 1 visits the bricks
+// and blocks whose bits name it, or every brick when bit j of oct_full is
+// set.  Before its box is read, a
 // brick waits until it and its six face neighbours have finished their latest
 // earlier sweep of the round (their values are this sweep's old values), then
 // for its upwind bricks in this sweep as usual.  Flags carry epoch + j, so
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int ntx = a.ntx, nty = a.nty, ntz = a.ntz;
   // a block-masked sweep takes tickets only for the bricks with an active block
-  const int ntile = OCT ? a.nticket[8] : (a.nticket ? *a.nticket : ntx * nty * ntz);
+  const int ntile = a.nticket ? *a.nticket : ntx * nty * ntz;
   const uint8_t *__restrict__ tact = a.tact;
   const long long plane = a.plane, px = a.px;
   const float hmin = a.hmin;
@@ -152,11 +154,13 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     // also orders every read of s_next before its next write
     if (__syncthreads_or(tk >= ntile || s_abort)) break;
     int lt, osw = 0;
-    unsigned obit = 0;  // OCT: the ticket's ordering bit
-    if constexpr (OCT) {  // (sweep << 28) | brick in sweep order
+    unsigned obit = 0;   // OCT: the ticket's ordering bit
+    bool sfull = false;  // OCT: the ticket's sweep visits every block
+    if constexpr (OCT) {  // (sweep << 27) | brick in sweep order
       const int e = a.torder[tk];
-      osw = e >> 28;
-      lt = e & 0x0fffffff;
+      osw = e >> 27;
+      lt = e & 0x07ffffff;
+      sfull = (a.oct_full >> osw) & 1u;
       const int sn = (a.oct_first + osw) % 8 + 1;
       obit = 1u << (sn - 1);
       ordering_signs(sn, &sxd, &syd, &szd);
@@ -185,7 +189,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
         const int bx = G::NBX * bi + tid % G::NBX, by = G::NBY * bj + (tid / G::NBX) % G::NBY;
         const int bz = bk * NZB + q;
         if (bx < a.nbx && by < a.nby && bz < a.nbz)
-          act = OCT ? (__ldg(a.oct_bits + ((long long)bz * a.nby + by) * a.nbx + bx) & obit) != 0
+          act = OCT ? sfull || (__ldg(a.oct_bits + ((long long)bz * a.nby + by) * a.nbx + bx) & obit) != 0
                     : __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0;
         if (act) {  // the block's planes 8q .. 8q+7 (grid order) in sweep order
           const int lo = szd > 0 ? 8 * q : BZ - 8 * q - 8;
@@ -221,7 +225,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
         if (n >= 0) {
           const unsigned tb = __ldg(a.oct_tbits + n);
           for (int j = osw - 1; j >= 0 && need < 0; --j)
-            if ((tb >> ((a.oct_first + j) % 8)) & 1u) need = j;
+            if (((a.oct_full >> j) & 1u) || ((tb >> ((a.oct_first + j) % 8)) & 1u)) need = j;
         }
         if (need >= 0 && ld_acquire_gpu(a.tflag + n) < a.epoch + need) {
           const long long t0 = cycles();
@@ -273,7 +277,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
 #pragma unroll
       for (int q = 0; q < NZB; ++q) {
         const int bz = bk * NZB + q;
-        if (bz < a.nbz && (OCT ? (__ldg(a.oct_bits + ((long long)bz * a.nby + by) * a.nbx + bx) & obit) != 0
+        if (bz < a.nbz && (OCT ? sfull || (__ldg(a.oct_bits + ((long long)bz * a.nby + by) * a.nbx + bx) & obit) != 0
                                 : __ldg(blk_active + ((long long)bz * a.nby + by) * a.nbx + bx) != 0))
           actz |= 1u << q;
       }
@@ -298,7 +302,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
       if (tid == 2 && lk > 0) up = tile - szd * ntx * nty;
       // an upwind brick without an active block keeps its values: nothing to wait for
       if constexpr (OCT) {
-        if (up >= 0 && !(__ldg(a.oct_tbits + up) & obit)) up = -1;
+        if (up >= 0 && !sfull && !(__ldg(a.oct_tbits + up) & obit)) up = -1;
       } else {
         if (up >= 0 && tact && !tact[up]) up = -1;
       }
