@@ -92,19 +92,33 @@ def run_fsm(field: np.ndarray, spacing, rounds: int = 1, **kw) -> dict:
     return solve(field, spacing, fixed_sweeps=8 * int(rounds), **kw)
 
 
+def _data_ptr(a, itemsize):
+    """Address of a C-contiguous numpy array, or of a contiguous device tensor
+    (any object with data_ptr(), e.g. a torch CUDA tensor)."""
+    if isinstance(a, np.ndarray):
+        if a.itemsize != itemsize or not a.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous with %d-byte elements" % itemsize)
+        return a.ctypes.data
+    if a.element_size() != itemsize or not a.is_contiguous():
+        raise ValueError("tensors must be contiguous with %d-byte elements" % itemsize)
+    return int(a.data_ptr())
+
+
 def solve_batch(fields, spacings, frozen=None, **kw):
     """Solves many grids in one batched solve (pdfs_solve_batch), in place.
-    Returns the per-grid stats dicts."""
+    Fields (float64) and frozen masks (uint8) are numpy arrays or device
+    tensors.  Returns the per-grid stats dicts."""
     n = len(fields)
     grids = (L.Grid * n)()
     fptr = (C.c_void_p * n)()
     mptr = (C.c_void_p * n)()
     for i, f in enumerate(fields):
-        _check_field(f)
+        if isinstance(f, np.ndarray):
+            _check_field(f)
         g = _grid(f, spacings[i])
         grids[i] = g
-        fptr[i] = f.ctypes.data
-        mptr[i] = frozen[i].ctypes.data if frozen is not None and frozen[i] is not None else None
+        fptr[i] = _data_ptr(f, 8)
+        mptr[i] = _data_ptr(frozen[i], 1) if frozen is not None and frozen[i] is not None else None
     o = make_opts(**kw)
     st = (L.Stats * n)()
     s = L.load().pdfs_solve_batch(n, grids, fptr, mptr if frozen is not None else None, C.byref(o), st)

@@ -291,7 +291,9 @@ static cudaError_t launch_oct(const SweepArgs &a, const Layout &L, int sms, cuda
 cudaError_t launch_octant_round(int which, int arith, bool iso, int nsw, const SweepArgs &a0, const Layout &L,
                                 int *list, int *cnt_off, int sms, cudaStream_t st, int *g) {
   // FP32 min-update rounds on the FP32 masked bricks (16 x 16 x 32), FP64
-  // replace-update (polish) rounds on the FP64 ones (16 x 16 x 16)
+  // replace-update (polish) rounds on the FP64 ones (16 x 16 x 16).  (FP32
+  // rounds on 16^3 bricks, 8 CTAs per SM instead of 4, were measured slower
+  // on the 768^3 grid: full round 22.4 -> 25.9 ms, masked 13.8 -> 15.0 ms.)
   const int bz = which == 0 ? 32 : 16;
   if (!a0.tflag || !a0.torder || !a0.oct_bits || !a0.oct_tbits || a0.ntx < 1 || L.ty != 16 || L.tx != 16 ||
       L.xo != 0 || which == 1 || (which == 2 && (!a0.bcap64 || !a0.bcap32)) || a0.ntz != (a0.nz + bz - 1) / bz ||

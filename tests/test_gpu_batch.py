@@ -41,6 +41,21 @@ def test_batch_fp64_bit_exact_per_grid():
         assert s["sweeps_fp64"] % 8 == 0 and s["status"] == 0
 
 
+def test_batch_device_tensors_equal_host_arrays():
+    """Fields and masks handed over as device tensors (the inputs already in
+    HBM): the same bits as host arrays, solved in place on the device."""
+    torch = pytest.importorskip("torch")
+    ws = uneven_batch(9, 21)
+    sps = [(w.dx, w.dy, w.dz) for w in ws]
+    kw = dict(freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64, arith=L.ARITH_PAIR, tol=1e-9)
+    host = [w.field.copy() for w in ws]
+    api.solve_batch(host, sps, frozen=[w.frozen for w in ws], **kw)
+    dev = [torch.from_numpy(w.field).cuda() for w in ws]
+    api.solve_batch(dev, sps, frozen=[torch.from_numpy(w.frozen).cuda() for w in ws], **kw)
+    for h, d in zip(host, dev):
+        assert h.tobytes() == d.cpu().numpy().tobytes()
+
+
 def test_batch_polish_within_tolerance():
     ws = uneven_batch(10, 9)
     fields = [w.field.copy() for w in ws]
