@@ -218,20 +218,20 @@ def kernel_name(kind, tile, prec, arith):
     return "ws_sweep_kernel<%s, %d, %d, %s, %s>" % ((t,) + ty + (mode, ar))
 
 
-def traffic_per_launch(kind, prec, nodes, tile, masked=False):
+def traffic_per_launch(kind, prec, nodes, tile, masked=False, full_round=False):
     """DRAM bytes of one launch of the dominant sweep kernel: the per-update
     traffic an ncu capture measured (profiles/traffic.json, dram__bytes_read
     + dram__bytes_write over the capture's executed voxel updates) times this
     launch's updates; None without a capture for that kernel.  masked: the
     block-masked sweeps (bricks), whose traffic per executed update differs
-    from a full sweep's."""
+    from a full sweep's; full_round: the FP32 first cycle as one unmasked round."""
     from pdfs_gb300 import _lib as L
     try:
         t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     except (OSError, ValueError):
         return None
     key = "fp32" if kind == "fp32" else ("fp64_replace" if prec == L.PREC_FP32_POLISH64 else "fp64_min")
-    key += "_masked_brick" if masked else "_" + kernel_kind(kind, tile)
+    key += "_masked_brick" if masked else ("_round" if full_round else "_" + kernel_kind(kind, tile))
     e = t.get(key)
     return None if not e else float(e["dram_bytes_per_update"]) * nodes
 
@@ -638,7 +638,7 @@ def main():
     if dom is not None:
         # traffic: ncu DRAM bytes per update of this kernel (profiles/traffic.json) x its updates per launch
         tr = traffic_per_launch(dom["phase"], prec, dom["updates"] / dom["launches"], st["tile"],
-                                masked=dom["kind"] == "masked")
+                                masked=dom["kind"] == "masked", full_round=bool(dom.get("full_round")))
         roof = {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": hbm, "unit": "GB/s", "frac": dom["frac"],
                 "traffic": tr, "kernel": dom["kernel"],
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s",
