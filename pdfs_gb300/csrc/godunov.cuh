@@ -266,16 +266,26 @@ __device__ __forceinline__ double p_add(double b, float x) {
 // FP32-pair field, FP32 increment: god_mixed64's scheme with the base, the
 // minima and the result in pairs.  The differences to the base and the
 // final sum run on the FP32 pipe, so no FP64 instruction is left.
+//
+// The three pairwise differences are formed first, all at once, and the
+// base and the differences to it are chosen from their signs: for
+// normalised pairs the sign of p_sub(a, b) is the sign of a - b (a tie gives
+// 0, two infinite minima NaN, which counts as a tie), so the base and the
+// increments are the ones an exact comparison would pick, with the choice
+// no longer ahead of the subtractions on the update's dependency chain.
 template <bool ISO>
 __device__ __forceinline__ double god_pair(double m0, double m1, double m2, const GodConst32 &k) {
-  const bool b0 = !p_lt(m1, m0) && !p_lt(m2, m0);  // which axis holds the base
-  const bool b1 = !b0 && !p_lt(m2, m1);
+  const float d10 = p_sub(m1, m0), d20 = p_sub(m2, m0), d21 = p_sub(m2, m1);
+  const bool b0 = !(d10 < 0.0f) && !(d20 < 0.0f);  // which axis holds the base
+  const bool b1 = !b0 && !(d21 < 0.0f);
   const double base = b0 ? m0 : (b1 ? m1 : m2);
-  if (!(p_hi(base) < INFINITY)) return base;  // no finite neighbour
-  const double pa = b0 ? m1 : m0, pb = (b0 || b1) ? m2 : m1;
-  const float ea = p_sub(pa, base), eb = p_sub(pb, base);
-  const float e0 = b0 ? 0.0f : ea, e1 = b0 ? ea : (b1 ? 0.0f : eb), e2 = (b0 || b1) ? eb : 0.0f;
-  return p_add(base, god32s<ISO>(e0, e1, e2, k));
+  // increments above the base, in axis order (the base's own is 0);
+  // 0 - d is p_sub with the operands swapped, signed zeros included
+  const float e0 = b0 ? 0.0f : (b1 ? __fsub_rn(0.0f, d10) : __fsub_rn(0.0f, d20));
+  const float e1 = b0 ? d10 : (b1 ? 0.0f : __fsub_rn(0.0f, d21));
+  const float e2 = b0 ? d20 : (b1 ? d21 : 0.0f);
+  const double g = p_add(base, god32s<ISO>(e0, e1, e2, k));
+  return p_hi(base) < INFINITY ? g : base;  // no finite neighbour: the base
 }
 
 }  // namespace pdfs
