@@ -141,64 +141,100 @@ __global__ void __launch_bounds__(256) k_octant_mask(const float *__restrict__ u
   }
 }
 
-// The same masks from a shared-memory copy of the field: one CTA per
-// 16 x 16 x 8 region (2 x 2 blocks), its box with a one-node halo fetched by
-// one TMA copy, thread (lx, ly) walking its column's 8 planes.  For the
-// layouts whose interior x starts 16-byte aligned (pencils, bricks).
+// The same masks from shared-memory copies of the field: one CTA per
+// 16 x 16 column of 2 x 2 blocks and kOmChunks blocks along z, each block's
+// box (one-node halo) fetched by one TMA copy into one of two buffers, the
+// next box in flight while a block is evaluated; thread (lx, ly) walks its
+// column's 8 planes of each block.  For the layouts whose interior x starts
+// 16-byte aligned (pencils, bricks).
 constexpr int kOmW = 20, kOmRY = 18, kOmRZ = 10;  // box: x0-1 .. x0+16 rounded to 16 bytes, y0-1 .. y0+16, z0-1 .. z0+8
+constexpr int kOmChunks = 4;
+// floats of one buffer: the box rounded up to 128 bytes (TMA destinations are 128-byte aligned)
+constexpr int kOmBuf = (kOmRZ * kOmRY * kOmW * 4 + 127) / 128 * 32;
 __global__ void __launch_bounds__(256) k_octant_mask_tma(const __grid_constant__ CUtensorMap tm, const uint32_t *__restrict__ fmask,
                                                          MaskLayout M, int nx, int ny, int nz, float hx, float hy,
                                                          float hz, float slack, float far, int nbx, int nby, int nbz,
                                                          uint8_t *__restrict__ omask) {
-  __shared__ __align__(128) float box[kOmRZ][kOmRY][kOmW];
-  __shared__ __align__(8) uint64_t bar;
+  __shared__ __align__(128) float sbox[2][kOmBuf];
+  __shared__ __align__(8) uint64_t bar[2];
   __shared__ unsigned s_c[4];
   const int nrx = (nbx + 1) / 2, nry = (nby + 1) / 2;
-  const int rx = (int)(blockIdx.x % nrx), ry = (int)((blockIdx.x / nrx) % nry), bz = (int)(blockIdx.x / ((long long)nrx * nry));
+  const int rx = (int)(blockIdx.x % nrx), ry = (int)((blockIdx.x / nrx) % nry);
+  const int bz0 = kOmChunks * (int)(blockIdx.x / ((long long)nrx * nry));
+  const int nch = min(kOmChunks, nbz - bz0);
   const int tid = threadIdx.x, lx = tid & 15, ly = tid >> 4, lane = tid & 31;
-  const int x0 = 1 + 16 * rx, y0 = 1 + 16 * ry, z0 = 1 + 8 * bz;
+  const int x0 = 1 + 16 * rx, y0 = 1 + 16 * ry;
+  constexpr unsigned kBox = (unsigned)(sizeof(float) * kOmRZ * kOmRY * kOmW);
+  static_assert((kOmBuf * 4) % 128 == 0 && kOmBuf * 4 >= (int)kBox, "buffer size");
+  auto box = [&](int b, int k, int r, int xx) { return sbox[b][(k * kOmRY + r) * kOmW + xx]; };
   if (tid < 4) s_c[tid] = 0u;
   if (tid == 0) {
-    mbar_init(&bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     mbar_fence_init();
   }
   __syncthreads();
-  if (tid == 0) {
-    mbar_arrive_tx(&bar, (unsigned)sizeof(box));
-    tma_load_3d(&box[0][0][0], &tm, x0 - 1, y0 - 1, z0 - 1, &bar);
-  }
-  // bounded wait for the copy; on expiry every ordering is kept (always safe)
-  bool landed = mbar_try(&bar, 0);
-  if (!landed) {
-    const long long t0 = clock64();
-    while (!(landed = mbar_try(&bar, 0)) && clock64() - t0 < 4000000000ll) {
+  int last[2] = {-1, -1};  // thread 0: the last block copied into each buffer
+  if (tid == 0)
+    for (int c = 0; c < min(2, nch); ++c) {
+      mbar_arrive_tx(&bar[c], kBox);
+      tma_load_3d(&sbox[c][0], &tm, x0 - 1, y0 - 1, 8 * (bz0 + c), &bar[c]);
+      last[c] = c;
     }
-  }
   const int x = x0 + lx, y = y0 + ly;
-  unsigned acc = 0;  // the orderings my nodes accept
-  if (landed && x <= nx && y <= ny) {
-    const int z1 = min(nz, z0 + 7);
-    for (int z = z0; z <= z1; ++z) {
-      const int k = z - z0 + 1;
-      if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
-      const float c = fabsf(box[k][ly + 1][lx + 1]);
-      if (!(c < far)) continue;
-      acc |= octant_orderings(
-          octant_axis(c, fabsf(box[k][ly + 1][lx]), fabsf(box[k][ly + 1][lx + 2]), slack * hx),
-          octant_axis(c, fabsf(box[k][ly][lx + 1]), fabsf(box[k][ly + 2][lx + 1]), slack * hy),
-          octant_axis(c, fabsf(box[k - 1][ly + 1][lx + 1]), fabsf(box[k + 1][ly + 1][lx + 1]), slack * hz));
+  bool ok = true;  // every copy so far landed
+  for (int c = 0; c < nch; ++c) {
+    const int b = c & 1, bz = bz0 + c, z0 = 1 + 8 * bz;
+    // bounded wait for the copy; on expiry every ordering is kept (always safe)
+    bool landed = ok && mbar_try(&bar[b], (c >> 1) & 1);
+    if (ok && !landed) {
+      const long long t0 = clock64();
+      while (!(landed = mbar_try(&bar[b], (c >> 1) & 1)) && clock64() - t0 < 4000000000ll) {
+      }
     }
-  }
-  // the 4 blocks: lanes 0-7 and 16-23 of a warp (rows 2w, 2w + 1) hold x block
-  // 2 rx, lanes 8-15 and 24-31 x block 2 rx + 1; both rows are in y block ly / 8
+    ok = landed;
+    unsigned acc = 0;  // the orderings my nodes accept
+    if (landed && x <= nx && y <= ny) {
+      const int z1 = min(nz, z0 + 7);
+      for (int z = z0; z <= z1; ++z) {
+        const int k = z - z0 + 1;
+        if (fmask && ((fmask[M.word(x, y, z)] >> ((x - 1) & 31)) & 1u)) continue;
+        const float cc = fabsf(box(b, k, ly + 1, lx + 1));
+        if (!(cc < far)) continue;
+        acc |= octant_orderings(
+            octant_axis(cc, fabsf(box(b, k, ly + 1, lx)), fabsf(box(b, k, ly + 1, lx + 2)), slack * hx),
+            octant_axis(cc, fabsf(box(b, k, ly, lx + 1)), fabsf(box(b, k, ly + 2, lx + 1)), slack * hy),
+            octant_axis(cc, fabsf(box(b, k - 1, ly + 1, lx + 1)), fabsf(box(b, k + 1, ly + 1, lx + 1)), slack * hz));
+      }
+    }
+    // the 4 blocks: lanes 0-7 and 16-23 of a warp (rows 2w, 2w + 1) hold x block
+    // 2 rx, lanes 8-15 and 24-31 x block 2 rx + 1; both rows are in y block ly / 8
 #pragma unroll
-  for (int off = 1; off <= 16; off <<= 1)
-    if (off != 8) acc |= __shfl_xor_sync(0xffffffffu, acc, off);
-  if ((lane & 23) == 0 && acc) atomicOr(&s_c[((ly >> 3) << 1) | (lane >> 3)], acc);
-  __syncthreads();
-  if (tid < 4) {
-    const int bx = 2 * rx + (tid & 1), by = 2 * ry + (tid >> 1);
-    if (bx < nbx && by < nby) omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)(landed ? s_c[tid] : 0xffu);
+    for (int off = 1; off <= 16; off <<= 1)
+      if (off != 8) acc |= __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((lane & 23) == 0 && acc) atomicOr(&s_c[((ly >> 3) << 1) | (lane >> 3)], acc);
+    __syncthreads();  // the box is read and the block sums are complete
+    if (tid < 4) {
+      const int bx = 2 * rx + (tid & 1), by = 2 * ry + (tid >> 1);
+      if (bx < nbx && by < nby) omask[((long long)bz * nby + by) * nbx + bx] = (uint8_t)(landed ? s_c[tid] : 0xffu);
+      s_c[tid] = 0u;
+    }
+    if (tid == 0 && ok && c + 2 < nch) {  // the buffer's next box
+      fence_proxy_async();
+      mbar_arrive_tx(&bar[b], kBox);
+      tma_load_3d(&sbox[b][0], &tm, x0 - 1, y0 - 1, 8 * (bz + 2), &bar[b]);
+      last[b] = c + 2;
+    }
+    __syncthreads();  // the sums are reset before the next block's
+  }
+  // a copy that did not land in time is still drained (bounded) before the CTA leaves
+  if (tid == 0 && !ok) {
+    for (int b = 0; b < 2; ++b) {
+      if (last[b] < 0) continue;
+      const long long t0 = clock64();
+      while (!mbar_try(&bar[b], (last[b] >> 1) & 1) && clock64() - t0 < 4000000000ll) {
+      }
+    }
   }
 }
 
@@ -232,7 +268,7 @@ cudaError_t octant_mask(const float *u32, const Layout &L, const uint32_t *fmask
     CUtensorMap m;
     cudaError_t e = encode_field_map(&m, (void *)u32, 4, L, g.nz + 2, kOmW, kOmRY, kOmRZ);
     if (e != cudaSuccess) return e;
-    const long long ctas = (long long)((nbx + 1) / 2) * ((nby + 1) / 2) * nbz;
+    const long long ctas = (long long)((nbx + 1) / 2) * ((nby + 1) / 2) * ((nbz + kOmChunks - 1) / kOmChunks);
     k_octant_mask_tma<<<(unsigned)ctas, 256, 0, st>>>(m, fmask, M, g.nx, g.ny, g.nz, (float)g.dx, (float)g.dy,
                                                       (float)g.dz, slack, far, nbx, nby, nbz, omask);
     return cudaGetLastError();
