@@ -202,7 +202,8 @@ int pdfs_ctx_sweep(pdfs_ctx *c, int sn, const uint8_t *active, float *block_chan
  * updated node of the block, every axis the Godunov update uses has its
  * smaller neighbour on the side ordering sn sweeps from (an axis the update
  * does not use, or whose neighbours differ by at most h/4, accepts both), or
- * where that holds in a face-neighbour block.  These are the masks of the
+ * where that holds in the face-neighbour block ordering sn sweeps into the
+ * block from (along any axis).  These are the masks of the
  * FP32 octant rounds (PDFS_SCHED_OCTANT); the polish's round uses a band of
  * h/20 instead of h/4.  orderings: one byte per block,
  * host or device.  PDFS_ERR_INVALID for a context without an FP32 field. */

@@ -238,8 +238,9 @@ __global__ void __launch_bounds__(256) k_octant_mask_tma(const __grid_constant__
   }
 }
 
-// active[b] = ordering sn matters to block b or to one of its six face
-// neighbours (dilate) ; count receives the number of active blocks.
+// active[b] = ordering sn matters to block b or (dilate) to the face
+// neighbour it sweeps from along some axis; count receives the number of
+// active blocks.
 __global__ void k_octant_active(const uint8_t *__restrict__ omask, int sn, int dilate, uint8_t *__restrict__ active,
                                 int nbx, int nby, int nbz, int *__restrict__ count) {
   const long long n = (long long)nbx * nby * nbz;
@@ -250,9 +251,12 @@ __global__ void k_octant_active(const uint8_t *__restrict__ omask, int sn, int d
     bool on = (omask[b] & bit) != 0;
     if (dilate && !on) {
       const long long pl = (long long)nbx * nby;
-      on = (bx > 0 && (omask[b - 1] & bit)) || (bx < nbx - 1 && (omask[b + 1] & bit)) ||
-           (by > 0 && (omask[b - nbx] & bit)) || (by < nby - 1 && (omask[b + nbx] & bit)) ||
-           (bz > 0 && (omask[b - pl] & bit)) || (bz < nbz - 1 && (omask[b + pl] & bit));
+      int sx, sy, sz;
+      ordering_signs(sn, &sx, &sy, &sz);
+      const int ux = bx - sx, uy = by - sy, uz = bz - sz;  // the upwind neighbour along each axis
+      on = (ux >= 0 && ux < nbx && (omask[b - sx] & bit)) ||
+           (uy >= 0 && uy < nby && (omask[b - (long long)sy * nbx] & bit)) ||
+           (uz >= 0 && uz < nbz && (omask[b - (long long)sz * pl] & bit));
     }
     active[b] = on ? 1 : 0;
     local += on ? 1 : 0;
@@ -279,20 +283,27 @@ cudaError_t octant_mask(const float *u32, const Layout &L, const uint32_t *fmask
   return cudaGetLastError();
 }
 
-// out[b] = omask of block b | omask of its six face neighbours (the widened
-// masks that octant_active(dilate = 1) applies one ordering at a time).
+// out[b] = omask of block b, widened: ordering sn also where it matters to the
+// face neighbour that sn sweeps into b from (the lower-x neighbour for an
+// ordering that sweeps +x, ...) -- the characteristics that cross the face
+// into b.  octant_active(dilate = 1) applies the same rule one ordering at a
+// time.  (Widening by all six neighbours' masks, whatever the direction: the
+// 768^3 octant solve took 70.8 ms against 69.0, with the same sweeps.)
 __global__ void k_octant_union(const uint8_t *__restrict__ omask, uint8_t *__restrict__ out, int nbx, int nby,
                                int nbz) {
   const long long n = (long long)nbx * nby * nbz, pl = (long long)nbx * nby;
   for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n; b += (long long)gridDim.x * blockDim.x) {
     const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / pl);
+    constexpr unsigned XP = orderings_along(0, 1), XM = orderings_along(0, -1);
+    constexpr unsigned YP = orderings_along(1, 1), YM = orderings_along(1, -1);
+    constexpr unsigned ZP = orderings_along(2, 1), ZM = orderings_along(2, -1);
     unsigned m = omask[b];
-    if (bx > 0) m |= omask[b - 1];
-    if (bx < nbx - 1) m |= omask[b + 1];
-    if (by > 0) m |= omask[b - nbx];
-    if (by < nby - 1) m |= omask[b + nbx];
-    if (bz > 0) m |= omask[b - pl];
-    if (bz < nbz - 1) m |= omask[b + pl];
+    if (bx > 0) m |= omask[b - 1] & XP;
+    if (bx < nbx - 1) m |= omask[b + 1] & XM;
+    if (by > 0) m |= omask[b - nbx] & YP;
+    if (by < nby - 1) m |= omask[b + nbx] & YM;
+    if (bz > 0) m |= omask[b - pl] & ZP;
+    if (bz < nbz - 1) m |= omask[b + pl] & ZM;
     out[b] = (uint8_t)m;
   }
 }

@@ -52,13 +52,15 @@ def orderings_ref(u32, frozen, spacing, widen=True):
     blk = np.bitwise_or.reduce(pad.reshape(nbz, 8, nby, 8, nbx, 8), axis=(1, 3, 5))
     if not widen:
         return blk
+    # ordering sn also where it holds in the face neighbour sn sweeps into the block from
+    up = [np.uint8(sum(1 << (sn - 1) for sn in range(1, 9) if signs(sn)[a] > 0)) for a in range(3)]
     out = blk.copy()
-    out[1:] |= blk[:-1]
-    out[:-1] |= blk[1:]
-    out[:, 1:] |= blk[:, :-1]
-    out[:, :-1] |= blk[:, 1:]
-    out[:, :, 1:] |= blk[:, :, :-1]
-    out[:, :, :-1] |= blk[:, :, 1:]
+    out[:, :, 1:] |= blk[:, :, :-1] & up[0]
+    out[:, :, :-1] |= blk[:, :, 1:] & ~up[0]
+    out[:, 1:] |= blk[:, :-1] & up[1]
+    out[:, :-1] |= blk[:, 1:] & ~up[1]
+    out[1:] |= blk[:-1] & up[2]
+    out[:-1] |= blk[1:] & ~up[2]
     return out
 
 
