@@ -62,6 +62,14 @@ struct T3Geo {
 __device__ __forceinline__ void st_release_gpu(int *p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
+// A brick's completion: the CTA barrier before it orders every thread's
+// stores before thread 0's acquire-release fence at GPU scope, which orders
+// them before the relaxed flag store (the fence-then-relaxed-store pattern of
+// CUTLASS's arrival barriers).
+__device__ __forceinline__ void publish_gpu(int *p, int v) {
+  asm volatile("fence.acq_rel.gpu;\n" ::: "memory");
+  asm volatile("st.relaxed.gpu.global.s32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
 
 // Column of thread tid when the brick's 16 x BY columns are listed by
 // diagonal d = lx + ly (then by ly).  Column (lx, ly) holds a node of level L
@@ -455,10 +463,7 @@ __global__ void __launch_bounds__(16 * BY_) t3_sweep_kernel(const __grid_constan
     // publish: the barrier orders every thread's stores before thread 0's
     // GPU-scope fence, which orders them before the flag
     __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      if (tile != a.poison_col) st_release_gpu(a.tflag + tile, epoch);
-    }
+    if (tid == 0 && tile != a.poison_col) publish_gpu(a.tflag + tile, epoch);
   }
   // the CTA's max change -> the grid's counter (one atomic per warp)
   {
