@@ -179,3 +179,25 @@ def test_octant_scheduler_headline_accuracy():
     assert err <= 1e-6, err
     assert sa["masked_sweeps_fp32"] >= 8 and sa["masked_sweeps_fp64"] == 8
     assert sa["voxel_updates"] < sb["voxel_updates"]
+
+
+@pytest.mark.parametrize("shape", [(12, 200, 30), (150, 9, 40), (40, 36, 300), (16, 16, 16), (5, 3, 7)])
+def test_octant_rounds_on_thin_grids(shape):
+    """Grids one brick thick (or one brick in all) along some axis: the
+    rounds' ticket keys and waits degenerate there (one level per axis), and
+    the solve still ends on a certified fixed point within 1e-6 of the
+    oracle's, with the octant rounds run (FP32 first cycle, FP32 round, polish
+    round) and every wait ending."""
+    nx, ny, nz = shape
+    w = W.random_spheres(nx, ny, nz, 1.0, 1.0, 1.0, 3, 2.0, 9.0, seed=sum(shape) + 5)
+    sp = (w.dx, w.dy, w.dz)
+    a = w.field.copy()
+    st = api.solve(a, sp, frozen=w.frozen, freeze=L.FREEZE_MASK, precision=L.PREC_FP32_POLISH64,
+                   arith=L.ARITH_PAIR, tol=1e-5, scheduler=L.SCHED_OCTANT)
+    ref = w.field.copy()
+    O.solve(ref, sp, tol=1e-12, frozen=w.frozen, threads=8)
+    i = (slice(1, -1),) * 3
+    err = float(np.max(np.abs(a[i] - ref[i]) / np.maximum(np.abs(ref[i]), 1.0)))
+    assert err <= 1e-6, err
+    assert st["masked_sweeps_fp64"] == 8 and st["sweeps_fp32"] >= 8
+
