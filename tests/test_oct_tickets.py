@@ -125,3 +125,34 @@ def test_every_wait_is_on_an_earlier_ticket(n, first, density):
         for t in ups:
             if active(j, t):
                 assert pos[(j, oriented(t, s, n))] < tk
+
+
+def diag_column(tid, bx=16, by=16):
+    """diag_column in tile3d.cuh: thread tid's brick column when the bx x by
+    columns are listed by diagonal lx + ly, then by ly."""
+    base = 0
+    for d in range(bx + by - 1):
+        lo, hi = max(0, d - (bx - 1)), min(d, by - 1)
+        if tid < base + hi - lo + 1:
+            ly = lo + tid - base
+            return d - ly, ly
+        base += hi - lo + 1
+    return 0, 0
+
+
+@pytest.mark.parametrize("bz", [16, 32])
+def test_diagonal_columns(bz):
+    """Every column of a 16 x 16 brick has one thread, and a warp's 32 columns
+    span at most 8 diagonals: its level body runs on bz + 2 .. bz + 7 levels
+    (158 warp-level bodies per 16^3 brick, 286 per 16 x 16 x 32, against 256 and
+    384 for warps of two rows)."""
+    cols = [diag_column(t) for t in range(256)]
+    assert sorted(cols) == sorted((x, y) for x in range(16) for y in range(16))
+    spans = []
+    for w in range(8):
+        d = [x + y for x, y in cols[32 * w:32 * w + 32]]
+        spans.append(max(d) - min(d))
+    assert max(spans) <= 7 and min(spans) >= 2
+    bodies = sum(bz + s for s in spans)
+    assert bodies == {16: 158, 32: 286}[bz]
+    assert bodies < 8 * (bz + 16)
